@@ -1,0 +1,198 @@
+// fair_internal.cuh -- shared declarations of the GB300 AIR hot-path library.
+//
+// Device layout of one matrix (DevCSR): 64-bit row offsets (m+1), 0-based
+// int32 column indices, FP64 master values plus optional FP32/FP16 copies
+// derived from them. The transposed matrix (CSR of A') is a second DevCSR,
+// built on the GPU by a stable counting sort and cached in the handle.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "fair_gpu.h"
+
+namespace fair {
+
+// ---- error plumbing -------------------------------------------------------
+void set_detail(const std::string &s);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define FAIR_CUDA(call)                                                          \
+    do {                                                                         \
+        cudaError_t e__ = (call);                                                \
+        if (e__ != cudaSuccess) return ::fair::cuda_fail(e__, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define FAIR_TRY(call)                    \
+    do {                                  \
+        int s__ = (call);                 \
+        if (s__ != FAIR_OK) return s__;   \
+    } while (0)
+
+// ---- device buffers ---------------------------------------------------------
+// A growable device allocation; grow() keeps nothing of the old contents.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    int grow(size_t need);
+    void release();
+    template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct DevCSR {
+    int32_t m = 0, n = 0;
+    int64_t nnz = 0;
+    int32_t max_row = 0;  // longest row (nonzeros)
+    DevBuf rowptr;        // int64 [m+1]
+    DevBuf col;           // int32 [nnz], 0-based
+    DevBuf v64;           // double [nnz]
+    DevBuf v32;           // float [nnz] (derived, valid if has32)
+    DevBuf v16;           // __half [nnz] (derived, valid if has16)
+    bool has32 = false, has16 = false;
+    void release();
+    bool empty() const { return rowptr.p == nullptr; }
+};
+
+// ---- geometry (geometry.cu) -------------------------------------------------
+struct GeomTables {
+    int kind = 0;  // 0 = parallel beam, 1 = fan beam
+    int N = 0, nth = 0, p = 0;
+    // host-computed tables (libm trig, no fused multiply-add), uploaded
+    DevBuf grid;                 // N+1 grid-line coordinates (x == y)
+    DevBuf cth, sth;             // parallel: cos/sin per angle
+    DevBuf bx0, by0;             // parallel: detector start points per bin
+    DevBuf ax0th, ay0th, aath, abth;  // fan: rotated source and direction per angle
+    DevBuf com, som;             // fan: cos/sin of the ray angle per bin
+    void release();
+};
+int build_geometry(const GeomTables &G, DevCSR &A, cudaStream_t s);
+
+// ---- scans / sparse kernels (sparse.cu) -----------------------------------------
+// Exclusive scan of counts[0..m) into out[0..m] (out[m] = total).
+int scan_counts(const int32_t *counts, int64_t m, int64_t *out, cudaStream_t s);
+int csr_max_row(DevCSR &A, cudaStream_t s);
+int csr_build_transpose(const DevCSR &A, DevCSR &AT, cudaStream_t s);
+// After an upload of 1-based JA: convert to 0-based, validate, find max row.
+int csr_check_upload(DevCSR &A, cudaStream_t s);
+int csr_make_lowprec(DevCSR &A, int prec, cudaStream_t s);
+int csr_scale(DevCSR &A, double c, cudaStream_t s);
+int csr_row_norms(const DevCSR &A, int p, double *d_out, cudaStream_t s);
+int csr_row_dot(const DevCSR &A, int32_t row, const double *d_x, double *d_out, cudaStream_t s);
+int csr_add_mult_row(const DevCSR &A, int32_t row, double c, double *d_w, int bmode,
+                     double lb, double ub, cudaStream_t s);
+
+// y = A x in the requested precision (FP64 vectors for F64; FP32 for F32/F16).
+int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s);
+
+// ---- fused solvers (solvers.cu) -----------------------------------------------
+struct SirtDev {
+    int prec = FAIR_PREC_F64;
+    int32_t m = 0, n = 0;
+    const DevCSR *A = nullptr, *AT = nullptr;
+    const double *b = nullptr;   // m
+    const double *Minv = nullptr;  // m: M diag (weights, FP64)
+    const double *D = nullptr;   // n: D diag (FP64; nullptr = 1)
+    double *x = nullptr;         // n, FP64 master iterate
+    float *x32 = nullptr;        // n, FP32 shadow (F32/F16)
+    void *r = nullptr;           // m residual (double or float)
+    double omg = 1.0;
+    int bmode = 0;  // bit0 = upper bound, bit1 = lower bound
+    double lb = 0.0, ub = 0.0;
+};
+int sirt_weights(const DevCSR &A, const DevCSR &AT, bool sart, double *d_M, double *d_D,
+                 cudaStream_t s);
+int sirt_iterations(const SirtDev &S, int K, cudaStream_t s);
+// Same with CUDA events around each pass; summed pass durations in ms.
+int sirt_iterations_timed(const SirtDev &S, int K, cudaStream_t s, float *ms1, float *ms2);
+int sirt_prepare_shadow(const SirtDev &S, cudaStream_t s);
+
+// Gradient descent and power method pieces (solvers.cu).
+struct GdDev {
+    const DevCSR *A = nullptr, *AT = nullptr;
+    const double *b = nullptr;
+    double *x = nullptr, *xn = nullptr, *r = nullptr;
+    double *partials = nullptr;  // reduction scratch
+    int *flag = nullptr;         // [0] = done, [1] = accepted iterations
+    double step = 0.0;           // rho / sigma^2
+    double tol = 0.0;
+    int bmode = 0;
+    double lb = 0.0, ub = 0.0;
+};
+int gd_run(const GdDev &G, int maxiter, cudaStream_t s);
+int normest_run(const DevCSR &A, const DevCSR &AT, double *d_v, double *d_vn, double *d_w,
+                double *d_partials, int *d_flag, double tol, int maxit, double *sigma,
+                cudaStream_t s);
+int fill_uniform(double *d_v, int64_t n, uint64_t seed, uint64_t ctr, cudaStream_t s);
+
+// Kaczmarz sweep (kaczmarz.cu).
+struct SweepDev {
+    const DevCSR *A = nullptr;
+    const double *b = nullptr, *nrA = nullptr, *cumul = nullptr;
+    double *x = nullptr;
+    const int32_t *ord = nullptr;  // 1-based rows
+    int32_t nord = 0;
+    bool rand_rowprob = false;
+    uint64_t seed = 0, ctr = 0;
+    double omg = 1.0;
+    int bmode = 0;  // bit0 = upper bound, bit1 = lower bound (add_mult_row)
+    double lb = 0.0, ub = 0.0;
+};
+int kaczmarz_sweep(const SweepDev &S, int dir, cudaStream_t s);
+
+// Elementwise vector ops (solvers.cu): op 0: out = a - b; 1: out = a + c*b;
+// 2: out = a / c; 3: out = .5*(a + b). Every operation separately rounded.
+enum { VEC_SUB = 0, VEC_AXPY = 1, VEC_DIV = 2, VEC_MEAN = 3 };
+int vec_op(int op, double *out, const double *a, const double *b, double c, int64_t n,
+           cudaStream_t s);
+int vec_to_f32(const double *a, int64_t n, float *o, cudaStream_t s);
+int vec_to_f64(const float *a, int64_t n, double *o, cudaStream_t s);
+
+// Deterministic reductions (solvers.cu).
+int dev_sumsq_diff(const double *a, const double *b, int64_t n, double *d_partials,
+                   double *d_out, cudaStream_t s);
+int dev_dot(const double *a, const double *b, int64_t n, double *d_partials, double *d_out,
+            cudaStream_t s);
+
+// ---- launch helpers -----------------------------------------------------------
+int sm_count();
+constexpr int kReduceBlocks = 4096;  // partial-sum slots used by reductions (>= any grid)
+
+// ---- project random stream ---------------------------------------------------------
+__host__ __device__ inline uint64_t splitmix64(uint64_t seed, uint64_t k) {
+    uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+__host__ __device__ inline double uniform01(uint64_t seed, uint64_t k) {
+    return (double)(splitmix64(seed, k) >> 11) * 0x1.0p-53;
+}
+
+// gfortran MAX/MIN semantics: the non-NaN argument wins.
+__host__ __device__ inline double fmax_f(double a, double b) { return (b > a || a != a) ? b : a; }
+__host__ __device__ inline double fmin_f(double a, double b) { return (b < a || a != a) ? b : a; }
+
+}  // namespace fair
+
+// The opaque handle behind fair_csr.
+struct fair_csr_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int prec = FAIR_PREC_F64;
+    fair::DevCSR A;   // the matrix
+    fair::DevCSR AT;  // cached transpose
+    bool at_valid = false;
+    // work buffers reused across calls
+    fair::DevBuf w_in, w_out, w_b, w_x, w_x32, w_r, w_M, w_D, w_xn, w_tmp, w_part, w_flag;
+    fair::DevBuf w_ord, w_cumul, w_nrA, w_y;
+    // state of fair_sirt_prepare (device-resident SIRT)
+    bool sirt_ready = false, sirt_sart = false;
+    int sirt_prec = FAIR_PREC_F64;
+    double sirt_omg = 1.0, sirt_lb = 0.0, sirt_ub = 0.0;
+    int sirt_bmode = 0;
+    fair::DevBuf s_M, s_D, s_r, s_x32;
+};

@@ -1,0 +1,43 @@
+/*
+ * fair_gpu_ext.h -- device-resident entry points of the GB300 library.
+ *
+ * These have no counterpart in the reference (which has no device memory):
+ * they run the same kernels as fair_sirt / fair_matvecmul on vectors that
+ * already live in GPU memory, enqueued on the handle's stream without any
+ * host synchronisation, so that callers which keep their data on the GPU
+ * (and the benchmark) can time the iterations alone.
+ */
+#ifndef FAIR_GPU_EXT_H
+#define FAIR_GPU_EXT_H
+
+#include "fair_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Prepare SIRT on the handle: transpose, weights (FP64) and the value copies
+ * of the handle's precision. method is 'cimmino' or 'sart' (AIRMs.f90:1070). */
+int fair_sirt_prepare(fair_csr h, const char *sirt_method, const fair_opts *options);
+
+/* Enqueue K SIRT iterations on device vectors (FP64 b of m entries, FP64 x of
+ * n entries, updated in place). Asynchronous on the handle's stream. */
+int fair_sirt_run_device(fair_csr h, const double *d_b, double *d_x, int32_t K);
+
+/* Same, recording CUDA events around every kernel: on return (synchronised)
+ * ms_pass1 / ms_pass2 hold the summed durations of the residual pass over A
+ * and of the update pass over A'. */
+int fair_sirt_run_device_timed(fair_csr h, const double *d_b, double *d_x, int32_t K,
+                               float *ms_pass1, float *ms_pass2);
+
+/* Kernel launches one fair_sirt_run_device(K) enqueues. */
+int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches);
+
+/* Enqueue one product y = A x (trans = 0) or y = A' x (trans = 1) on device
+ * vectors: FP64 vectors for FAIR_PREC_F64, FP32 vectors otherwise. */
+int fair_spmv_device(fair_csr h, int32_t trans, const void *d_x, void *d_y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FAIR_GPU_EXT_H */

@@ -1,0 +1,917 @@
+/*
+ * fair_oracle.c -- CPU oracle for the AIR reconstruction hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (see fair_oracle.h): a serial FP64 restatement of
+ * the reference Fortran, line by line, used to check the GPU library. Build
+ * with -O2 -ffp-contract=off so that no multiply-add is fused: the reference
+ * built with the default x86-64 gfortran flags rounds every product and sum.
+ *
+ * Parity status: UNPINNED by the reference (no golden vectors exist and the
+ * Fortran cannot be compiled here); pinned by analytic known-answer tests.
+ *
+ * Citations are file:line in the reference project.
+ */
+#include "fair_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static const double PI = 3.141592653589793; /* = 4*atan(1d0), system_generation.f90:4 */
+
+/* gfortran MAX/MIN: the result is the non-NaN argument when one is NaN. */
+static inline double fmax_f(double a, double b) { return (b > a || a != a) ? b : a; }
+static inline double fmin_f(double a, double b) { return (b < a || a != a) ? b : a; }
+
+/* ------------------------------------------------------------------------- */
+/* Project PRNG: SplitMix64 (Steele, Lea & Flood 2014), one global stream.    */
+/* It stands in for the unseeded Fortran random_number stream; every consumer */
+/* draws from it in the same order as the reference draws from random_number. */
+/* ------------------------------------------------------------------------- */
+static uint64_t g_seed = 0, g_ctr = 0;
+
+void or_random_seed(uint64_t seed) { g_seed = seed; g_ctr = 0; }
+uint64_t or_random_counter(void) { return g_ctr; }
+
+static uint64_t sm64(uint64_t seed, uint64_t k) {
+    uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+double or_random_number(void) {
+    uint64_t z = sm64(g_seed, g_ctr++);
+    return (double)(z >> 11) * 0x1.0p-53; /* uniform on [0,1) */
+}
+
+/* ------------------------------------------------------------------------- */
+/* system_generation.f90                                                     */
+/* ------------------------------------------------------------------------- */
+
+/* linspace, system_generation.f90:17-35: x(i) = c*i + d with d = a - c. */
+void or_linspace(double a, double b, int n, double *x) {
+    double c = (b - a) / (n - 1);
+    double d = a - c;
+    for (int i = 1; i <= n; ++i) x[i - 1] = c * i + d;
+}
+
+/* quicksort, system_generation.f90:37-77 (Hoare partition, middle pivot,
+ * carrying the index permutation). Arrays are addressed 1-based here. */
+static void quicksort1(double *a, int32_t *ind, int f, int l) {
+    double x = a[(f + l) / 2], t;
+    int i = f, j = l, m;
+    for (;;) {
+        while (a[i] < x) i++;
+        while (x < a[j]) j--;
+        if (i >= j) break;
+        t = a[i]; a[i] = a[j]; a[j] = t;
+        m = ind[i]; ind[i] = ind[j]; ind[j] = m;
+        i++;
+        j--;
+    }
+    if (f < i - 1) quicksort1(a, ind, f, i - 1);
+    if (j + 1 < l) quicksort1(a, ind, j + 1, l);
+}
+
+void or_csr_free(or_csr *A) {
+    free(A->IA); free(A->JA); free(A->vA);
+    A->IA = NULL; A->JA = NULL; A->vA = NULL;
+}
+
+/* Work arrays for one ray (sizes n+1 and 2n+2, 1-based addressing). */
+typedef struct {
+    int n;
+    double *x, *y, *tx, *yx, *ty, *xy, *t, *xxy, *yxy, *pxx, *pyy, *txx, *tyy;
+    int32_t *ind;
+} ray_work;
+
+static int ray_work_alloc(ray_work *w, int n) {
+    w->n = n;
+    size_t a1 = (size_t)(n + 2), a2 = (size_t)(2 * n + 3);
+    w->x = calloc(a1, 8); w->y = calloc(a1, 8); w->tx = calloc(a1, 8);
+    w->yx = calloc(a1, 8); w->ty = calloc(a1, 8); w->xy = calloc(a1, 8);
+    w->t = calloc(a2, 8); w->xxy = calloc(a2, 8); w->yxy = calloc(a2, 8);
+    w->pxx = calloc(a2, 8); w->pyy = calloc(a2, 8);
+    w->txx = calloc(a2, 8); w->tyy = calloc(a2, 8);
+    w->ind = calloc(a2, 4);
+    return (w->x && w->y && w->tx && w->yx && w->ty && w->xy && w->t && w->xxy &&
+            w->yxy && w->pxx && w->pyy && w->txx && w->tyy && w->ind) ? 0 : -1;
+}
+
+static void ray_work_free(ray_work *w) {
+    free(w->x); free(w->y); free(w->tx); free(w->yx); free(w->ty); free(w->xy);
+    free(w->t); free(w->xxy); free(w->yxy); free(w->pxx); free(w->pyy);
+    free(w->txx); free(w->tyy); free(w->ind);
+}
+
+/*
+ * One ray of paralleltomo/fanlineartomo: intersections, sort, in-box filter.
+ * system_generation.f90:163-193 (fan) and :357-387 (parallel), identical code.
+ * Returns n_int, the number of in-box points left in txx/tyy (1-based).
+ */
+static int ray_points(ray_work *w, double a, double b, double x0th, double y0th) {
+    const int n = w->n, np = n + 1, nt = 2 * n + 2;
+    for (int k = 1; k <= np; ++k) {
+        w->tx[k] = (w->x[k] - x0th) / a;
+        w->yx[k] = b * w->tx[k] + y0th;
+        w->ty[k] = (w->y[k] - y0th) / b;
+        w->xy[k] = a * w->ty[k] + x0th;
+    }
+    for (int k = 1; k <= np; ++k) {
+        w->t[k] = w->tx[k];       w->t[np + k] = w->ty[k];
+        w->xxy[k] = w->x[k];      w->xxy[np + k] = w->xy[k];
+        w->yxy[k] = w->yx[k];     w->yxy[np + k] = w->y[k];
+    }
+    for (int k = 1; k <= nt; ++k) w->ind[k] = k;
+    quicksort1(w->t, w->ind, 1, nt);
+    for (int k = 1; k <= nt; ++k) {
+        w->pxx[k] = w->xxy[w->ind[k]];
+        w->pyy[k] = w->yxy[w->ind[k]];
+    }
+    const double lo = -.5 * n, hi = .5 * n;
+    int n_int = 0;
+    for (int k = 1; k <= nt; ++k) {
+        if (w->pxx[k] >= lo && w->pxx[k] <= hi && w->pyy[k] >= lo && w->pyy[k] <= hi) {
+            n_int++;
+            w->txx[n_int] = w->pxx[k];
+            w->tyy[n_int] = w->pyy[k];
+        }
+    }
+    return n_int;
+}
+
+/*
+ * Segments of one ray: the "remove double points" loop and the column rule,
+ * system_generation.f90:196-203/:279-297 (fan) and :390-397/:463-482
+ * (parallel). `excluded` is the parallel-beam boundary rule of :393-394.
+ * With vA == NULL only counts. Returns the count, or -1 when a column index
+ * of 0 appears ("++ Something went wrong", :293/:478).
+ */
+static int64_t ray_segments(const ray_work *w, int n_int, int excluded,
+                            int32_t *JA, double *vA) {
+    const int n = w->n;
+    int64_t m = 0;
+    for (int k = 1; k <= n_int - 1; ++k) {
+        double dx = w->txx[k] - w->txx[k + 1];
+        double dy = w->tyy[k] - w->tyy[k + 1];
+        double test_val = sqrt(dx * dx + dy * dy);
+        if (test_val > 1e-10 && !excluded) {
+            if (vA) {
+                vA[m] = test_val;
+                double xm = .5 * (w->txx[k] + w->txx[k + 1] + n);
+                double ym = .5 * (w->tyy[k] + w->tyy[k + 1] + n);
+                int32_t ja = (int32_t)floor(xm) * n + (n - (int32_t)floor(ym));
+                if (ja == 0) return -1;
+                JA[m] = ja;
+            }
+            m++;
+        }
+    }
+    return m;
+}
+
+/* Shared two-pass CSR build: count pass, then fill pass (:143-212/:221-302). */
+typedef void (*ray_param_fn)(void *ctx, int i, int j, double *a, double *b,
+                             double *x0th, double *y0th, int *excluded);
+
+static int build_two_pass(int n, int nth, int p, ray_work *w, ray_param_fn fn,
+                          void *ctx, or_csr *A) {
+    int64_t m = (int64_t)nth * p;
+    A->IA = calloc((size_t)m + 1, sizeof(int64_t));
+    if (!A->IA) return OR_ERR_ALLOC;
+    A->IA[0] = 0;
+    int64_t nnz = 0;
+    for (int i = 1; i <= nth; ++i) {
+        for (int j = 1; j <= p; ++j) {
+            double a, b, x0th, y0th;
+            int excl;
+            fn(ctx, i, j, &a, &b, &x0th, &y0th, &excl);
+            int n_int = ray_points(w, a, b, x0th, y0th);
+            int64_t c = ray_segments(w, n_int, excl, NULL, NULL);
+            nnz += c;
+            int64_t r = (int64_t)(i - 1) * p + j;
+            A->IA[r] = A->IA[r - 1] + c;
+        }
+    }
+    A->m = (int32_t)m;
+    A->n = n * n;
+    A->nnz = nnz;
+    A->vA = malloc((size_t)(nnz ? nnz : 1) * sizeof(double));
+    A->JA = malloc((size_t)(nnz ? nnz : 1) * sizeof(int32_t));
+    if (!A->vA || !A->JA) return OR_ERR_ALLOC;
+    int64_t count = 0;
+    for (int i = 1; i <= nth; ++i) {
+        for (int j = 1; j <= p; ++j) {
+            double a, b, x0th, y0th;
+            int excl;
+            fn(ctx, i, j, &a, &b, &x0th, &y0th, &excl);
+            int n_int = ray_points(w, a, b, x0th, y0th);
+            int64_t c = ray_segments(w, n_int, excl, A->JA + count, A->vA + count);
+            if (c < 0) return OR_ERR_GEOMETRY;
+            count += c;
+        }
+    }
+    if (count < nnz) return OR_ERR_GEOMETRY; /* "Didn't hit all elements" */
+    return OR_OK;
+}
+
+/* paralleltomo per-ray parameters, system_generation.f90:328-363. */
+typedef struct { int n, p; const double *theta; double *x0, *y0; } par_ctx;
+
+static void par_params(void *vctx, int i, int j, double *a, double *b,
+                       double *x0th, double *y0th, int *excluded) {
+    par_ctx *c = (par_ctx *)vctx;
+    double th = c->theta[i - 1];
+    double ct = cos(th), st = sin(th);
+    *x0th = ct * c->x0[j - 1] - st * c->y0[j - 1];
+    *y0th = st * c->x0[j - 1] + ct * c->y0[j - 1];
+    *a = -st;
+    *b = ct;
+    *excluded = ((*b == 0.0 && fabs(*y0th - .5 * c->n) < 1e-15) ||
+                 (*a == 0.0 && fabs(*x0th - .5 * c->n) < 1e-15));
+}
+
+int or_paralleltomo(int n, int nth, int p, const double *theta, or_csr *A) {
+    memset(A, 0, sizeof(*A));
+    ray_work w;
+    if (ray_work_alloc(&w, n)) return OR_ERR_ALLOC;
+    double *x0 = malloc(sizeof(double) * p), *y0 = malloc(sizeof(double) * p);
+    double d = p - 1;
+    or_linspace(-.5 * d, .5 * d, p, x0);
+    for (int j = 0; j < p; ++j) y0[j] = 0 * x0[j];
+    or_linspace(-.5 * n, .5 * n, n + 1, w.x + 1);
+    for (int k = 1; k <= n + 1; ++k) w.y[k] = w.x[k];
+    par_ctx ctx = {n, p, theta, x0, y0};
+    int st = build_two_pass(n, nth, p, &w, par_params, &ctx, A);
+    free(x0); free(y0);
+    ray_work_free(&w);
+    return st;
+}
+
+/* paralleltomo with the rays split over threads (OpenMP): the same per-ray
+ * code as or_paralleltomo, so the result is identical; used to build large
+ * inputs for the CPU timing only. */
+int or_paralleltomo_mt(int n, int nth, int p, const double *theta, int nthreads, or_csr *A) {
+    memset(A, 0, sizeof(*A));
+    int64_t m = (int64_t)nth * p;
+    double *x0 = malloc(sizeof(double) * p), *y0 = malloc(sizeof(double) * p);
+    double d = p - 1;
+    or_linspace(-.5 * d, .5 * d, p, x0);
+    for (int j = 0; j < p; ++j) y0[j] = 0 * x0[j];
+    double *grid = malloc(sizeof(double) * (n + 1));
+    or_linspace(-.5 * n, .5 * n, n + 1, grid);
+    par_ctx ctx = {n, p, theta, x0, y0};
+    A->IA = calloc((size_t)m + 1, sizeof(int64_t));
+    int64_t *cnt = calloc((size_t)m, sizeof(int64_t));
+    int st = OR_OK;
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel num_threads(nthreads)
+    {
+        ray_work w;
+        ray_work_alloc(&w, n);
+        memcpy(w.x + 1, grid, sizeof(double) * (n + 1));
+        memcpy(w.y + 1, grid, sizeof(double) * (n + 1));
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t r = 0; r < m; ++r) {
+            double a, b, x0th, y0th;
+            int excl;
+            par_params(&ctx, (int)(r / p) + 1, (int)(r % p) + 1, &a, &b, &x0th, &y0th, &excl);
+            int n_int = ray_points(&w, a, b, x0th, y0th);
+            cnt[r] = ray_segments(&w, n_int, excl, NULL, NULL);
+        }
+#pragma omp single
+        {
+            for (int64_t r = 0; r < m; ++r) A->IA[r + 1] = A->IA[r] + cnt[r];
+            A->nnz = A->IA[m];
+            A->vA = malloc(sizeof(double) * (size_t)(A->nnz ? A->nnz : 1));
+            A->JA = malloc(sizeof(int32_t) * (size_t)(A->nnz ? A->nnz : 1));
+        }
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t r = 0; r < m; ++r) {
+            double a, b, x0th, y0th;
+            int excl;
+            par_params(&ctx, (int)(r / p) + 1, (int)(r % p) + 1, &a, &b, &x0th, &y0th, &excl);
+            int n_int = ray_points(&w, a, b, x0th, y0th);
+            int64_t c = ray_segments(&w, n_int, excl, A->JA + A->IA[r], A->vA + A->IA[r]);
+            if (c < 0) {
+#pragma omp atomic write
+                st = OR_ERR_GEOMETRY;
+            }
+        }
+        ray_work_free(&w);
+    }
+    A->m = (int32_t)m;
+    A->n = n * n;
+    free(cnt); free(x0); free(y0); free(grid);
+    return st;
+}
+
+/* fanlineartomo per-ray parameters, system_generation.f90:98-157. */
+typedef struct { double R, x0, y0; const double *theta; double *omega; } fan_ctx;
+
+static void fan_params(void *vctx, int i, int j, double *a, double *b,
+                       double *x0th, double *y0th, int *excluded) {
+    fan_ctx *c = (fan_ctx *)vctx;
+    double th = c->theta[i - 1];
+    double ct = cos(th), st = sin(th);
+    *x0th = ct * c->x0 - st * c->y0;
+    *y0th = st * c->x0 + ct * c->y0;
+    double ath = -*x0th / c->R;
+    double bth = -*y0th / c->R;
+    double om = c->omega[j - 1];
+    *a = cos(om) * ath - sin(om) * bth;
+    *b = sin(om) * ath + cos(om) * bth;
+    *excluded = 0;
+}
+
+/* geometry_fix = 0 reproduces the odd-p ray angles of :122 (offset .5 where
+ * the even branch at :129 has .5*pi); geometry_fix = 1 uses .5*pi for both. */
+int or_fanlineartomo(int n, int nth, int p, double r, double dw, double sd,
+                     const double *theta, int geometry_fix, or_csr *A) {
+    memset(A, 0, sizeof(*A));
+    ray_work w;
+    if (ray_work_alloc(&w, n)) return OR_ERR_ALLOC;
+    double R = r * n, dwn = dw * n, sdn = sd * n;
+    double dew = dwn / p;
+    for (int i = 1; i <= n + 1; ++i) {
+        w.x[i] = i - .5 * n - 1.0;
+        w.y[i] = i - .5 * n - 1.0;
+    }
+    double *omega = malloc(sizeof(double) * p);
+    if (p % 2 == 1) {
+        int h = (p - 1) / 2;
+        for (int i = 1; i <= h; ++i) {
+            double dep = i * dew;
+            omega[h - i] = atan(sdn / dep) - (geometry_fix ? .5 * PI : .5);
+            omega[h + i] = .5 * PI - atan(sdn / dep);
+        }
+        omega[h] = 0.0;
+    } else {
+        int h = p / 2;
+        for (int i = 1; i <= h; ++i) {
+            double dep = (i - .5) * dew;
+            omega[h - i] = atan(sdn / dep) - .5 * PI;
+            omega[h + i - 1] = .5 * PI - atan(sdn / dep);
+        }
+    }
+    fan_ctx ctx = {R, 0.0, R, theta, omega};
+    int st = build_two_pass(n, nth, p, &w, fan_params, &ctx, A);
+    free(omega);
+    ray_work_free(&w);
+    return st;
+}
+
+/* add_white_noise, system_generation.f90:709-745 (Newton inverse normal CDF
+ * on uniforms drawn from the project stream). */
+int or_add_white_noise(int64_t m, const double *b, double eta, double *bt, double *e) {
+    const double tol = 1e-14;
+    for (int64_t k = 0; k < m; ++k) {
+        double u = or_random_number();
+        double x = 0.0;
+        for (int i = 1; i <= 100; ++i) {
+            double f = .5 * (1 + erf(x / sqrt(2.0))) - u;
+            double df = sqrt(2.0 / PI) * exp(-.5 * (x * x));
+            if (fabs(f / df) < tol) break;
+            if (i == 100 && fabs(f / df) > tol) return OR_ERR_NEWTON;
+            x = x - f / df;
+        }
+        e[k] = x;
+    }
+    double nb = 0, ne = 0;
+    for (int64_t k = 0; k < m; ++k) nb += b[k] * b[k];
+    for (int64_t k = 0; k < m; ++k) ne += e[k] * e[k];
+    nb = sqrt(nb);
+    ne = sqrt(ne);
+    double s = eta * nb;
+    for (int64_t k = 0; k < m; ++k) {
+        e[k] = s * e[k] / ne;
+        bt[k] = b[k] + e[k];
+    }
+    return OR_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+/* sparse_matrices.f90                                                       */
+/* ------------------------------------------------------------------------- */
+
+/* csr_matrowvec, sparse_matrices.f90:252-270 (k is 1-based). */
+double or_rowvecmult(const or_csr *A, int k, const double *v) {
+    double f = 0.0;
+    for (int64_t i = A->IA[k - 1]; i < A->IA[k]; ++i) f = f + v[A->JA[i] - 1] * A->vA[i];
+    return f;
+}
+
+/* MMRS, sparse_matrices.f90:349-368 (row-parallel, each row serial). */
+void or_matvecmul(const or_csr *A, const double *v, double *w, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 1) {
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+        for (int k = 1; k <= A->m; ++k) w[k - 1] = or_rowvecmult(A, k, v);
+        return;
+    }
+#endif
+    (void)nthreads;
+    for (int k = 1; k <= A->m; ++k) w[k - 1] = or_rowvecmult(A, k, v);
+}
+
+/* MMCS via sparsetransmul, sparse_matrices.f90:300-347/:370-393, with the
+ * serial scatter order (the shipped OpenMP version of this loop races). */
+void or_transvecmul(const or_csr *A, const double *v, double *w) {
+    memset(w, 0, sizeof(double) * (size_t)A->n);
+    for (int k = 1; k <= A->m; ++k) {
+        for (int64_t i = A->IA[k - 1]; i < A->IA[k]; ++i) {
+            int32_t c = A->JA[i] - 1;
+            w[c] = w[c] + v[k - 1] * A->vA[i];
+        }
+    }
+}
+
+/* reorder, sparse_matrices.f90:492-570: stable counting sort; B is the CSR
+ * form of A^T (B.m = A.n, B.JA holds 1-based row indices of A). */
+int or_reorder(const or_csr *A, or_csr *B) {
+    memset(B, 0, sizeof(*B));
+    int nc = A->n;
+    B->m = A->n;
+    B->n = A->m;
+    B->nnz = A->nnz;
+    B->IA = calloc((size_t)nc + 1, sizeof(int64_t));
+    B->JA = malloc(sizeof(int32_t) * (size_t)(A->nnz ? A->nnz : 1));
+    B->vA = malloc(sizeof(double) * (size_t)(A->nnz ? A->nnz : 1));
+    if (!B->IA || !B->JA || !B->vA) return OR_ERR_ALLOC;
+    for (int64_t i = 0; i < A->nnz; ++i) B->IA[A->JA[i]] += 1;
+    int64_t cumsum = 0;
+    for (int i = 0; i <= nc; ++i) { cumsum += B->IA[i]; B->IA[i] = cumsum; }
+    for (int i = 1; i <= A->m; ++i) {
+        for (int64_t j = A->IA[i - 1]; j < A->IA[i]; ++j) {
+            int col = A->JA[j] - 1;
+            int64_t dest = B->IA[col];
+            B->JA[dest] = i;
+            B->vA[dest] = A->vA[j];
+            B->IA[col] += 1;
+        }
+    }
+    int64_t last = 0;
+    for (int col = 0; col <= nc - 1; ++col) { int64_t t = B->IA[col]; B->IA[col] = last; last = t; }
+    return OR_OK;
+}
+
+/* compute_row_norms, sparse_matrices.f90:740-780. */
+void or_row_norms(const or_csr *A, int p, double *nrA, int nthreads) {
+    (void)nthreads;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads > 1 ? nthreads : 1) schedule(static)
+#endif
+    for (int k = 1; k <= A->m; ++k) {
+        double s = 0.0;
+        for (int64_t i = A->IA[k - 1]; i < A->IA[k]; ++i) {
+            double av = fabs(A->vA[i]);
+            double pw = av;
+            for (int q = 1; q < p; ++q) pw *= av;
+            s = s + pw;
+        }
+        nrA[k - 1] = pow(s, 1.0 / p);
+    }
+}
+
+/* compute_column_norms, sparse_matrices.f90:782-793 (= row norms of A^T). */
+int or_column_norms(const or_csr *A, int p, double *ncA) {
+    or_csr B;
+    int st = or_reorder(A, &B);
+    if (st) return st;
+    or_row_norms(&B, p, ncA, 1);
+    or_csr_free(&B);
+    return OR_OK;
+}
+
+/* add_mult_row, sparse_matrices.f90:795-822: bound only the touched entries,
+ * lower bound first, then upper bound. */
+void or_add_mult_row(const or_csr *A, int k, double c, double *w,
+                     const double *lwrb, const double *upb) {
+    for (int64_t i = A->IA[k - 1]; i < A->IA[k]; ++i) {
+        int32_t j = A->JA[i] - 1;
+        w[j] = w[j] + c * A->vA[i];
+        if (lwrb) w[j] = fmax_f(w[j], *lwrb);
+        if (upb) w[j] = fmin_f(w[j], *upb);
+    }
+}
+
+/* scalar_mult, sparse_matrices.f90:824-831. */
+void or_scalar_mult(or_csr *A, double c) {
+    for (int64_t i = 0; i < A->nnz; ++i) A->vA[i] = c * A->vA[i];
+}
+
+/* ------------------------------------------------------------------------- */
+/* AIRMs.f90                                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* initialise_options, AIRMs.f90:17-37 */
+void or_initialise_options(or_opts *o) {
+    o->upb = 0; o->lwrb = 0; o->ubound = 0.0; o->lbound = 1.0;
+    o->damp = 0.0; o->relaxpar = 1.0; o->verbose = 0; o->rowprobability = 0;
+}
+
+static double norm2v(const double *v, int64_t n) {
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i) s += v[i] * v[i];
+    return sqrt(s);
+}
+
+static double dotv(const double *a, const double *b, int64_t n) {
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+static void apply_box(double *x, int64_t n, int upb, int lwrb, double ub, double lb) {
+    /* AIRMs.f90:1093-1100 / :963-970: upper bound first, then lower bound */
+    if (upb && !lwrb) { for (int64_t j = 0; j < n; ++j) x[j] = fmin_f(x[j], ub); }
+    else if (!upb && lwrb) { for (int64_t j = 0; j < n; ++j) x[j] = fmax_f(x[j], lb); }
+    else if (upb && lwrb) {
+        for (int64_t j = 0; j < n; ++j) { x[j] = fmin_f(x[j], ub); x[j] = fmax_f(x[j], lb); }
+    }
+}
+
+/* sirt, AIRMs.f90:997-1127 */
+int or_sirt(const char *method, const or_csr *A, const double *b, int maxits,
+            const double *x0, const or_opts *o, double *xout, int nthreads) {
+    int upb = 0, lwrb = 0;
+    double ub = 0.0, lb = 1.0, omg = 1.0;
+    if (o) { upb = o->upb; lwrb = o->lwrb; ub = o->ubound; lb = o->lbound; omg = o->relaxpar; }
+    const int64_t m = A->m, n = A->n;
+    double *x = malloc(sizeof(double) * n), *xn = malloc(sizeof(double) * n);
+    double *D = malloc(sizeof(double) * n), *M = malloc(sizeof(double) * m);
+    double *r = malloc(sizeof(double) * m), *g = malloc(sizeof(double) * n);
+    if (!x || !xn || !D || !M || !r || !g) return OR_ERR_ALLOC;
+    for (int64_t j = 0; j < n; ++j) x[j] = x0 ? x0[j] : 0.0;
+    if (!strcmp(method, "cimmino")) {
+        or_row_norms(A, 2, M, nthreads);
+        for (int64_t i = 0; i < m; ++i) M[i] = (double)A->m * (M[i] * M[i]);
+        for (int64_t j = 0; j < n; ++j) D[j] = 1.0;
+    } else if (!strcmp(method, "sart")) {
+        or_row_norms(A, 1, M, nthreads);
+        int st = or_column_norms(A, 1, D);
+        if (st) return st;
+    } else {
+        free(x); free(xn); free(D); free(M); free(r); free(g);
+        return OR_ERR_METHOD; /* "Not a recognised SIRT method." */
+    }
+    for (int it = 1; it <= maxits; ++it) {
+        or_matvecmul(A, x, r, nthreads);
+        for (int64_t i = 0; i < m; ++i) r[i] = (b[i] - r[i]) / M[i];
+        or_transvecmul(A, r, g);
+        for (int64_t j = 0; j < n; ++j) xn[j] = x[j] + omg * g[j] / D[j];
+        apply_box(xn, n, upb, lwrb, ub, lb);
+        memcpy(x, xn, sizeof(double) * n);
+    }
+    memcpy(xout, x, sizeof(double) * n);
+    free(x); free(xn); free(D); free(M); free(r); free(g);
+    return OR_OK;
+}
+
+/* normest, AIRMs.f90:1129-1173, with the start vector v0 given (the
+ * reference draws it with random_number). */
+double or_normest(const or_csr *A, double tol, int maxit, const double *v0, int nthreads) {
+    const int64_t m = A->m, n = A->n;
+    double *v = malloc(sizeof(double) * n), *vn = malloc(sizeof(double) * n);
+    double *w = malloc(sizeof(double) * m), *d = malloc(sizeof(double) * n);
+    memcpy(v, v0, sizeof(double) * n);
+    for (int i = 1; i <= maxit; ++i) {
+        or_matvecmul(A, v, w, nthreads);
+        or_transvecmul(A, w, vn);
+        double s = norm2v(vn, n);
+        for (int64_t j = 0; j < n; ++j) vn[j] = vn[j] / s;
+        for (int64_t j = 0; j < n; ++j) d[j] = vn[j] - v[j];
+        if (norm2v(d, n) < tol) break;
+        memcpy(v, vn, sizeof(double) * n);
+    }
+    or_matvecmul(A, v, w, nthreads);
+    double sigma = sqrt(dotv(w, w, m) / dotv(v, v, n));
+    free(v); free(vn); free(w); free(d);
+    return sigma;
+}
+
+/* gradient_descent, AIRMs.f90:860-995. v0 is normest's start vector, drawn
+ * from the project stream when NULL. */
+int or_gradient_descent(const or_csr *A, const double *b, int max_iter,
+                        const double *x0, double rho, double tol,
+                        const or_opts *o, const double *v0, double *xout,
+                        int *iters_done, int nthreads) {
+    int upb = 0, lwrb = 0;
+    double ub = 0.0, lb = 1.0;
+    if (o) { upb = o->upb; lwrb = o->lwrb; ub = o->ubound; lb = o->lbound; }
+    if (tol < 0.0) return OR_ERR_ARG; /* "Must use positive tolerance." */
+    const int64_t m = A->m, n = A->n;
+    for (int64_t j = 0; j < n; ++j) xout[j] = x0 ? x0[j] : 0.0;
+    double *vs = NULL;
+    if (!v0) {
+        vs = malloc(sizeof(double) * n);
+        for (int64_t j = 0; j < n; ++j) vs[j] = or_random_number();
+        v0 = vs;
+    }
+    double sigma = or_normest(A, 1e-5, 100, v0, nthreads);
+    free(vs);
+    sigma = sigma * sigma;
+    double *r = malloc(sizeof(double) * m), *g = malloc(sizeof(double) * n);
+    double *xn = malloc(sizeof(double) * n), *d = malloc(sizeof(double) * n);
+    for (int64_t i = 0; i < m; ++i) r[i] = -b[i];
+    int it, done = 0;
+    for (it = 1; it <= max_iter; ++it) {
+        or_transvecmul(A, r, g);
+        double s = rho / sigma;
+        for (int64_t j = 0; j < n; ++j) xn[j] = xout[j] - s * g[j];
+        apply_box(xn, n, upb, lwrb, ub, lb);
+        for (int64_t j = 0; j < n; ++j) d[j] = xn[j] - xout[j];
+        if (norm2v(d, n) < tol) break;
+        memcpy(xout, xn, sizeof(double) * n);
+        or_matvecmul(A, xout, r, nthreads);
+        for (int64_t i = 0; i < m; ++i) r[i] = r[i] - b[i];
+        done = it;
+    }
+    if (iters_done) *iters_done = done;
+    free(r); free(g); free(xn); free(d);
+    return OR_OK;
+}
+
+/* scramble, AIRMs.f90:1175-1212: two passes of random swaps over 1..n. */
+void or_scramble(int n, int32_t *arr) {
+    for (int i = 1; i <= n; ++i) arr[i - 1] = i;
+    for (int k = 1; k <= 2; ++k) {
+        for (int i = 1; i <= n; ++i) {
+            double u = or_random_number();
+            int j = 1 + (int)floor(n * u);
+            int32_t t = arr[j - 1];
+            arr[j - 1] = arr[i - 1];
+            arr[i - 1] = t;
+        }
+    }
+}
+
+typedef struct {
+    const or_csr *A;
+    const double *b, *nrA, *cumul;
+    int isrand, rowprob, upb, lwrb;
+    double omg, ub, lb;
+} sweep_ctx;
+
+/* basic_sweep, AIRMs.f90:813-858. ord is 1-based rows; dir = -1 walks it
+ * reversed (the ord(nord:1:-1) actual argument). */
+static void basic_sweep(const sweep_ctx *c, double *x, const int32_t *ord, int nord, int dir) {
+    for (int ii = 1; ii <= nord; ++ii) {
+        int i = dir > 0 ? ord[ii - 1] : ord[nord - ii];
+        int ri;
+        if (c->isrand && c->rowprob) {
+            double u = or_random_number();
+            ri = 1;
+            while (ri < c->A->m && c->cumul[ri - 1] < u) ri++;
+        } else {
+            ri = i;
+        }
+        double inp = or_rowvecmult(c->A, ri, x);
+        double coeff = (c->omg * (c->b[ri - 1] - inp) / c->nrA[ri - 1]);
+        or_add_mult_row(c->A, ri, coeff, x, c->lwrb ? &c->lb : NULL, c->upb ? &c->ub : NULL);
+    }
+}
+
+/* Shared set-up of art and twin_art: AIRMs.f90:217-312 / :525-628. */
+static int art_setup(const char *method, const or_csr *A, const int *Kin, int nK,
+                     const int32_t *order, int nord_in, double dmp, int rowprob,
+                     int *Kuse, int32_t *ord, int *nord_out, double *nrA,
+                     double *cumul, int *isrand, int *issym) {
+    const int m = A->m;
+    int nord;
+    *isrand = 0;
+    *issym = 0;
+    for (int l = 0; l < nK; ++l) Kuse[l] = Kin[l];
+    if (!strcmp(method, "kaczmarz") || !strcmp(method, "symkaczmarz") ||
+        !strcmp(method, "randkaczmarz")) {
+        if (!strcmp(method, "symkaczmarz")) {
+            for (int l = 0; l < nK; ++l) if (Kin[l] % 2 == 1) return OR_ERR_ARG;
+            for (int l = 0; l < nK; ++l) Kuse[l] = Kuse[l] / 2;
+            *issym = 1;
+        }
+        if (!strcmp(method, "randkaczmarz")) *isrand = 1;
+        if (order) { nord = nord_in; for (int i = 0; i < nord; ++i) ord[i] = order[i]; }
+        else { nord = m; for (int i = 0; i < m; ++i) ord[i] = i + 1; }
+    } else {
+        return OR_ERR_METHOD;
+    }
+    or_row_norms(A, 2, nrA, 1);
+    double mx = -INFINITY;
+    for (int i = 0; i < m; ++i) { nrA[i] = nrA[i] * nrA[i]; if (nrA[i] > mx) mx = nrA[i]; }
+    for (int i = 0; i < m; ++i) nrA[i] = nrA[i] + dmp * mx;
+    int l = nord, k = 0;
+    for (int i = 0; i < l; ++i) if (nrA[ord[i] - 1] > 0) ord[k++] = ord[i];
+    nord = k;
+    if (*isrand) {
+        or_scramble(nord, ord);
+        if (rowprob) {
+            double cs = 0;
+            for (int i = 0; i < nord; ++i) { cs = cs + nrA[i]; cumul[i] = cs; }
+            double s = 0;
+            for (int i = 0; i < m; ++i) s += nrA[i];
+            for (int i = 0; i < nord; ++i) cumul[i] = cumul[i] / s;
+            for (int i = nord; i < m; ++i) cumul[i] = 1.0;
+        }
+    }
+    *nord_out = nord;
+    return OR_OK;
+}
+
+/* art, AIRMs.f90:59-369. Xout is n x nK, column-major. */
+int or_art(const char *method, const or_csr *A, const double *b, const int *Kin,
+           int nK, const double *x0, const double *xref, const int32_t *order,
+           int nord_in, const or_opts *o, double *Xout) {
+    const int64_t m = A->m, n = A->n;
+    int upb = 0, lwrb = 0, rowprob = 0;
+    double ub = 0.0, lb = 1.0, dmp = 0.0, omg = 1.0;
+    if (o) {
+        upb = o->upb; lwrb = o->lwrb; ub = o->ubound; lb = o->lbound;
+        dmp = o->damp; omg = o->relaxpar; rowprob = o->rowprobability;
+    }
+    for (int l = 1; l < nK; ++l) if (Kin[l] < Kin[l - 1]) return OR_ERR_ARG;
+    int *Kuse = malloc(sizeof(int) * nK);
+    int32_t *ord = malloc(sizeof(int32_t) * (m + 1));
+    double *nrA = malloc(sizeof(double) * m), *cumul = calloc(m, sizeof(double));
+    double *x = malloc(sizeof(double) * n), *xp = malloc(sizeof(double) * n);
+    double *d = malloc(sizeof(double) * n);
+    int nord, isrand, issym;
+    int st = art_setup(method, A, Kin, nK, order, nord_in, dmp, rowprob, Kuse, ord,
+                       &nord, nrA, cumul, &isrand, &issym);
+    if (st) { free(Kuse); free(ord); free(nrA); free(cumul); free(x); free(xp); free(d); return st; }
+    for (int64_t j = 0; j < n; ++j) x[j] = x0 ? x0[j] : 0.0;
+    memset(Xout, 0, sizeof(double) * n * nK);
+    sweep_ctx c = {A, b, nrA, cumul, isrand, rowprob, upb, lwrb, omg, ub, lb};
+    int maxiter = 0;
+    for (int l = 0; l < nK; ++l) if (Kuse[l] > maxiter) maxiter = Kuse[l];
+    int l = 0;
+    for (int iter = 1; iter <= maxiter; ++iter) {
+        if (isrand) or_scramble(nord, ord);
+        if (xref) memcpy(xp, x, sizeof(double) * n);
+        basic_sweep(&c, x, ord, nord, +1);
+        if (issym) basic_sweep(&c, x, ord, nord, -1);
+        if (xref) {
+            for (int64_t j = 0; j < n; ++j) d[j] = x[j] - xref[j];
+            double e1 = norm2v(d, n);
+            for (int64_t j = 0; j < n; ++j) d[j] = xp[j] - xref[j];
+            double e0 = norm2v(d, n);
+            if (e1 > e0) { memcpy(Xout + (size_t)n * (nK - 1), xp, sizeof(double) * n); break; }
+        }
+        if (l < nK && iter == Kuse[l]) { memcpy(Xout + (size_t)n * l, x, sizeof(double) * n); l++; }
+    }
+    free(Kuse); free(ord); free(nrA); free(cumul); free(x); free(xp); free(d);
+    return OR_OK;
+}
+
+/* twin_art, AIRMs.f90:371-811. Xstore/Ystore are n x nK column-major; EG has
+ * max(Kin) entries. slack < 0 selects the default of 7. */
+int or_twin_art(const char *method, const char *stoprule, const or_csr *A,
+                const double *b, const int *Kin, int nK, const double *x0,
+                const double *y0, const int32_t *order, int nord_in, int slack,
+                const or_opts *o, double *xout, int *final_it, double *Xstore,
+                double *Ystore, double *EG) {
+    const int64_t m = A->m, n = A->n;
+    int slck = slack >= 0 ? slack : 7;
+    int upb = 0, lwrb = 0, rowprob = 0;
+    double ub = 0.0, lb = 1.0, dmp = 0.0, omg = 1.0;
+    if (o) {
+        upb = o->upb; lwrb = o->lwrb; ub = o->ubound; lb = o->lbound;
+        dmp = o->damp; omg = o->relaxpar; rowprob = o->rowprobability;
+    }
+    int eg = !strcmp(stoprule, "errorgauge"), ms = !strcmp(stoprule, "mutualstep");
+    for (int l = 1; l < nK; ++l) if (Kin[l] < Kin[l - 1]) return OR_ERR_ARG;
+    int maxK = 0;
+    for (int l = 0; l < nK; ++l) if (Kin[l] > maxK) maxK = Kin[l];
+    int *Kuse = malloc(sizeof(int) * nK);
+    int32_t *ord = malloc(sizeof(int32_t) * (m + 1));
+    double *nrA = malloc(sizeof(double) * m), *cumul = calloc(m, sizeof(double));
+    int nord, isrand, issym;
+    int st = art_setup(method, A, Kin, nK, order, nord_in, dmp, rowprob, Kuse, ord,
+                       &nord, nrA, cumul, &isrand, &issym);
+    if (!st && !eg && !ms) st = OR_ERR_METHOD;
+    if (st) { free(Kuse); free(ord); free(nrA); free(cumul); return st; }
+    double *x = calloc(n, 8), *y = calloc(n, 8), *v = calloc(n, 8), *w = calloc(n, 8);
+    double *d = calloc(n, 8);
+    sweep_ctx c = {A, b, nrA, cumul, isrand, rowprob, upb, lwrb, omg, ub, lb};
+    memset(Xstore, 0, sizeof(double) * n * nK);
+    memset(Ystore, 0, sizeof(double) * n * nK);
+    memset(EG, 0, sizeof(double) * (maxK > 0 ? maxK : 1));
+    int startiter;
+    if (x0 && y0) {
+        memcpy(x, x0, 8 * n); memcpy(y, y0, 8 * n);
+        for (int64_t j = 0; j < n; ++j) d[j] = x0[j] - y0[j];
+        if (norm2v(d, n) < 1e-10) { st = OR_ERR_ARG; goto done; }
+        startiter = 1;
+    } else {
+        const double *s0 = x0 ? x0 : y0;
+        for (int64_t j = 0; j < n; ++j) { x[j] = s0 ? s0[j] : 0.0; y[j] = x[j]; }
+        basic_sweep(&c, x, ord, nord, +1);
+        if (issym) basic_sweep(&c, x, ord, nord, -1);
+        basic_sweep(&c, y, ord, nord, -1);
+        if (issym) basic_sweep(&c, y, ord, nord, +1);
+        for (int64_t j = 0; j < n; ++j) d[j] = x[j] - y[j];
+        EG[0] = norm2v(d, n);
+        startiter = 2;
+    }
+    int maxiter = 0;
+    for (int l = 0; l < nK; ++l) if (Kuse[l] > maxiter) maxiter = Kuse[l];
+    int l = 0, trck = 0, iter;
+    double minEG = 1.79769313486231570815e308; /* huge(minEG) */
+    *final_it = 0;
+    for (iter = startiter; iter <= maxiter; ++iter) {
+        if (isrand) or_scramble(nord, ord);
+        if (ms) memcpy(v, x, 8 * n);
+        basic_sweep(&c, x, ord, nord, +1);
+        if (issym) basic_sweep(&c, x, ord, nord, -1);
+        if (ms) {
+            for (int64_t j = 0; j < n; ++j) v[j] = x[j] - v[j];
+            for (int64_t j = 0; j < n; ++j) x[j] = x[j] - v[j];
+        }
+        if (ms) memcpy(w, y, 8 * n);
+        basic_sweep(&c, y, ord, nord, -1);
+        if (issym) basic_sweep(&c, y, ord, nord, +1);
+        if (ms) {
+            for (int64_t j = 0; j < n; ++j) w[j] = y[j] - w[j];
+            for (int64_t j = 0; j < n; ++j) y[j] = y[j] - w[j];
+        }
+        if (eg) {
+            for (int64_t j = 0; j < n; ++j) d[j] = x[j] - y[j];
+            EG[iter - 1] = norm2v(d, n);
+            if (EG[iter - 1] < minEG) {
+                minEG = EG[iter - 1];
+                memcpy(v, x, 8 * n); memcpy(w, y, 8 * n);
+                trck = 0;
+                *final_it = iter;
+            } else {
+                trck = trck + 1;
+                if (trck >= slck) break;
+            }
+        } else {
+            double nw = norm2v(w, n), nv = norm2v(v, n);
+            for (int64_t j = 0; j < n; ++j) w[j] = w[j] / nw;
+            for (int64_t j = 0; j < n; ++j) v[j] = v[j] / nv;
+            for (int64_t j = 0; j < n; ++j) d[j] = x[j] - y[j];
+            double mat1 = dotv(v, v, n), mat2 = dotv(w, w, n), mat3 = -dotv(v, w, n);
+            double rhs1 = -dotv(v, d, n), rhs2 = dotv(w, d, n);
+            double det = mat1 * mat2 - mat3 * mat3;
+            double alph = (rhs1 * mat2 - rhs2 * mat3) / det;
+            double bet = (mat1 * rhs2 - mat3 * rhs1) / det;
+            for (int64_t j = 0; j < n; ++j) x[j] = x[j] + alph * v[j];
+            for (int64_t j = 0; j < n; ++j) y[j] = y[j] + bet * w[j];
+            for (int64_t j = 0; j < n; ++j) d[j] = x[j] - y[j];
+            EG[iter - 1] = norm2v(d, n);
+            if (fabs(alph) + fabs(bet) < 1e-5) break;
+        }
+        if (l < nK && iter == Kuse[l]) {
+            memcpy(Xstore + (size_t)n * l, x, 8 * n);
+            memcpy(Ystore + (size_t)n * l, y, 8 * n);
+            l++;
+        }
+    }
+    if (eg) {
+        for (int64_t j = 0; j < n; ++j) xout[j] = .5 * (v[j] + w[j]);
+    } else {
+        for (int64_t j = 0; j < n; ++j) xout[j] = .5 * (x[j] + y[j]);
+        *final_it = iter;
+    }
+done:
+    free(Kuse); free(ord); free(nrA); free(cumul);
+    free(x); free(y); free(v); free(w); free(d);
+    return st;
+}
+
+/* ------------------------------------------------------------------------- */
+/* phantomgallery.f90                                                        */
+/* ------------------------------------------------------------------------- */
+
+/* shepplogan, phantomgallery.f90:116-164 on the meshgrid of :17-56, returned
+ * already vectorised column by column (vectorise, :672-690). */
+void or_shepplogan(int N, double *v) {
+    static const double e[10][6] = {
+        {1, .69, .92, 0, 0, 0},          {-.8, .6624, .874, 0, -.0184, 0},
+        {-.2, .11, .31, .22, 0, -18},    {-.2, .16, .41, -.22, 0, 18},
+        {.1, .21, .25, 0, .35, 0},       {.1, .046, .046, 0, .1, 0},
+        {.1, .046, .046, 0, -.1, 0},     {.1, .046, .023, -.08, -.605, 0},
+        {.1, .023, .023, 0, -.606, 0},   {.1, .023, .046, .06, -.605, 0}};
+    double *lx = malloc(sizeof(double) * N), *ly = malloc(sizeof(double) * N);
+    or_linspace(-1.0, 1.0, N, lx);  /* x(i,j) = lx(j) */
+    or_linspace(1.0, -1.0, N, ly);  /* y(i,j) = ly(i) */
+    for (int64_t k = 0; k < (int64_t)N * N; ++k) v[k] = 0.0;
+    for (int q = 0; q < 10; ++q) {
+        double A = e[q][0], a2 = e[q][1] * e[q][1], b2 = e[q][2] * e[q][2];
+        double x0 = e[q][3], y0 = e[q][4], phi = e[q][5] * PI / 180.0;
+        double c = cos(phi), s = sin(phi);
+        for (int j = 0; j < N; ++j) {
+            for (int i = 0; i < N; ++i) {
+                double xc = lx[j], yc = ly[i];
+                double u = (xc - x0) * c + (yc - y0) * s;
+                double w = (yc - y0) * c - (xc - x0) * s;
+                if (u * u / a2 + w * w / b2 <= 1.0) v[(int64_t)j * N + i] += A;
+            }
+        }
+    }
+    free(lx); free(ly);
+}
