@@ -360,9 +360,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--prec", choices=["f64", "f32", "f16"], default="f64")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
+    ap.add_argument("--n", type=int, default=1024, help="image size N (profiling cases)")
+    ap.add_argument("--angles", type=int, default=720)
+    ap.add_argument("--bins", type=int, default=1448)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global N, NTH, P, WORKLOAD
+    N, NTH, P = args.n, args.angles, args.bins
+    WORKLOAD = (f"parallel-beam N={N}, {NTH} angles over [0,pi), {P} bins; SIRT (Cimmino)")
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -64,6 +64,14 @@ void DevCSR::release() {
     max_row = 0;
 }
 
+int DevCSR::alloc_entries(int64_t nnz_, cudaStream_t s) {
+    FAIR_TRY(col.grow(sizeof(int32_t) * (size_t)(nnz_ + kEntryPad)));
+    FAIR_TRY(v64.grow(sizeof(double) * (size_t)(nnz_ + kEntryPad)));
+    FAIR_CUDA(cudaMemsetAsync(col.as<int32_t>() + nnz_, 0, sizeof(int32_t) * kEntryPad, s));
+    FAIR_CUDA(cudaMemsetAsync(v64.as<double>() + nnz_, 0, sizeof(double) * kEntryPad, s));
+    return FAIR_OK;
+}
+
 void GeomTables::release() {
     grid.release(); cth.release(); sth.release(); bx0.release(); by0.release();
     ax0th.release(); ay0th.release(); aath.release(); abth.release();
@@ -288,8 +296,11 @@ static int upload_csr(fair_csr h, int32_t m, int32_t n, int64_t nnz, const doubl
     h->A.nnz = nnz;
     cudaStream_t s = h->stream;
     FAIR_TRY(upload(h->A.rowptr, rp, (size_t)m + 1, s));
-    FAIR_TRY(upload(h->A.col, JA, (size_t)nnz, s));
-    FAIR_TRY(upload(h->A.v64, vA, (size_t)nnz, s));
+    FAIR_TRY(h->A.alloc_entries(nnz, s));
+    if (nnz) {
+        FAIR_CUDA(cudaMemcpyAsync(h->A.col.p, JA, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, s));
+        FAIR_CUDA(cudaMemcpyAsync(h->A.v64.p, vA, sizeof(double) * nnz, cudaMemcpyHostToDevice, s));
+    }
     int st = csr_check_upload(h->A, s);
     if (st) h->A.release();
     return st;

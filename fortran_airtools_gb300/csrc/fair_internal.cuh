@@ -42,10 +42,17 @@ struct DevBuf {
     template <typename T> T *as() const { return static_cast<T *>(p); }
 };
 
+// Spare entries after every column/value array: the 16-byte-aligned load
+// window of the row engine (rows.cuh) may read up to 3 entries past the end.
+constexpr int64_t kEntryPad = 4;
+
 struct DevCSR {
     int32_t m = 0, n = 0;
     int64_t nnz = 0;
-    int32_t max_row = 0;  // longest row (nonzeros)
+    int32_t max_row = 0;        // longest row (nonzeros)
+    int lanes_per_row = 8;      // G of the row engine (4, 8, 16 or 32)
+    // allocate col and v64 for nnz entries plus the pad (pad zeroed)
+    int alloc_entries(int64_t nnz_, cudaStream_t s);
     DevBuf rowptr;        // int64 [m+1]
     DevBuf col;           // int32 [nnz], 0-based
     DevBuf v64;           // double [nnz]

@@ -412,8 +412,7 @@ int build_geometry(const GeomTables &T, DevCSR &A, cudaStream_t s) {
                               cudaMemcpyDeviceToHost, s));
     FAIR_CUDA(cudaStreamSynchronize(s));
     A.nnz = nnz;
-    FAIR_TRY(A.col.grow(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
-    FAIR_TRY(A.v64.grow(sizeof(double) * (nnz > 0 ? nnz : 1)));
+    FAIR_TRY(A.alloc_entries(nnz, s));
 
     k_geom_fill<<<blocks, threads, 0, s>>>(G, A.rowptr.as<int64_t>(), A.col.as<int32_t>(),
                                            A.v64.as<double>(), ncols, err.as<int>());

@@ -13,6 +13,7 @@
 #include <algorithm>
 
 #include "fair_internal.cuh"
+#include "rows.cuh"
 
 namespace fair {
 
@@ -283,20 +284,34 @@ __global__ void k_check_rowptr(const int64_t *rowptr, int32_t m, int *err) {
 }
 
 // ------------------------------------------------------------ row norms ----
+// p-norm of every row (compute_row_norms, sparse_matrices.f90:740-780): a warp
+// per row, four independent loads in flight per lane.
 __global__ void k_row_norms(const int64_t *rowptr, int32_t m, const double *v, int p,
                             double *out) {
     int lane = threadIdx.x & 31;
     int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = warp; r < m; r += nw) {
-        double s = 0.0;
-        for (int64_t j = rowptr[r] + lane; j < rowptr[r + 1]; j += 32) {
-            double a = fabs(v[j]), t = a;
-            for (int q = 1; q < p; ++q) t *= a;
-            s += t;
+        const int64_t s = rowptr[r], e = rowptr[r + 1];
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        int64_t j = s + lane;
+        for (; j + 96 < e; j += 128) {
+            double a[4] = {fabs(__ldcs(v + j)), fabs(__ldcs(v + j + 32)), fabs(__ldcs(v + j + 64)),
+                           fabs(__ldcs(v + j + 96))};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                double t = a[u];
+                for (int q = 1; q < p; ++q) t *= a[u];
+                acc[u] += t;
+            }
         }
-        s = warp_sum(s);
-        if (lane == 0) out[r] = p == 1 ? s : (p == 2 ? sqrt(s) : pow(s, 1.0 / p));
+        for (; j < e; j += 32) {
+            double a = fabs(__ldcs(v + j)), t = a;
+            for (int q = 1; q < p; ++q) t *= a;
+            acc[0] += t;
+        }
+        double sum = warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));
+        if (lane == 0) out[r] = p == 1 ? sum : (p == 2 ? sqrt(sum) : pow(sum, 1.0 / p));
     }
 }
 
@@ -324,67 +339,36 @@ __global__ void k_add_mult_row(const int64_t *rowptr, int32_t row, const int32_t
 }
 
 // ----------------------------------------------------------------- SpMV ----
-template <typename VT> __device__ __forceinline__ float ldv32(const VT *p) { return (float)*p; }
-template <> __device__ __forceinline__ float ldv32<__half>(const __half *p) {
-    return __half2float(__ldcs(p));
-}
-template <> __device__ __forceinline__ float ldv32<float>(const float *p) { return __ldcs(p); }
+struct EpiStore64 {
+    double *y;
+    __device__ void operator()(int64_t i, double acc) const { y[i] = acc; }
+};
+struct EpiStore32 {
+    float *y;
+    __device__ void operator()(int64_t i, float acc) const { y[i] = acc; }
+};
 
-__global__ void __launch_bounds__(256) k_spmv_f64(const int64_t *__restrict__ rowptr, int32_t m,
-                                                  const int32_t *__restrict__ col,
-                                                  const double *__restrict__ v,
-                                                  const double *__restrict__ x,
-                                                  double *__restrict__ y) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = warp; r < m; r += nw) {
-        int64_t s = rowptr[r], e = rowptr[r + 1];
-        double acc = 0.0;
-        int64_t j = s + lane;
-        for (; j + 96 < e; j += 128) {
-            int32_t c0 = __ldcs(col + j), c1 = __ldcs(col + j + 32), c2 = __ldcs(col + j + 64),
-                    c3 = __ldcs(col + j + 96);
-            double v0 = __ldcs(v + j), v1 = __ldcs(v + j + 32), v2 = __ldcs(v + j + 64),
-                   v3 = __ldcs(v + j + 96);
-            acc += __ldg(x + c0) * v0;
-            acc += __ldg(x + c1) * v1;
-            acc += __ldg(x + c2) * v2;
-            acc += __ldg(x + c3) * v3;
-        }
-        for (; j < e; j += 32) acc += __ldg(x + __ldcs(col + j)) * __ldcs(v + j);
-        acc = warp_sum(acc);
-        if (lane == 0) y[r] = acc;
-    }
+template <int G>
+__global__ void __launch_bounds__(256) k_spmv_f64(const int64_t *rowptr, int32_t m,
+                                                  const int32_t *col, const double *v,
+                                                  const double *x, EpiStore64 epi) {
+    chunk_rows<double, double, double, G>(rowptr, m, col, v, x, epi);
 }
 
-template <typename VT>
-__global__ void __launch_bounds__(256) k_spmv_lp(const int64_t *__restrict__ rowptr, int32_t m,
-                                                 const int32_t *__restrict__ col,
-                                                 const VT *__restrict__ v,
-                                                 const float *__restrict__ x,
-                                                 float *__restrict__ y) {
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = warp; r < m; r += nw) {
-        int64_t s = rowptr[r], e = rowptr[r + 1];
-        float acc = 0.f;
-        int64_t j = s + lane;
-        for (; j + 96 < e; j += 128) {
-            int32_t c0 = __ldcs(col + j), c1 = __ldcs(col + j + 32), c2 = __ldcs(col + j + 64),
-                    c3 = __ldcs(col + j + 96);
-            float v0 = ldv32(v + j), v1 = ldv32(v + j + 32), v2 = ldv32(v + j + 64),
-                  v3 = ldv32(v + j + 96);
-            acc += __ldg(x + c0) * v0;
-            acc += __ldg(x + c1) * v1;
-            acc += __ldg(x + c2) * v2;
-            acc += __ldg(x + c3) * v3;
-        }
-        for (; j < e; j += 32) acc += __ldg(x + __ldcs(col + j)) * ldv32(v + j);
-        acc = warp_sum(acc);
-        if (lane == 0) y[r] = acc;
-    }
+template <typename VT, int G>
+__global__ void __launch_bounds__(256) k_spmv_lp(const int64_t *rowptr, int32_t m,
+                                                 const int32_t *col, const VT *v,
+                                                 const float *x, EpiStore32 epi) {
+    chunk_rows<VT, float, float, G>(rowptr, m, col, v, x, epi);
+}
+
+template <class K>
+int chunk_grid(K kernel, int64_t m) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0);
+    if (occ < 1) occ = 1;
+    int64_t need = (((int64_t)m + 31) / 32 + 7) / 8;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, need));
 }
 
 int grid_for(int threads, int64_t work_items, int per_sm = 8) {
@@ -439,8 +423,7 @@ int csr_build_transpose(const DevCSR &A, DevCSR &AT, cudaStream_t s) {
     FAIR_TRY(fill.grow(sizeof(int32_t) * ((size_t)A.n + 1)));
     FAIR_TRY(tsrc.grow(sizeof(int64_t) * (nnz > 0 ? nnz : 1)));
     FAIR_TRY(AT.rowptr.grow(sizeof(int64_t) * ((size_t)A.n + 1)));
-    FAIR_TRY(AT.col.grow(sizeof(int32_t) * (nnz > 0 ? nnz : 1)));
-    FAIR_TRY(AT.v64.grow(sizeof(double) * (nnz > 0 ? nnz : 1)));
+    FAIR_TRY(AT.alloc_entries(nnz, s));
     FAIR_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)A.n + 1), s));
     FAIR_CUDA(cudaMemsetAsync(fill.p, 0, sizeof(int32_t) * ((size_t)A.n + 1), s));
     if (nnz > 0)
@@ -513,18 +496,16 @@ int csr_check_upload(DevCSR &A, cudaStream_t s) {
 }
 
 int csr_make_lowprec(DevCSR &A, int prec, cudaStream_t s) {
-    int64_t n = A.nnz > 0 ? A.nnz : 1;
+    const int64_t n = A.nnz + kEntryPad;  // conversion covers the zeroed pad too
     if (prec == FAIR_PREC_F32 && !A.has32) {
         FAIR_TRY(A.v32.grow(sizeof(float) * n));
-        if (A.nnz > 0)
-            k_to_f32<<<grid_for(256, A.nnz), 256, 0, s>>>(A.v64.as<double>(), A.nnz, A.v32.as<float>());
+        k_to_f32<<<grid_for(256, n), 256, 0, s>>>(A.v64.as<double>(), n, A.v32.as<float>());
         FAIR_CUDA(cudaGetLastError());
         A.has32 = true;
     }
     if (prec == FAIR_PREC_F16 && !A.has16) {
         FAIR_TRY(A.v16.grow(sizeof(__half) * n));
-        if (A.nnz > 0)
-            k_to_f16<<<grid_for(256, A.nnz), 256, 0, s>>>(A.v64.as<double>(), A.nnz, A.v16.as<__half>());
+        k_to_f16<<<grid_for(256, n), 256, 0, s>>>(A.v64.as<double>(), n, A.v16.as<__half>());
         FAIR_CUDA(cudaGetLastError());
         A.has16 = true;
     }
@@ -532,7 +513,7 @@ int csr_make_lowprec(DevCSR &A, int prec, cudaStream_t s) {
 }
 
 int csr_scale(DevCSR &A, double c, cudaStream_t s) {
-    if (A.nnz > 0)
+    if (A.nnz > 0)  // the pad stays 0 (c * 0 = 0 for finite c; the pad is never used)
         k_scale<<<grid_for(256, A.nnz), 256, 0, s>>>(A.v64.as<double>(), A.nnz, c);
     FAIR_CUDA(cudaGetLastError());
     // derived copies are rebuilt from the scaled master values
@@ -566,19 +547,32 @@ int csr_add_mult_row(const DevCSR &A, int32_t row, double c, double *d_w, int bm
 
 int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s) {
     if (A.m == 0) return FAIR_OK;
-    int grid = grid_for(256, (int64_t)A.m * 32);
+    const int64_t *rp = A.rowptr.as<int64_t>();
+    const int32_t *cl = A.col.as<int32_t>();
+    const int G = A.lanes_per_row;
+#define SPMV_G(CALL)                                          \
+    switch (G) {                                              \
+        case 4: { constexpr int g_ = 4; CALL; } break;        \
+        case 16: { constexpr int g_ = 16; CALL; } break;      \
+        case 32: { constexpr int g_ = 32; CALL; } break;      \
+        default: { constexpr int g_ = 8; CALL; } break;       \
+    }
     if (prec == FAIR_PREC_F64) {
-        k_spmv_f64<<<grid, 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(),
-                                        A.v64.as<double>(), (const double *)d_x, (double *)d_y);
+        EpiStore64 e{(double *)d_y};
+        SPMV_G((k_spmv_f64<g_><<<chunk_grid(k_spmv_f64<g_>, A.m), 256, 0, s>>>(
+            rp, A.m, cl, A.v64.as<double>(), (const double *)d_x, e)));
     } else if (prec == FAIR_PREC_F32) {
         FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(A), prec, s));
-        k_spmv_lp<float><<<grid, 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(),
-                                              A.v32.as<float>(), (const float *)d_x, (float *)d_y);
+        EpiStore32 e{(float *)d_y};
+        SPMV_G((k_spmv_lp<float, g_><<<chunk_grid(k_spmv_lp<float, g_>, A.m), 256, 0, s>>>(
+            rp, A.m, cl, A.v32.as<float>(), (const float *)d_x, e)));
     } else {
         FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(A), prec, s));
-        k_spmv_lp<__half><<<grid, 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(),
-                                               A.v16.as<__half>(), (const float *)d_x, (float *)d_y);
+        EpiStore32 e{(float *)d_y};
+        SPMV_G((k_spmv_lp<__half, g_><<<chunk_grid(k_spmv_lp<__half, g_>, A.m), 256, 0, s>>>(
+            rp, A.m, cl, A.v16.as<__half>(), (const float *)d_x, e)));
     }
+#undef SPMV_G
     FAIR_CUDA(cudaGetLastError());
     return FAIR_OK;
 }

@@ -149,7 +149,11 @@ static int ray_points(ray_work *w, double a, double b, double x0th, double y0th)
  * system_generation.f90:196-203/:279-297 (fan) and :390-397/:463-482
  * (parallel). `excluded` is the parallel-beam boundary rule of :393-394.
  * With vA == NULL only counts. Returns the count, or -1 when a column index
- * of 0 appears ("++ Something went wrong", :293/:478).
+ * outside 1..n^2 appears. The reference stops for index 0 ("++ Something went
+ * wrong", :293/:478); an index above n^2 (a ray lying on the right or top edge
+ * whose direction component is a rounding residue rather than exactly 0, so
+ * the boundary rule does not drop it) would be written out of range and read
+ * out of bounds by every later product, so it is refused the same way.
  */
 static int64_t ray_segments(const ray_work *w, int n_int, int excluded,
                             int32_t *JA, double *vA) {
@@ -165,7 +169,7 @@ static int64_t ray_segments(const ray_work *w, int n_int, int excluded,
                 double xm = .5 * (w->txx[k] + w->txx[k + 1] + n);
                 double ym = .5 * (w->tyy[k] + w->tyy[k + 1] + n);
                 int32_t ja = (int32_t)floor(xm) * n + (n - (int32_t)floor(ym));
-                if (ja == 0) return -1;
+                if (ja < 1 || ja > n * n) return -1;
                 JA[m] = ja;
             }
             m++;

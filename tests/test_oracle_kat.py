@@ -1,0 +1,293 @@
+"""Known-answer tests that pin the CPU oracle (no GPU needed).
+
+The reference ships no tests, fixtures or golden vectors, and its Fortran
+cannot be compiled here, so the oracle's restatement is pinned by answers
+that follow from the geometry and the algebra alone: axis-aligned rays,
+chord lengths, the boundary rule, transposition, adjoint identities,
+fixed points and the reference's bound orders.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import rel_err
+
+
+def dense(R):
+    return sp.csr_matrix((R.vA, R.JA - 1, R.IA), shape=(R.m, R.n)).toarray()
+
+
+def chord(a, b, x0, y0, h):
+    """Length of the line {(x0,y0) + t(a,b)} inside the square [-h,h]^2."""
+    lo, hi = -np.inf, np.inf
+    for p0, d in ((x0, a), (y0, b)):
+        if d == 0:
+            if not (-h <= p0 <= h):
+                return 0.0
+            continue
+        t1, t2 = (-h - p0) / d, (h - p0) / d
+        lo, hi = max(lo, min(t1, t2)), min(hi, max(t1, t2))
+    return max(hi - lo, 0.0) * np.hypot(a, b)
+
+
+def test_prng_splitmix64_vector(oracle):
+    # first output of SplitMix64 from state 0 is 0xE220A8397B1DCDAF
+    oracle.random_seed(0)
+    u = oracle.random_number(1)[0]
+    assert u == (0xE220A8397B1DCDAF >> 11) * 2.0 ** -53
+
+
+def test_linspace_formula(oracle):
+    """x(i) = c*i + d with c = (b-a)/(n-1), d = a - c (system_generation.f90:29-34)."""
+    a, b, n = 0.0, np.pi, 400
+    c = (b - a) / (n - 1)
+    d = a - c
+    ref = np.array([c * i + d for i in range(1, n + 1)])
+    assert np.array_equal(oracle.linspace(a, b, n), ref)
+    assert oracle.linspace(a, b, n)[0] == 0.0
+
+
+def test_parallel_axis_aligned(oracle):
+    """theta = 0: ray j at x0 = j - (p+1)/2 crosses N pixels of one column
+    from bottom to top, each of length 1."""
+    N, p = 8, 12
+    R = oracle.paralleltomo(N, 1, p, np.array([0.0]))
+    x0 = oracle.linspace(-(p - 1) / 2, (p - 1) / 2, p)
+    for j in range(p):
+        row = slice(R.IA[j], R.IA[j + 1])
+        if abs(x0[j]) < N / 2:
+            cb = int(np.floor(x0[j] + N / 2))
+            assert list(R.JA[row]) == [cb * N + r for r in range(N, 0, -1)]
+            assert np.all(R.vA[row] == 1.0)
+        else:
+            assert R.IA[j + 1] == R.IA[j]
+
+
+def test_parallel_boundary_rule(oracle):
+    """The ray on the right edge (x0 = N/2) is dropped (:393-394); the one on
+    the left edge is kept and assigned to the first pixel column."""
+    N, p = 8, 9
+    R = oracle.paralleltomo(N, 1, p, np.array([0.0]))
+    assert R.IA[9] - R.IA[8] == 0
+    assert list(R.JA[R.IA[0]:R.IA[1]]) == list(range(8, 0, -1))
+
+
+def test_parallel_edge_ray_refused(oracle):
+    """theta = linspace(0,pi,8)[7] = pi leaves a = -sin(pi) ~ -1.2e-16, so the
+    ray with x0 = -N/2 lies on the right edge without being dropped by the
+    a == 0 rule; its column index exceeds N^2 and the build is refused."""
+    with pytest.raises(oracle.OracleError):
+        oracle.paralleltomo(10, 8, 15, oracle.linspace(0.0, np.pi, 8))
+
+
+@pytest.mark.parametrize("theta", [0.3, 0.7853981633974483, 1.2, 2.0, 2.9])
+def test_parallel_chord_lengths(oracle, theta):
+    """Each row's lengths sum to the chord of its ray through the square."""
+    N, p = 16, 24
+    R = oracle.paralleltomo(N, 1, p, np.array([theta]))
+    x0 = oracle.linspace(-(p - 1) / 2, (p - 1) / 2, p)
+    for j in range(p):
+        a, b = -np.sin(theta), np.cos(theta)
+        xs, ys = np.cos(theta) * x0[j], np.sin(theta) * x0[j]
+        L = R.vA[R.IA[j]:R.IA[j + 1]].sum()
+        assert abs(L - chord(a, b, xs, ys, N / 2)) < 1e-9
+
+
+def test_parallel_columns_in_range_and_area(oracle):
+    N, nth, p = 32, 12, 48
+    th = oracle.linspace(0.0, np.pi, nth)
+    R = oracle.paralleltomo(N, nth, p, th)
+    assert R.JA.min() >= 1 and R.JA.max() <= N * N
+    assert R.vA[R.IA[0]:R.IA[p]].sum() == N * N
+
+
+@pytest.mark.parametrize("fix", [True, False])
+def test_fan_chord_lengths(oracle, fix):
+    """Fan beam: each row's lengths sum to the chord of the ray from the
+    source (0,R) rotated by theta with the per-bin angle."""
+    N, p, r, dw, sd = 16, 21, 2.0, 1.5, 2.0
+    th = np.array([0.4])
+    R = oracle.fanlineartomo(N, 1, p, r, dw, sd, th, geometry_fix=fix)
+    Rs, dwn, sdn = r * N, dw * N, sd * N
+    dew = dwn / p
+    h = (p - 1) // 2
+    dep = np.arange(1, h + 1) * dew
+    off = 0.5 * np.pi if fix else 0.5
+    omega = np.concatenate([np.arctan(sdn / dep[::-1]) - off, [0.0], 0.5 * np.pi - np.arctan(sdn / dep)])
+    c, s = np.cos(th[0]), np.sin(th[0])
+    x0, y0 = -s * Rs, c * Rs
+    ath, bth = -x0 / Rs, -y0 / Rs
+    for j in range(p):
+        a = np.cos(omega[j]) * ath - np.sin(omega[j]) * bth
+        b = np.sin(omega[j]) * ath + np.cos(omega[j]) * bth
+        L = R.vA[R.IA[j]:R.IA[j + 1]].sum()
+        assert abs(L - chord(a, b, x0, y0, N / 2)) < 1e-9
+
+
+def test_fan_odd_p_angle_offset(oracle):
+    """The reference subtracts .5 (not .5*pi) from the left-half ray angles
+    when p is odd (system_generation.f90:122): the mirror symmetry of the fan
+    at theta = 0 holds only with the fix."""
+    N, p = 16, 17
+    th = np.array([0.0])
+
+    def mirror_ok(R):
+        for j in range(p):
+            a = sorted(R.vA[R.IA[j]:R.IA[j + 1]])
+            b = sorted(R.vA[R.IA[p - 1 - j]:R.IA[p - j]])
+            if len(a) != len(b) or not np.allclose(a, b, atol=1e-12):
+                return False
+        return True
+
+    assert mirror_ok(oracle.fanlineartomo(N, 1, p, 2.0, 1.0, 2.0, th, geometry_fix=True))
+    assert not mirror_ok(oracle.fanlineartomo(N, 1, p, 2.0, 1.0, 2.0, th, geometry_fix=False))
+
+
+def test_reorder_is_stable_transpose(oracle):
+    N, nth, p = 16, 10, 24
+    R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
+    T = oracle.reorder(R)
+    S = sp.csr_matrix((R.vA, R.JA - 1, R.IA), shape=(R.m, R.n)).T.tocsr()
+    S.sort_indices()
+    assert np.array_equal(T.IA, S.indptr) and np.array_equal(T.JA - 1, S.indices)
+    assert np.array_equal(T.vA, S.data)
+
+
+def test_operators_against_dense(oracle):
+    N, nth, p = 12, 9, 18
+    R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
+    D = dense(R)
+    rng = np.random.default_rng(0)
+    x, y = rng.standard_normal(R.n), rng.standard_normal(R.m)
+    assert np.allclose(oracle.matvecmul(R, x), D @ x, rtol=1e-13, atol=1e-13)
+    assert np.allclose(oracle.transvecmul(R, y), D.T @ y, rtol=1e-13, atol=1e-13)
+    assert np.allclose(oracle.row_norms(R, 2), np.linalg.norm(D, axis=1), rtol=1e-14)
+    assert np.allclose(oracle.row_norms(R, 1), np.abs(D).sum(1), rtol=1e-14)
+    assert np.allclose(oracle.column_norms(R, 1), np.abs(D).sum(0), rtol=1e-14)
+    assert abs(oracle.matvecmul(R, x) @ y - x @ oracle.transvecmul(R, y)) < 1e-10
+    k = 5
+    assert abs(oracle.rowvecmult(R, k, x) - D[k - 1] @ x) < 1e-12
+
+
+def test_add_mult_row_bound_order(oracle):
+    """add_mult_row: max(lb) then min(ub) on the touched entries (:811-818)."""
+    N = 4
+    R = oracle.paralleltomo(N, 1, 6, np.array([0.0]))
+    w = np.zeros(R.n)
+    oracle.add_mult_row(R, 2, 1.0, w, lwrb=0.7, upb=0.3)  # lb > ub: ub wins
+    touched = R.JA[R.IA[1]:R.IA[2]] - 1
+    assert np.all(w[touched] == 0.3)
+    assert np.count_nonzero(w) == len(touched)
+
+
+def test_sirt_bound_order_and_fixed_point(oracle):
+    """sirt bounds: min(ub) then max(lb) (:1097-1099); a solution of a
+    consistent system is a fixed point of Cimmino and SART."""
+    N, nth, p = 12, 10, 18
+    R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
+    xt = oracle.shepplogan(N)
+    b = oracle.matvecmul(R, xt)
+    for m in ("cimmino", "sart"):
+        x1 = oracle.sirt(m, R, b, 1, x0=xt)
+        assert rel_err(x1, xt) < 1e-12
+    o = oracle.options(lbound=0.7, ubound=0.3)
+    x = oracle.sirt("cimmino", R, b, 1, opts=o)
+    assert np.all(x == 0.7)
+
+
+def test_sirt_and_kaczmarz_converge(oracle):
+    N, nth, p = 12, 24, 18
+    R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
+    xt = oracle.shepplogan(N)
+    b = oracle.matvecmul(R, xt)
+    e5 = rel_err(oracle.sirt("sart", R, b, 5), xt)
+    e50 = rel_err(oracle.sirt("sart", R, b, 50), xt)
+    assert e50 < e5
+    X = oracle.art("kaczmarz", R, b, [1, 10])
+    assert rel_err(X[:, 1], xt) < rel_err(X[:, 0], xt)
+
+
+def test_kaczmarz_single_projection(oracle):
+    """One ART step with relaxpar 1 puts x on the hyperplane of its row."""
+    N = 8
+    R = oracle.paralleltomo(N, 1, 12, np.array([0.3]))
+    b = np.arange(1, R.m + 1, dtype=float)
+    order = np.array([5], np.int32)
+    X = oracle.art("kaczmarz", R, b, [1], order=order)
+    assert abs(oracle.rowvecmult(R, 5, X[:, 0]) - b[4]) < 1e-12
+
+
+def test_normest_matches_svd(oracle):
+    N, nth, p = 10, 8, 16
+    R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
+    smax = np.linalg.svd(dense(R), compute_uv=False)[0]
+    v0 = np.random.default_rng(1).uniform(size=R.n)
+    assert abs(oracle.normest(R, v0, tol=1e-12, maxit=5000) - smax) < 1e-6 * smax
+
+
+def test_gradient_descent_decreases_residual(oracle):
+    N, nth, p = 10, 12, 16
+    R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
+    b = oracle.matvecmul(R, oracle.shepplogan(N))
+    oracle.random_seed(2)
+    x5, _ = oracle.gradient_descent(R, b, max_iter=5)
+    oracle.random_seed(2)
+    x50, _ = oracle.gradient_descent(R, b, max_iter=50)
+    r5 = np.linalg.norm(oracle.matvecmul(R, x5) - b)
+    r50 = np.linalg.norm(oracle.matvecmul(R, x50) - b)
+    assert r50 < r5
+
+
+def test_scramble_recipe(oracle):
+    """Two passes of swaps with j = 1 + floor(n*u) (AIRMs.f90:1199-1210)."""
+    oracle.random_seed(4)
+    u = oracle.random_number(2 * 50)
+    oracle.random_seed(4)
+    perm = oracle.scramble(50)
+    ref = list(range(1, 51))
+    k = 0
+    for _ in range(2):
+        for i in range(50):
+            j = int(np.floor(50 * u[k]))
+            k += 1
+            ref[j], ref[i] = ref[i], ref[j]
+    assert list(perm) == ref
+    assert sorted(perm) == list(range(1, 51))
+
+
+def test_shepplogan(oracle):
+    """10-ellipse phantom on the [-1,1]^2 meshgrid (phantomgallery.f90:116-164)."""
+    N = 64
+    v = oracle.shepplogan(N).reshape(N, N, order="F")
+    lin = oracle.linspace(-1, 1, N)
+    X, Y = np.meshgrid(lin, oracle.linspace(1, -1, N))
+    E = [(1, .69, .92, 0, 0, 0), (-.8, .6624, .874, 0, -.0184, 0), (-.2, .11, .31, .22, 0, -18),
+         (-.2, .16, .41, -.22, 0, 18), (.1, .21, .25, 0, .35, 0), (.1, .046, .046, 0, .1, 0),
+         (.1, .046, .046, 0, -.1, 0), (.1, .046, .023, -.08, -.605, 0),
+         (.1, .023, .023, 0, -.606, 0), (.1, .023, .046, .06, -.605, 0)]
+    ref = np.zeros((N, N))
+    for A, a, b, x0, y0, ph in E:
+        ph = ph * np.pi / 180
+        u = (X - x0) * np.cos(ph) + (Y - y0) * np.sin(ph)
+        w = (Y - y0) * np.cos(ph) - (X - x0) * np.sin(ph)
+        ref[u * u / (a * a) + w * w / (b * b) <= 1] += A
+    assert np.allclose(v, ref)
+
+
+def test_white_noise_scaling(oracle):
+    b = np.linspace(1, 2, 500)
+    oracle.random_seed(3)
+    bt, e = oracle.add_white_noise(b, 0.05)
+    assert abs(np.linalg.norm(e) - 0.05 * np.linalg.norm(b)) < 1e-12
+    assert np.allclose(bt, b + e)
+    assert abs(e.mean()) < 0.1 * e.std()
+
+
+def test_twin_art_error_gauge(oracle):
+    N, nth, p = 10, 12, 16
+    R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
+    b = oracle.matvecmul(R, oracle.shepplogan(N))
+    xout, fi, Xs, Ys, EG = oracle.twin_art("kaczmarz", "errorgauge", R, b, [20],
+                                           opts=oracle.options(relaxpar=0.5))
+    assert 1 <= fi <= 20
+    assert EG[1] < EG[0]
