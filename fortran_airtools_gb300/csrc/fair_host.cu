@@ -225,6 +225,11 @@ int fair_csr_create(fair_csr *out) {
         return cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
     }
     h->own_stream = true;
+    if (h->w_sched.grow(4 * sizeof(unsigned)) != FAIR_OK ||
+        cudaMemset(h->w_sched.p, 0, 4 * sizeof(unsigned)) != cudaSuccess) {
+        fair_csr_destroy(h);
+        return FAIR_ERR_ALLOC;
+    }
     *out = h;
     return FAIR_OK;
 }
@@ -237,7 +242,7 @@ int fair_csr_destroy(fair_csr h) {
     h->AT.release();
     DevBuf *bufs[] = {&h->w_in, &h->w_out, &h->w_b, &h->w_x, &h->w_x32, &h->w_r, &h->w_M,
                       &h->w_D, &h->w_xn, &h->w_tmp, &h->w_part, &h->w_flag, &h->w_ord,
-                      &h->w_cumul, &h->w_nrA, &h->w_y, &h->s_M, &h->s_D, &h->s_r, &h->s_x32};
+                      &h->w_cumul, &h->w_nrA, &h->w_y, &h->s_M, &h->s_D, &h->s_r, &h->s_x32, &h->w_sched};
     for (DevBuf *b : bufs) b->release();
     if (h->own_stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -474,12 +479,12 @@ static int apply_op(fair_csr h, const DevCSR &M, const double *v, double *w) {
     FAIR_TRY(upload(h->w_in, v, (size_t)M.n, s));
     FAIR_TRY(h->w_out.grow(sizeof(double) * ((size_t)M.m + 1)));
     if (h->prec == FAIR_PREC_F64) {
-        FAIR_TRY(spmv(M, FAIR_PREC_F64, h->w_in.p, h->w_out.p, s));
+        FAIR_TRY(spmv(M, FAIR_PREC_F64, h->w_in.p, h->w_out.p, s, h->w_sched.as<unsigned>()));
     } else {
         FAIR_TRY(h->w_x32.grow(sizeof(float) * ((size_t)M.n + 1)));
         FAIR_TRY(h->w_tmp.grow(sizeof(float) * ((size_t)M.m + 1)));
         FAIR_TRY(vec_to_f32(h->w_in.as<double>(), M.n, h->w_x32.as<float>(), s));
-        FAIR_TRY(spmv(M, h->prec, h->w_x32.p, h->w_tmp.p, s));
+        FAIR_TRY(spmv(M, h->prec, h->w_x32.p, h->w_tmp.p, s, h->w_sched.as<unsigned>()));
         FAIR_TRY(vec_to_f64(h->w_tmp.as<float>(), M.m, h->w_out.as<double>(), s));
     }
     return download<double>(w, h->w_out.p, (size_t)M.m, s);
@@ -633,6 +638,7 @@ int fair_sirt(double *xout, const char *sirt_method, fair_csr h, const double *b
     S.bmode = o.bmode();
     S.lb = o.lb;
     S.ub = o.ub;
+    S.sched = h->w_sched.as<unsigned>();
     FAIR_TRY(sirt_prepare_shadow(S, s));
     FAIR_TRY(sirt_iterations(S, maxits, s));
     return download<double>(xout, h->w_x.p, (size_t)n, s);
@@ -1117,6 +1123,7 @@ static int device_sirt(fair_csr h, const double *d_b, double *d_x, SirtDev &S) {
     S.bmode = h->sirt_bmode;
     S.lb = h->sirt_lb;
     S.ub = h->sirt_ub;
+    S.sched = h->w_sched.as<unsigned>();
     return sirt_prepare_shadow(S, h->stream);
 }
 
@@ -1148,7 +1155,7 @@ int fair_spmv_device(fair_csr h, int32_t trans, const void *d_x, void *d_y) {
     NEED_MATRIX(h);
     if (!d_x || !d_y) return FAIR_ERR_NULL;
     if (trans) FAIR_TRY(ensure_transpose(h));
-    return spmv(trans ? h->AT : h->A, h->prec, d_x, d_y, h->stream);
+    return spmv(trans ? h->AT : h->A, h->prec, d_x, d_y, h->stream, h->w_sched.as<unsigned>());
 }
 
 }  // extern "C"

@@ -92,7 +92,9 @@ int csr_add_mult_row(const DevCSR &A, int32_t row, double c, double *d_w, int bm
                      double lb, double ub, cudaStream_t s);
 
 // y = A x in the requested precision (FP64 vectors for F64; FP32 for F32/F16).
-int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s);
+// `sched`: two zeroed counters for dynamic chunk scheduling (rows.cuh), or null.
+int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s,
+         unsigned *sched = nullptr);
 
 // ---- fused solvers (solvers.cu) -----------------------------------------------
 struct SirtDev {
@@ -108,6 +110,7 @@ struct SirtDev {
     double omg = 1.0;
     int bmode = 0;  // bit0 = upper bound, bit1 = lower bound
     double lb = 0.0, ub = 0.0;
+    unsigned *sched = nullptr;   // chunk-scheduling counters (rows.cuh)
 };
 int sirt_weights(const DevCSR &A, const DevCSR &AT, bool sart, double *d_M, double *d_D,
                  cudaStream_t s);
@@ -196,6 +199,7 @@ struct fair_csr_s {
     // work buffers reused across calls
     fair::DevBuf w_in, w_out, w_b, w_x, w_x32, w_r, w_M, w_D, w_xn, w_tmp, w_part, w_flag;
     fair::DevBuf w_ord, w_cumul, w_nrA, w_y;
+    fair::DevBuf w_sched;  // two zeroed counters for dynamic chunk scheduling
     // state of fair_sirt_prepare (device-resident SIRT)
     bool sirt_ready = false, sirt_sart = false;
     int sirt_prec = FAIR_PREC_F64;

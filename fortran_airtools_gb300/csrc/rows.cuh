@@ -46,6 +46,29 @@ template <> struct VLoad<__half, float> {
     }
 };
 
+// Next chunk for this warp. With `sched` (two zeroed counters) chunks are
+// claimed dynamically, one atomic per chunk, which balances the warps when
+// chunk costs differ (runs of empty edge rays); the last warp to run out
+// resets the counters for the next launch on the stream. Without `sched`
+// the warps stride over the chunks in a fixed order (used where block sums
+// must not depend on scheduling).
+__device__ __forceinline__ int64_t next_chunk(unsigned *sched, int64_t prev, int64_t nwarps,
+                                              int lane) {
+    if (!sched) return prev + nwarps;
+    unsigned c = 0;
+    if (lane == 0) c = atomicAdd(&sched[0], 1u);
+    return (int64_t)__shfl_sync(0xffffffffu, c, 0);
+}
+
+__device__ __forceinline__ void finish_chunks(unsigned *sched, int64_t nwarps, int lane) {
+    if (!sched || lane != 0) return;
+    unsigned done = atomicAdd(&sched[1], 1u);
+    if (done == (unsigned)(nwarps - 1)) {  // every warp has stopped claiming
+        sched[0] = 0u;
+        sched[1] = 0u;
+    }
+}
+
 // Sum over the rows of every chunk owned by this warp; calls epi(row, sum)
 // from the lane that owns `row` (all lanes of the warp call epi together).
 // VT: stored value type; XT: gathered vector type; ACC: accumulator type.
@@ -53,13 +76,15 @@ template <typename VT, typename XT, typename ACC, int G, class Epi>
 __device__ __forceinline__ void chunk_rows(const int64_t *__restrict__ rowptr, int32_t m,
                                            const int32_t *__restrict__ col,
                                            const VT *__restrict__ val,
-                                           const XT *__restrict__ x, Epi &epi) {
+                                           const XT *__restrict__ x, Epi &epi,
+                                           unsigned *sched = nullptr) {
     constexpr int R = 32 / G;
     const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t nchunks = ((int64_t)m + 31) >> 5;
-    for (int64_t ch = warp; ch < nchunks; ch += nwarps) {
+    for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
+         ch = next_chunk(sched, ch, nwarps, lane)) {
         const int64_t base = ch << 5;
         ACC mine = 0;
 #pragma unroll 1
@@ -110,6 +135,7 @@ __device__ __forceinline__ void chunk_rows(const int64_t *__restrict__ rowptr, i
         const int64_t row = base + lane;
         if (row < m) epi(row, mine);
     }
+    finish_chunks(sched, nwarps, lane);
 }
 
 // Lanes per row used when none has been tuned.

@@ -120,26 +120,30 @@ struct EpiStoreSq {  // y = Ax, partial sum of y^2
 template <int G>
 __global__ void __launch_bounds__(256) k_sirt_resid_f64(const int64_t *rowptr, int32_t m,
                                                         const int32_t *col, const double *v,
-                                                        const double *x, EpiResidF64 epi) {
-    chunk_rows<double, double, double, G>(rowptr, m, col, v, x, epi);
+                                                        const double *x, EpiResidF64 epi,
+                                                        unsigned *sched) {
+    chunk_rows<double, double, double, G>(rowptr, m, col, v, x, epi, sched);
 }
 template <typename VT, int G>
 __global__ void __launch_bounds__(256) k_sirt_resid_lp(const int64_t *rowptr, int32_t m,
                                                        const int32_t *col, const VT *v,
-                                                       const float *x, EpiResidLP epi) {
-    chunk_rows<VT, float, float, G>(rowptr, m, col, v, x, epi);
+                                                       const float *x, EpiResidLP epi,
+                                                       unsigned *sched) {
+    chunk_rows<VT, float, float, G>(rowptr, m, col, v, x, epi, sched);
 }
 template <int G>
 __global__ void __launch_bounds__(256) k_sirt_update_f64(const int64_t *rowptr, int32_t m,
                                                          const int32_t *col, const double *v,
-                                                         const double *r, EpiUpdateF64 epi) {
-    chunk_rows<double, double, double, G>(rowptr, m, col, v, r, epi);
+                                                         const double *r, EpiUpdateF64 epi,
+                                                         unsigned *sched) {
+    chunk_rows<double, double, double, G>(rowptr, m, col, v, r, epi, sched);
 }
 template <typename VT, int G>
 __global__ void __launch_bounds__(256) k_sirt_update_lp(const int64_t *rowptr, int32_t m,
                                                         const int32_t *col, const VT *v,
-                                                        const float *r, EpiUpdateLP epi) {
-    chunk_rows<VT, float, float, G>(rowptr, m, col, v, r, epi);
+                                                        const float *r, EpiUpdateLP epi,
+                                                        unsigned *sched) {
+    chunk_rows<VT, float, float, G>(rowptr, m, col, v, r, epi, sched);
 }
 template <int G>
 __global__ void __launch_bounds__(256) k_gd_update(const int64_t *rowptr, int32_t m,
@@ -344,30 +348,30 @@ static void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
         if (S.prec == FAIR_PREC_F64) {
             EpiResidF64 e{S.b, S.Minv, (double *)S.r};
             FAIR_G_DISPATCH(G, (k_sirt_resid_f64<g_><<<chunk_grid(k_sirt_resid_f64<g_>, M.m), 256, 0, s>>>(
-                                    rp, M.m, cl, M.v64.as<double>(), S.x, e)));
+                                    rp, M.m, cl, M.v64.as<double>(), S.x, e, S.sched)));
         } else {
             EpiResidLP e{S.b, S.Minv, (float *)S.r};
             if (S.prec == FAIR_PREC_F32) {
                 FAIR_G_DISPATCH(G, (k_sirt_resid_lp<float, g_><<<chunk_grid(k_sirt_resid_lp<float, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v32.as<float>(), S.x32, e)));
+                                        rp, M.m, cl, M.v32.as<float>(), S.x32, e, S.sched)));
             } else {
                 FAIR_G_DISPATCH(G, (k_sirt_resid_lp<__half, g_><<<chunk_grid(k_sirt_resid_lp<__half, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v16.as<__half>(), S.x32, e)));
+                                        rp, M.m, cl, M.v16.as<__half>(), S.x32, e, S.sched)));
             }
         }
     } else {
         if (S.prec == FAIR_PREC_F64) {
             EpiUpdateF64 e{S.D, S.x, S.omg, S.lb, S.ub, S.bmode};
             FAIR_G_DISPATCH(G, (k_sirt_update_f64<g_><<<chunk_grid(k_sirt_update_f64<g_>, M.m), 256, 0, s>>>(
-                                    rp, M.m, cl, M.v64.as<double>(), (const double *)S.r, e)));
+                                    rp, M.m, cl, M.v64.as<double>(), (const double *)S.r, e, S.sched)));
         } else {
             EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode};
             if (S.prec == FAIR_PREC_F32) {
                 FAIR_G_DISPATCH(G, (k_sirt_update_lp<float, g_><<<chunk_grid(k_sirt_update_lp<float, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v32.as<float>(), (const float *)S.r, e)));
+                                        rp, M.m, cl, M.v32.as<float>(), (const float *)S.r, e, S.sched)));
             } else {
                 FAIR_G_DISPATCH(G, (k_sirt_update_lp<__half, g_><<<chunk_grid(k_sirt_update_lp<__half, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v16.as<__half>(), (const float *)S.r, e)));
+                                        rp, M.m, cl, M.v16.as<__half>(), (const float *)S.r, e, S.sched)));
             }
         }
     }

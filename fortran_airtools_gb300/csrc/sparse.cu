@@ -351,15 +351,17 @@ struct EpiStore32 {
 template <int G>
 __global__ void __launch_bounds__(256) k_spmv_f64(const int64_t *rowptr, int32_t m,
                                                   const int32_t *col, const double *v,
-                                                  const double *x, EpiStore64 epi) {
-    chunk_rows<double, double, double, G>(rowptr, m, col, v, x, epi);
+                                                  const double *x, EpiStore64 epi,
+                                                  unsigned *sched) {
+    chunk_rows<double, double, double, G>(rowptr, m, col, v, x, epi, sched);
 }
 
 template <typename VT, int G>
 __global__ void __launch_bounds__(256) k_spmv_lp(const int64_t *rowptr, int32_t m,
                                                  const int32_t *col, const VT *v,
-                                                 const float *x, EpiStore32 epi) {
-    chunk_rows<VT, float, float, G>(rowptr, m, col, v, x, epi);
+                                                 const float *x, EpiStore32 epi,
+                                                 unsigned *sched) {
+    chunk_rows<VT, float, float, G>(rowptr, m, col, v, x, epi, sched);
 }
 
 template <class K>
@@ -545,7 +547,8 @@ int csr_add_mult_row(const DevCSR &A, int32_t row, double c, double *d_w, int bm
     return FAIR_OK;
 }
 
-int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s) {
+int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s,
+         unsigned *sched) {
     if (A.m == 0) return FAIR_OK;
     const int64_t *rp = A.rowptr.as<int64_t>();
     const int32_t *cl = A.col.as<int32_t>();
@@ -560,17 +563,17 @@ int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s) 
     if (prec == FAIR_PREC_F64) {
         EpiStore64 e{(double *)d_y};
         SPMV_G((k_spmv_f64<g_><<<chunk_grid(k_spmv_f64<g_>, A.m), 256, 0, s>>>(
-            rp, A.m, cl, A.v64.as<double>(), (const double *)d_x, e)));
+            rp, A.m, cl, A.v64.as<double>(), (const double *)d_x, e, sched)));
     } else if (prec == FAIR_PREC_F32) {
         FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(A), prec, s));
         EpiStore32 e{(float *)d_y};
         SPMV_G((k_spmv_lp<float, g_><<<chunk_grid(k_spmv_lp<float, g_>, A.m), 256, 0, s>>>(
-            rp, A.m, cl, A.v32.as<float>(), (const float *)d_x, e)));
+            rp, A.m, cl, A.v32.as<float>(), (const float *)d_x, e, sched)));
     } else {
         FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(A), prec, s));
         EpiStore32 e{(float *)d_y};
         SPMV_G((k_spmv_lp<__half, g_><<<chunk_grid(k_spmv_lp<__half, g_>, A.m), 256, 0, s>>>(
-            rp, A.m, cl, A.v16.as<__half>(), (const float *)d_x, e)));
+            rp, A.m, cl, A.v16.as<__half>(), (const float *)d_x, e, sched)));
     }
 #undef SPMV_G
     FAIR_CUDA(cudaGetLastError());
