@@ -36,8 +36,8 @@ sys.path.insert(0, ROOT)
 N, NTH, P = 1024, 720, 1448
 METRIC = "SIRT iter/s at N=1024 (FP64 vs mixed, <=1e-5 rel err); SpMV GB/s vs HBM peak"
 WORKLOAD = "parallel-beam N=1024, 720 angles over [0,pi), 1448 bins; SIRT (Cimmino)"
-PREC_NAMES = {"f64": 0, "f32": 1, "f16": 2}
-VAL_BYTES = {"f64": 8, "f32": 4, "f16": 2}
+PREC_NAMES = {"f64": 0, "f32": 1, "f16": 2, "q16": 3}
+VAL_BYTES = {"f64": 8, "f32": 4, "f16": 2, "q16": 2}
 
 
 def theta():
@@ -238,7 +238,7 @@ def run_ours(args):
 
     forms = {}
     results = {}
-    for prec in ("f64", "f32", "f16"):
+    for prec in ("f64", "f32", "f16", "q16"):
         A.set_precision(prec)
         check(L.fair_sirt_prepare(h, b"cimmino", C.byref(opts)))
         with torch.cuda.stream(stream):
@@ -277,7 +277,7 @@ def run_ours(args):
         forms[prec] = {"iter_per_s": world * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
                        "pass1_ms": ms1.value / kt, "pass2_ms": ms2.value / kt,
                        "launches": launches.value, "clocks": clocks}
-    for prec in ("f32", "f16"):
+    for prec in ("f32", "f16", "q16"):
         r = results["f64"]
         forms[prec]["rel_err_vs_f64"] = float(np.linalg.norm(results[prec] - r) / np.linalg.norm(r))
 
@@ -358,7 +358,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--prec", choices=["f64", "f32", "f16"], default="f64")
+    ap.add_argument("--prec", choices=["f64", "f32", "f16", "q16"], default="f64")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
     ap.add_argument("--n", type=int, default=1024, help="image size N (profiling cases)")
     ap.add_argument("--angles", type=int, default=720)

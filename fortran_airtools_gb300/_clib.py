@@ -27,7 +27,7 @@ FAIR_ERR_NULL = 8
 FAIR_ERR_STATE = 9
 FAIR_ERR_NOGPU = 10
 
-PREC = {"f64": 0, "f32": 1, "f16": 2}
+PREC = {"f64": 0, "f32": 1, "f16": 2, "q16": 3}
 
 
 class FairError(RuntimeError):

@@ -57,8 +57,8 @@ void DevBuf::release() {
 }
 
 void DevCSR::release() {
-    rowptr.release(); col.release(); v64.release(); v32.release(); v16.release();
-    has32 = has16 = false;
+    rowptr.release(); col.release(); v64.release(); v32.release(); v16.release(); vq.release();
+    has32 = has16 = hasq = false;
     m = n = 0;
     nnz = 0;
     max_row = 0;
@@ -273,8 +273,9 @@ int fair_csr_info(fair_csr h, int32_t *m, int32_t *n, int64_t *nnz) {
 
 int fair_csr_set_precision(fair_csr h, int32_t prec) {
     if (!h) return FAIR_ERR_NULL;
-    if (prec != FAIR_PREC_F64 && prec != FAIR_PREC_F32 && prec != FAIR_PREC_F16) {
-        set_detail("precision must be FAIR_PREC_F64, FAIR_PREC_F32 or FAIR_PREC_F16");
+    if (prec != FAIR_PREC_F64 && prec != FAIR_PREC_F32 && prec != FAIR_PREC_F16 &&
+        prec != FAIR_PREC_Q16) {
+        set_detail("precision must be FAIR_PREC_F64, _F32, _F16 or _Q16");
         return FAIR_ERR_ARG;
     }
     h->prec = prec;

@@ -58,7 +58,10 @@ struct DevCSR {
     DevBuf v64;           // double [nnz]
     DevBuf v32;           // float [nnz] (derived, valid if has32)
     DevBuf v16;           // __half [nnz] (derived, valid if has16)
-    bool has32 = false, has16 = false;
+    DevBuf vq;            // uint16/int16 [nnz] fixed point (derived, valid if hasq)
+    bool has32 = false, has16 = false, hasq = false;
+    bool qsigned = false;  // vq holds int16 (some value negative) instead of uint16
+    double qscale = 1.0;   // value = qscale * vq
     void release();
     bool empty() const { return rowptr.p == nullptr; }
 };

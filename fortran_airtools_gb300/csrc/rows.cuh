@@ -69,6 +69,23 @@ __device__ __forceinline__ void finish_chunks(unsigned *sched, int64_t nwarps, i
     }
 }
 
+// 16-bit fixed-point values: the integer codes are accumulated as floats and
+// the matrix scale is applied once per row in the epilogue.
+template <> struct VLoad<uint16_t, float> {
+    static __device__ __forceinline__ void ld(const uint16_t *p, float (&o)[4]) {
+        uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
+        o[0] = (float)(t.x & 0xffffu); o[1] = (float)(t.x >> 16);
+        o[2] = (float)(t.y & 0xffffu); o[3] = (float)(t.y >> 16);
+    }
+};
+template <> struct VLoad<int16_t, float> {
+    static __device__ __forceinline__ void ld(const int16_t *p, float (&o)[4]) {
+        uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
+        o[0] = (float)(int16_t)(t.x & 0xffffu); o[1] = (float)(int16_t)(t.x >> 16);
+        o[2] = (float)(int16_t)(t.y & 0xffffu); o[3] = (float)(int16_t)(t.y >> 16);
+    }
+};
+
 // Sum over the rows of every chunk owned by this warp; calls epi(row, sum)
 // from the lane that owns `row` (all lanes of the warp call epi together).
 // VT: stored value type; XT: gathered vector type; ACC: accumulator type.

@@ -60,8 +60,9 @@ struct EpiResidF64 {  // r = (b - Ax) / M
 struct EpiResidLP {  // same, FP32 dot, FP64 weighting, FP32 residual
     const double *b, *M;
     float *r;
+    double scale;  // 1, or the fixed-point scale of 16-bit codes
     __device__ void operator()(int64_t i, float acc) const {
-        r[i] = (float)__ddiv_rn(__dsub_rn(b[i], (double)acc), M[i]);
+        r[i] = (float)__ddiv_rn(__dsub_rn(b[i], __dmul_rn((double)acc, scale)), M[i]);
     }
 };
 struct EpiUpdateF64 {  // x = P(x + omg * (A'r) / D)
@@ -81,8 +82,9 @@ struct EpiUpdateLP {
     float *x32;
     double omg, lb, ub;
     int bmode;
+    double scale;  // 1, or the fixed-point scale of 16-bit codes
     __device__ void operator()(int64_t j, float acc) const {
-        double g = __dmul_rn(omg, (double)acc);
+        double g = __dmul_rn(omg, __dmul_rn((double)acc, scale));
         if (D) g = __ddiv_rn(g, D[j]);
         double t = box(__dadd_rn(x[j], g), bmode, lb, ub);
         x[j] = t;
@@ -337,43 +339,55 @@ int sirt_prepare_shadow(const SirtDev &S, cudaStream_t s) {
     return FAIR_OK;
 }
 
+template <typename VT>
+static void resid_lp(const SirtDev &S, const DevCSR &M, const VT *vals, double scale,
+                     cudaStream_t s) {
+    EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
+    FAIR_G_DISPATCH(M.lanes_per_row,
+                    (k_sirt_resid_lp<VT, g_><<<chunk_grid(k_sirt_resid_lp<VT, g_>, M.m), 256, 0, s>>>(
+                        M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals, S.x32, e, S.sched)));
+}
+
+template <typename VT>
+static void update_lp(const SirtDev &S, const DevCSR &M, const VT *vals, double scale,
+                      cudaStream_t s) {
+    EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale};
+    FAIR_G_DISPATCH(M.lanes_per_row,
+                    (k_sirt_update_lp<VT, g_><<<chunk_grid(k_sirt_update_lp<VT, g_>, M.m), 256, 0, s>>>(
+                        M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals,
+                        (const float *)S.r, e, S.sched)));
+}
+
 // One pass of a SIRT iteration: pass 1 = residual over A, pass 2 = update over A'.
 static void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
     const DevCSR &M = pass == 1 ? *S.A : *S.AT;
     if (M.m == 0) return;
-    const int64_t *rp = M.rowptr.as<int64_t>();
-    const int32_t *cl = M.col.as<int32_t>();
-    const int G = M.lanes_per_row;
-    if (pass == 1) {
-        if (S.prec == FAIR_PREC_F64) {
+    if (S.prec == FAIR_PREC_F64) {
+        const int64_t *rp = M.rowptr.as<int64_t>();
+        const int32_t *cl = M.col.as<int32_t>();
+        if (pass == 1) {
             EpiResidF64 e{S.b, S.Minv, (double *)S.r};
-            FAIR_G_DISPATCH(G, (k_sirt_resid_f64<g_><<<chunk_grid(k_sirt_resid_f64<g_>, M.m), 256, 0, s>>>(
-                                    rp, M.m, cl, M.v64.as<double>(), S.x, e, S.sched)));
+            FAIR_G_DISPATCH(M.lanes_per_row, (k_sirt_resid_f64<g_><<<chunk_grid(k_sirt_resid_f64<g_>, M.m), 256, 0, s>>>(
+                                                  rp, M.m, cl, M.v64.as<double>(), S.x, e, S.sched)));
         } else {
-            EpiResidLP e{S.b, S.Minv, (float *)S.r};
-            if (S.prec == FAIR_PREC_F32) {
-                FAIR_G_DISPATCH(G, (k_sirt_resid_lp<float, g_><<<chunk_grid(k_sirt_resid_lp<float, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v32.as<float>(), S.x32, e, S.sched)));
-            } else {
-                FAIR_G_DISPATCH(G, (k_sirt_resid_lp<__half, g_><<<chunk_grid(k_sirt_resid_lp<__half, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v16.as<__half>(), S.x32, e, S.sched)));
-            }
-        }
-    } else {
-        if (S.prec == FAIR_PREC_F64) {
             EpiUpdateF64 e{S.D, S.x, S.omg, S.lb, S.ub, S.bmode};
-            FAIR_G_DISPATCH(G, (k_sirt_update_f64<g_><<<chunk_grid(k_sirt_update_f64<g_>, M.m), 256, 0, s>>>(
-                                    rp, M.m, cl, M.v64.as<double>(), (const double *)S.r, e, S.sched)));
-        } else {
-            EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode};
-            if (S.prec == FAIR_PREC_F32) {
-                FAIR_G_DISPATCH(G, (k_sirt_update_lp<float, g_><<<chunk_grid(k_sirt_update_lp<float, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v32.as<float>(), (const float *)S.r, e, S.sched)));
-            } else {
-                FAIR_G_DISPATCH(G, (k_sirt_update_lp<__half, g_><<<chunk_grid(k_sirt_update_lp<__half, g_>, M.m), 256, 0, s>>>(
-                                        rp, M.m, cl, M.v16.as<__half>(), (const float *)S.r, e, S.sched)));
-            }
+            FAIR_G_DISPATCH(M.lanes_per_row, (k_sirt_update_f64<g_><<<chunk_grid(k_sirt_update_f64<g_>, M.m), 256, 0, s>>>(
+                                                  rp, M.m, cl, M.v64.as<double>(), (const double *)S.r, e, S.sched)));
         }
+        return;
+    }
+    if (S.prec == FAIR_PREC_F32) {
+        if (pass == 1) resid_lp(S, M, M.v32.as<float>(), 1.0, s);
+        else update_lp(S, M, M.v32.as<float>(), 1.0, s);
+    } else if (S.prec == FAIR_PREC_F16) {
+        if (pass == 1) resid_lp(S, M, M.v16.as<__half>(), 1.0, s);
+        else update_lp(S, M, M.v16.as<__half>(), 1.0, s);
+    } else if (M.qsigned) {
+        if (pass == 1) resid_lp(S, M, M.vq.as<int16_t>(), M.qscale, s);
+        else update_lp(S, M, M.vq.as<int16_t>(), M.qscale, s);
+    } else {
+        if (pass == 1) resid_lp(S, M, M.vq.as<uint16_t>(), M.qscale, s);
+        else update_lp(S, M, M.vq.as<uint16_t>(), M.qscale, s);
     }
 }
 

@@ -257,6 +257,41 @@ __global__ void k_to_f16(const double *v, int64_t n, __half *o) {
          e += (int64_t)gridDim.x * blockDim.x)
         o[e] = __double2half(v[e]);
 }
+// Largest |v| and smallest v of the array: per-block values, finished on the host.
+__global__ void k_absmax_min(const double *v, int64_t n, double *bmax, double *bmin) {
+    __shared__ double smax[32], smin[32];
+    double mx = 0.0, mn = INFINITY;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        mx = fmax(mx, fabs(v[e]));
+        mn = fmin(mn, v[e]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { smax[wid] = mx; smin[wid] = mn; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { mx = fmax(mx, smax[w]); mn = fmin(mn, smin[w]); }
+        bmax[blockIdx.x] = fmax(smax[0], mx);
+        bmin[blockIdx.x] = fmin(smin[0], mn);
+    }
+}
+
+// 16-bit fixed point: q = round(v / scale), unsigned or signed codes.
+template <typename Q>
+__global__ void k_to_q16(const double *v, int64_t n, double inv_scale, Q *o) {
+    const long long lo = (Q)-1 < 0 ? -32767 : 0, hi = (Q)-1 < 0 ? 32767 : 65535;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        long long q = llrint(v[e] * inv_scale);
+        o[e] = (Q)(q < lo ? lo : (q > hi ? hi : q));
+    }
+}
+
 __global__ void k_scale(double *v, int64_t n, double c) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
          e += (int64_t)gridDim.x * blockDim.x)
@@ -345,7 +380,8 @@ struct EpiStore64 {
 };
 struct EpiStore32 {
     float *y;
-    __device__ void operator()(int64_t i, float acc) const { y[i] = acc; }
+    float scale;  // 1 for FP32/FP16 values, the fixed-point scale for 16-bit codes
+    __device__ void operator()(int64_t i, float acc) const { y[i] = acc * scale; }
 };
 
 template <int G>
@@ -511,6 +547,32 @@ int csr_make_lowprec(DevCSR &A, int prec, cudaStream_t s) {
         FAIR_CUDA(cudaGetLastError());
         A.has16 = true;
     }
+    if (prec == FAIR_PREC_Q16 && !A.hasq) {
+        const int nb = 512;
+        DevBuf ext;
+        FAIR_TRY(ext.grow(sizeof(double) * 2 * nb));
+        k_absmax_min<<<nb, 256, 0, s>>>(A.v64.as<double>(), A.nnz, ext.as<double>(),
+                                        ext.as<double>() + nb);
+        FAIR_CUDA(cudaGetLastError());
+        double h[2 * nb];
+        FAIR_CUDA(cudaMemcpyAsync(h, ext.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+        FAIR_CUDA(cudaStreamSynchronize(s));
+        ext.release();
+        double mx = 0.0, mn = INFINITY;
+        for (int b = 0; b < nb; ++b) { mx = std::max(mx, h[b]); mn = std::min(mn, h[nb + b]); }
+        A.qsigned = mn < 0.0;
+        const double top = A.qsigned ? 32767.0 : 65535.0;
+        A.qscale = mx > 0.0 ? mx / top : 1.0;
+        FAIR_TRY(A.vq.grow(sizeof(uint16_t) * n));  // the pad converts from zeros
+        if (A.qsigned)
+            k_to_q16<int16_t><<<grid_for(256, n), 256, 0, s>>>(A.v64.as<double>(), n, 1.0 / A.qscale,
+                                                               A.vq.as<int16_t>());
+        else
+            k_to_q16<uint16_t><<<grid_for(256, n), 256, 0, s>>>(A.v64.as<double>(), n, 1.0 / A.qscale,
+                                                                A.vq.as<uint16_t>());
+        FAIR_CUDA(cudaGetLastError());
+        A.hasq = true;
+    }
     return FAIR_OK;
 }
 
@@ -521,6 +583,7 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
     // derived copies are rebuilt from the scaled master values
     A.has32 = false;
     A.has16 = false;
+    A.hasq = false;
     return FAIR_OK;
 }
 
@@ -566,14 +629,23 @@ int spmv(const DevCSR &A, int prec, const void *d_x, void *d_y, cudaStream_t s,
             rp, A.m, cl, A.v64.as<double>(), (const double *)d_x, e, sched)));
     } else if (prec == FAIR_PREC_F32) {
         FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(A), prec, s));
-        EpiStore32 e{(float *)d_y};
+        EpiStore32 e{(float *)d_y, 1.0f};
         SPMV_G((k_spmv_lp<float, g_><<<chunk_grid(k_spmv_lp<float, g_>, A.m), 256, 0, s>>>(
             rp, A.m, cl, A.v32.as<float>(), (const float *)d_x, e, sched)));
-    } else {
+    } else if (prec == FAIR_PREC_F16) {
         FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(A), prec, s));
-        EpiStore32 e{(float *)d_y};
+        EpiStore32 e{(float *)d_y, 1.0f};
         SPMV_G((k_spmv_lp<__half, g_><<<chunk_grid(k_spmv_lp<__half, g_>, A.m), 256, 0, s>>>(
             rp, A.m, cl, A.v16.as<__half>(), (const float *)d_x, e, sched)));
+    } else {
+        FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(A), prec, s));
+        EpiStore32 e{(float *)d_y, (float)A.qscale};
+        if (A.qsigned)
+            SPMV_G((k_spmv_lp<int16_t, g_><<<chunk_grid(k_spmv_lp<int16_t, g_>, A.m), 256, 0, s>>>(
+                rp, A.m, cl, A.vq.as<int16_t>(), (const float *)d_x, e, sched)))
+        else
+            SPMV_G((k_spmv_lp<uint16_t, g_><<<chunk_grid(k_spmv_lp<uint16_t, g_>, A.m), 256, 0, s>>>(
+                rp, A.m, cl, A.vq.as<uint16_t>(), (const float *)d_x, e, sched)))
     }
 #undef SPMV_G
     FAIR_CUDA(cudaGetLastError());

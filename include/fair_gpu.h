@@ -52,7 +52,10 @@ const char *fair_last_error_detail(void);
 enum {
     FAIR_PREC_F64 = 0, /* FP64 values, FP64 accumulation (the reference's real(8)) */
     FAIR_PREC_F32 = 1, /* FP32 values and vectors, FP32 accumulation, FP64 weights */
-    FAIR_PREC_F16 = 2  /* FP16-stored values, FP32 vectors/accumulation, FP64 weights */
+    FAIR_PREC_F16 = 2, /* FP16-stored values, FP32 vectors/accumulation, FP64 weights */
+    FAIR_PREC_Q16 = 3  /* 16-bit fixed-point values scaled by the largest |value|
+                          (unsigned when no value is negative), FP32 vectors and
+                          accumulation, FP64 weights and scale */
 };
 
 /* ---- opaque device matrix (type(csr_matrix), sparse_matrices.f90:157) --- */

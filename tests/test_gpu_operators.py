@@ -117,7 +117,7 @@ def test_size_errors(problem, fair):
         fair.CSRMatrix.construct(2, 2, [1.0], np.array([0, 1, 1], np.int32), np.array([3], np.int32))
 
 
-@pytest.mark.parametrize("prec,tol", [("f32", 1e-6), ("f16", 2e-3)])
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-6), ("f16", 2e-3), ("q16", 1e-4)])
 def test_reduced_precision_products(problem, oracle, prec, tol):
     A, R = problem
     x = np.random.default_rng(5).uniform(0, 1, R.n)

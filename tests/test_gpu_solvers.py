@@ -192,7 +192,7 @@ def test_twin_art(par, fair, oracle, rule, method, K):
     assert rel_err(g[4], r[4]) < TOL64
 
 
-@pytest.mark.parametrize("prec,tol", [("f32", 1e-5), ("f16", 5e-3)])
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-5), ("f16", 5e-3), ("q16", 1e-5)])
 def test_sirt_reduced_precision(par, fair, oracle, prec, tol):
     """FP32 / FP16-stored values with FP32 accumulation: error vs the FP64 oracle."""
     A, R, _, b = par
