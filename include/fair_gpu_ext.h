@@ -37,6 +37,23 @@ int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches);
  * vectors: FP64 vectors for FAIR_PREC_F64, FP32 vectors otherwise. */
 int fair_spmv_device(fair_csr h, int32_t trans, const void *d_x, void *d_y);
 
+/* Capacity, in doubles, of the fixed device array behind
+ * fair_matvecmul_noalloc (32 MiB): n + m of the matrix must fit in it. */
+#define FAIR_NOALLOC_MAX_ENTRIES 4194304
+
+/* w(m) = A*v(n) with host vectors, like fair_matvecmul, but without
+ * allocating any GPU memory: for callers that cannot call cudaMalloc during
+ * their run (a program that has reserved the GPU's memory for its own pool,
+ * a real-time loop that cannot take cudaMalloc's device synchronisation, a
+ * job held to a fixed memory budget on a shared GPU). No counterpart in the
+ * reference. The vectors are staged in one fixed device array of
+ * FAIR_NOALLOC_MAX_ENTRIES doubles that every GPU loading the library holds
+ * until exit; larger problems fail with FAIR_ERR_ARG. Computed in FP64 for
+ * any handle precision. The first call on a device looks up the array's
+ * address with that device current: make it before any stream capture.
+ * Calls share the array, so calls that overlap on the GPU race. */
+int fair_matvecmul_noalloc(fair_csr h, const double *v, int64_t size_v, double *w);
+
 #ifdef __cplusplus
 }
 #endif
