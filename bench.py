@@ -123,12 +123,14 @@ def algorithmic_bytes(nnz, m, n, prec):
     return pass1, pass2
 
 
-def traffic_from_profiles(kernel):
-    """Per-launch DRAM bytes of `kernel` recorded from an ncu capture, if any."""
+def traffic_from_profiles(kernel, prec, nnz):
+    """Per-launch DRAM bytes of `kernel` in form `prec` from the ncu capture
+    summarised in profiles/ (recorded for the N=1024 launch), if any."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(kernel)
+            t = json.load(f).get(prec, {}).get(kernel)
+        return None if t is None or nnz != 961254632 else t
     except Exception:
         return None
 
@@ -290,7 +292,7 @@ def run_ours(args):
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
-    traffic = traffic_from_profiles(kname)
+    traffic = traffic_from_profiles(kname, hp, nnz)
     for prec in forms:
         p1, p2 = algorithmic_bytes(nnz, m, n, prec)
         f = forms[prec]
