@@ -121,6 +121,8 @@ def _declare(L):
         "fair_random_seed": ([C.c_uint64], C.c_int),
         "fair_random_number": ([vp, i64], C.c_int),
         "fair_shepplogan": ([i32, vp], C.c_int),
+        "fair_sirt_adjoint": ([h, C.c_char_p, i32, vp, vp, i32, vp, P(Opts), vp, vp, vp, vp, vp],
+                              C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -108,6 +108,33 @@ def twin_art(art_method: str, stoprule: str, A: CSRMatrix, b, Kin, x0=None, y0=N
     return xout, int(fi[0]), Xs.T, Ys.T, EG
 
 
+def sirt_adjoint(sirt_method: str, A: CSRMatrix, b, K: int, lam, gx, x0=None,
+                 opts: Opts | None = None):
+    """Reverse-mode adjoint of K unrolled SIRT steps (fair_sirt_adjoint).
+
+    b: (m,) or (m, nrhs); lam: scalar or (nrhs,); gx = dL/dx_K with the shape of
+    x_K. Returns (x_K, dL/db, dL/dx0, dL/dlam) with the shapes of x_K, b, x_K, lam.
+    Only the bounds of ``opts`` are used (lam is the relaxation parameter)."""
+    b = np.asarray(b, np.float64)
+    single = b.ndim == 1
+    B = b.reshape(b.shape[0], -1)
+    nrhs = B.shape[1]
+    lam_arr = np.broadcast_to(np.asarray(lam, np.float64), (nrhs,)).copy()
+    Bc = np.asfortranarray(B)
+    GX = np.asfortranarray(np.asarray(gx, np.float64).reshape(A.n, nrhs))
+    X0 = None if x0 is None else np.asfortranarray(np.asarray(x0, np.float64).reshape(A.n, nrhs))
+    XK = np.zeros((A.n, nrhs), order="F")
+    GB = np.zeros((A.m, nrhs), order="F")
+    GX0 = np.zeros((A.n, nrhs), order="F")
+    GL = np.zeros(nrhs)
+    check(lib().fair_sirt_adjoint(A.handle, sirt_method.encode(), nrhs, ptr(Bc), ptr(X0), int(K),
+                                  ptr(lam_arr), C.byref(opts) if opts is not None else None,
+                                  ptr(GX), ptr(XK), ptr(GB), ptr(GX0), ptr(GL)))
+    if single:
+        return XK[:, 0], GB[:, 0], GX0[:, 0], float(GL[0])
+    return XK, GB, GX0, GL
+
+
 def scramble(number_of_values: int):
     """scramble, AIRMs.f90:1175-1212."""
     out = np.empty(int(number_of_values), np.int32)

@@ -1144,6 +1144,27 @@ int fair_sirt_run_device_timed(fair_csr h, const double *d_b, double *d_x, int32
     return sirt_iterations_timed(S, K, h->stream, ms_pass1, ms_pass2);
 }
 
+int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const double *b,
+                      const double *x0, int32_t K, const double *lambda, const fair_opts *options,
+                      const double *gx, double *xK, double *gb, double *gx0, double *glam) {
+    ENTER(h);
+    NEED_MATRIX(h);
+    if (!sirt_method || !b || !lambda || !gx || !gb || !gx0 || !glam) return FAIR_ERR_NULL;
+    bool sart;
+    if (!strcmp(sirt_method, "cimmino")) sart = false;
+    else if (!strcmp(sirt_method, "sart")) sart = true;
+    else { set_detail("Not a recognised SIRT method."); return FAIR_ERR_METHOD; }
+    if (nrhs < 1 || K < 0) { set_detail("nrhs >= 1 and K >= 0 required"); return FAIR_ERR_ARG; }
+    if (h->prec != FAIR_PREC_F64 && h->prec != FAIR_PREC_F32) {
+        set_detail("the adjoint runs in FP64 or FP32");
+        return FAIR_ERR_ARG;
+    }
+    OptVals o = read_opts(options);
+    FAIR_TRY(ensure_transpose(h));
+    return sirt_adjoint(h, sart, nrhs, b, x0, K, lambda, o.bmode(), o.lb, o.ub, gx, xK, gb, gx0,
+                        glam);
+}
+
 int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches) {
     if (!h || !launches) return FAIR_ERR_NULL;
     // one FP32 shadow conversion per call in reduced precision, two passes per iteration

@@ -140,6 +140,11 @@ int normest_run(const DevCSR &A, const DevCSR &AT, double *d_v, double *d_vn, do
                 cudaStream_t s);
 int fill_uniform(double *d_v, int64_t n, uint64_t seed, uint64_t ctr, cudaStream_t s);
 
+// Adjoint of unrolled SIRT (adjoint.cu); the handle must hold A and A'.
+int sirt_adjoint(fair_csr h, bool sart, int nrhs, const double *b, const double *x0, int K,
+                 const double *lam, int bmode, double lb, double ub, const double *gx,
+                 double *xK, double *gb, double *gx0, double *glam);
+
 // Kaczmarz sweep (kaczmarz.cu).
 struct SweepDev {
     const DevCSR *A = nullptr;

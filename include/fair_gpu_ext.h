@@ -37,6 +37,19 @@ int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches);
  * vectors: FP64 vectors for FAIR_PREC_F64, FP32 vectors otherwise. */
 int fair_spmv_device(fair_csr h, int32_t trans, const void *d_x, void *d_y);
 
+/* Reverse-mode adjoint of K unrolled SIRT steps with box projection (no
+ * counterpart in the reference; it differentiates the iteration of sirt,
+ * AIRMs.f90:1089-1110). For nrhs right-hand sides sharing the matrix:
+ *   x_{k+1} = P(x_k + lambda_c D^-1 A' M^-1 (b_c - A x_k)),  P = bounds of options
+ * ('cimmino' or 'sart' weights). Given gx = dL/dx_K (n x nrhs, column-major)
+ * it returns gb = dL/db (m x nrhs), gx0 = dL/dx0 (n x nrhs) and glam = dL/dlambda
+ * (nrhs); xK (may be NULL) receives x_K. x0 may be NULL (zeros). Checkpoints
+ * every ceil(sqrt(K)) steps. FP64 for FAIR_PREC_F64, FP32 values and vectors
+ * for FAIR_PREC_F32 (the lambda gradient is summed in FP64). */
+int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const double *b,
+                      const double *x0, int32_t K, const double *lambda, const fair_opts *options,
+                      const double *gx, double *xK, double *gb, double *gx0, double *glam);
+
 /* Capacity, in doubles, of the fixed device array behind
  * fair_matvecmul_noalloc (32 MiB): n + m of the matrix must fit in it. */
 #define FAIR_NOALLOC_MAX_ENTRIES 4194304

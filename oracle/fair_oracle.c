@@ -576,6 +576,76 @@ int or_sirt(const char *method, const or_csr *A, const double *b, int maxits,
     return OR_OK;
 }
 
+/* FP64 adjoint of K unrolled SIRT steps (the iteration of sirt, AIRMs.f90:
+ * 1089-1110, with x_{k+1} = P(x_k + lam * D^-1 A' M^-1 (b - A x_k))): stores
+ * every iterate, then runs the reverse recursion
+ *   gz = gx * [P does not clamp z_k]; glam += <gz, D^-1 g_k>;
+ *   w = M^-1 A D^-1 gz (0 on empty rows); gb += lam w; gx = gz - lam A' w.
+ * Returns x_K, dL/db, dL/dx0 and dL/dlam for gx = dL/dx_K. */
+int or_sirt_adjoint(const char *method, const or_csr *A, const double *b, const double *x0,
+                    int K, double lam, const or_opts *o, const double *gxK, double *xK,
+                    double *gb, double *gx0, double *glam) {
+    int upb = 0, lwrb = 0;
+    double ub = 0.0, lb = 1.0;
+    if (o) { upb = o->upb; lwrb = o->lwrb; ub = o->ubound; lb = o->lbound; }
+    const int64_t m = A->m, n = A->n;
+    int sart = !strcmp(method, "sart");
+    if (!sart && strcmp(method, "cimmino")) return OR_ERR_METHOD;
+    double *M = malloc(8 * m), *D = malloc(8 * n), *r = malloc(8 * m), *w = malloc(8 * m);
+    double *X = malloc(8 * n * (size_t)(K + 1)), *Gk = malloc(8 * n * (size_t)(K > 0 ? K : 1));
+    double *gx = malloc(8 * n), *gz = malloc(8 * n), *t = malloc(8 * n), *h = malloc(8 * n);
+    if (sart) {
+        or_row_norms(A, 1, M, 1);
+        int st = or_column_norms(A, 1, D);
+        if (st) return st;
+    } else {
+        or_row_norms(A, 2, M, 1);
+        for (int64_t i = 0; i < m; ++i) M[i] = (double)A->m * (M[i] * M[i]);
+        for (int64_t j = 0; j < n; ++j) D[j] = 1.0;
+    }
+    for (int64_t j = 0; j < n; ++j) X[j] = x0 ? x0[j] : 0.0;
+    for (int k = 0; k < K; ++k) {
+        double *xk = X + (size_t)k * n, *x1 = X + (size_t)(k + 1) * n, *g = Gk + (size_t)k * n;
+        or_matvecmul(A, xk, r, 1);
+        for (int64_t i = 0; i < m; ++i) r[i] = (b[i] - r[i]) / M[i];
+        or_transvecmul(A, r, g);
+        for (int64_t j = 0; j < n; ++j) {
+            double z = xk[j] + lam * g[j] / D[j];
+            if (upb) z = fmin_f(z, ub);
+            if (lwrb) z = fmax_f(z, lb);
+            x1[j] = z;
+        }
+    }
+    memcpy(xK, X + (size_t)K * n, 8 * n);
+    memcpy(gx, gxK, 8 * n);
+    memset(gb, 0, 8 * m);
+    double gl = 0.0;
+    for (int k = K - 1; k >= 0; --k) {
+        double *xk = X + (size_t)k * n, *g = Gk + (size_t)k * n;
+        for (int64_t j = 0; j < n; ++j) {
+            double z = xk[j] + lam * g[j] / D[j];
+            int pass = 1;
+            double zc = z;
+            if (upb) { pass = pass && z < ub; zc = z < ub ? z : ub; }
+            if (lwrb) pass = pass && zc > lb;
+            gz[j] = pass ? gx[j] : 0.0;
+            gl += gz[j] * (g[j] / D[j]);
+            t[j] = gz[j] / D[j];
+        }
+        or_matvecmul(A, t, w, 1);
+        for (int64_t i = 0; i < m; ++i) {
+            w[i] = M[i] != 0.0 ? w[i] / M[i] : 0.0;
+            gb[i] += lam * w[i];
+        }
+        or_transvecmul(A, w, h);
+        for (int64_t j = 0; j < n; ++j) gx[j] = gz[j] - lam * h[j];
+    }
+    memcpy(gx0, gx, 8 * n);
+    *glam = gl;
+    free(M); free(D); free(r); free(w); free(X); free(Gk); free(gx); free(gz); free(t); free(h);
+    return OR_OK;
+}
+
 /* normest, AIRMs.f90:1129-1173, with the start vector v0 given (the
  * reference draws it with random_number). */
 double or_normest(const or_csr *A, double tol, int maxit, const double *v0, int nthreads) {

@@ -83,6 +83,9 @@ int or_gradient_descent(const or_csr *A, const double *b, int max_iter,
                         int *iters_done, int nthreads);
 double or_normest(const or_csr *A, double tol, int maxit, const double *v0,
                   int nthreads);
+int or_sirt_adjoint(const char *method, const or_csr *A, const double *b, const double *x0,
+                    int K, double lam, const or_opts *o, const double *gxK, double *xK,
+                    double *gb, double *gx0, double *glam);
 void or_scramble(int n, int32_t *out);
 int or_art(const char *method, const or_csr *A, const double *b, const int *Kin,
            int nK, const double *x0, const double *xref, const int32_t *order,

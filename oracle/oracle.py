@@ -96,6 +96,8 @@ def _declare(L):
     L.or_normest.argtypes = [P(_CSR), d, i32, vp, i32]
     L.or_normest.restype = d
     L.or_scramble.argtypes = [i32, vp]
+    L.or_sirt_adjoint.argtypes = [C.c_char_p, P(_CSR), vp, vp, i32, d, P(_Opts), vp, vp, vp,
+                                  vp, P(C.c_double)]
     L.or_art.argtypes = [C.c_char_p, P(_CSR), vp, vp, i32, vp, vp, vp, i32, P(_Opts), vp]
     L.or_twin_art.argtypes = [C.c_char_p, C.c_char_p, P(_CSR), vp, vp, i32, vp, vp, vp,
                               i32, i32, P(_Opts), vp, P(C.c_int), vp, vp, vp]
@@ -298,6 +300,20 @@ def gradient_descent(A: OracleCSR, b, max_iter=100, x0=None, rho=1.5, tol=1e-6,
                                      C.byref(opts) if opts is not None else None,
                                      _p(v0), _p(x), C.byref(it), nthreads))
     return x, it.value
+
+
+def sirt_adjoint(method, A: OracleCSR, b, K, lam, gxK, x0=None, opts=None):
+    """FP64 adjoint of K unrolled SIRT steps (iteration of AIRMs.f90:1089-1110);
+    returns (x_K, dL/db, dL/dx0, dL/dlam) for gxK = dL/dx_K"""
+    b, x0, gxK = _f64(b), _f64(x0), _f64(gxK)
+    xK = np.empty(A.n)
+    gb = np.empty(A.m)
+    gx0 = np.empty(A.n)
+    gl = C.c_double(0.0)
+    _check(lib().or_sirt_adjoint(method.encode(), C.byref(A._c()), _p(b), _p(x0), K, lam,
+                                 C.byref(opts) if opts is not None else None, _p(gxK), _p(xK),
+                                 _p(gb), _p(gx0), C.byref(gl)))
+    return xK, gb, gx0, gl.value
 
 
 def scramble(n):

@@ -291,3 +291,32 @@ def test_twin_art_error_gauge(oracle):
                                            opts=oracle.options(relaxpar=0.5))
     assert 1 <= fi <= 20
     assert EG[1] < EG[0]
+
+
+def test_oracle_adjoint_matches_finite_differences(oracle):
+    """The FP64 CPU adjoint of K unrolled SIRT steps against central
+    differences of the oracle's own sirt (directional derivatives, h = 1e-6)."""
+    N, nth, p = 12, 16, 18
+    R = oracle.paralleltomo(N, nth, p, np.pi * np.arange(nth) / nth)
+    rng = np.random.default_rng(0)
+    xt = oracle.shepplogan(N)
+    b = oracle.matvecmul(R, xt) + 0.01 * rng.standard_normal(R.m)
+    x0 = np.full(R.n, 0.05)
+    K, lam = 8, 1.3
+    o = oracle.options(lbound=0.0)
+
+    def loss(bb, xx0, ll):
+        x = oracle.sirt("cimmino", R, bb, K, x0=xx0, opts=oracle.options(relaxpar=ll, lbound=0.0))
+        return 0.5 * np.sum((x - xt) ** 2), x
+
+    L0, xK = loss(b, x0, lam)
+    xk2, gb, gx0, gl = oracle.sirt_adjoint("cimmino", R, b, K, lam, xK - xt, x0=x0, opts=o)
+    assert np.array_equal(xk2, xK)
+    h = 1e-6
+    db, dx = rng.standard_normal(R.m), rng.standard_normal(R.n)
+    fd_b = (loss(b + h * db, x0, lam)[0] - loss(b - h * db, x0, lam)[0]) / (2 * h)
+    fd_x = (loss(b, x0 + h * dx, lam)[0] - loss(b, x0 - h * dx, lam)[0]) / (2 * h)
+    fd_l = (loss(b, x0, lam + h)[0] - loss(b, x0, lam - h)[0]) / (2 * h)
+    assert abs(fd_b - gb @ db) <= 1e-6 * abs(fd_b)
+    assert abs(fd_x - gx0 @ dx) <= 1e-6 * abs(fd_x)
+    assert abs(fd_l - gl) <= 1e-6 * abs(fd_l)
