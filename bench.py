@@ -354,6 +354,103 @@ def run_ours(args):
     return 0
 
 
+def run_kaczmarz(args):
+    """Kaczmarz family (a secondary measurement, one JSON line per case):
+    fan beam N=512, 720 angles over [0, 2pi), 725 unit bins, R = 2N, three-phase
+    phantom, bounds [0,1], FP64: random Kaczmarz with row-norm probabilities
+    and symmetric Kaczmarz; and fan beam N=128, 360 angles, 181 bins, 10
+    natural-order sweeps with relaxation 0.25. Rows/s and sweeps/s through the
+    host C-ABI call (b in, x out), beside the oracle's serial sweep on one core
+    (the reference's sweep is serial)."""
+    import fortran_airtools_gb300 as F
+    from oracle import oracle as O
+    cases = [
+        ("randkaczmarz", dict(n=512, nth=720, p=725), dict(rowprobability=True, lbound=0.0, ubound=1.0), 2),
+        ("symkaczmarz", dict(n=512, nth=720, p=725), dict(lbound=0.0, ubound=1.0), 2),
+        ("kaczmarz", dict(n=128, nth=360, p=181), dict(relaxpar=0.25), 10),
+    ]
+    for method, g, o, sweeps in cases:
+        th = 2 * np.pi * np.arange(g["nth"]) / g["nth"]
+        d = F.Data(n=g["n"], p=g["p"], nth=g["nth"], r=2.0, dw=g["p"] / g["n"], sd=2.0, theta=th)
+        A = F.fanlineartomo(d)
+        m, n, nnz = A.info()
+        xt = F.phantomgallery.three_phases(g["n"], seed=4) if g["n"] == 512 else \
+            F.phantomgallery.shepplogan(g["n"])
+        b = noisy(A.matvecmul(xt), seed=4)
+        opts = F.airms.options(**o)
+        nrow = int(np.count_nonzero(A.row_norms(2)))
+        F.airms.random_seed(4)
+        F.airms.art(method, A, b, [2 if method == "symkaczmarz" else 1], opts=opts)  # warm-up
+        F.airms.random_seed(4)
+        t0 = time.perf_counter()
+        F.airms.art(method, A, b, [sweeps], opts=opts)
+        gpu_s = time.perf_counter() - t0
+        rows = nrow * sweeps  # row projections (symkaczmarz: K counts single sweeps)
+        cpu = None
+        if not args.no_cpu:
+            vA, IA, JA = A.arrays()
+            R = O.OracleCSR(m, n, IA, JA, vA)
+            ro = O.options(**o)
+            O.random_seed(4)
+            k = 2 if method == "symkaczmarz" else 1
+            t0 = time.perf_counter()
+            O.art(method, R, b, [k], opts=ro)
+            cpu_s = (time.perf_counter() - t0) / k
+            cpu = {"value": nrow / cpu_s, "unit": "rows/s", "cores": 1, "kind": "port",
+                   "sample": f"{k} sweep(s) of the same problem"}
+        line = {"metric": f"{method} rows/s", "workload": f"fan N={g['n']}, {g['nth']} angles, {g['p']} bins",
+                "value": rows / gpu_s, "unit": "rows/s", "sweeps_per_s": sweeps / gpu_s,
+                "sweeps": sweeps, "nonzero_rows": nrow, "nnz": nnz, "dtype": "f64",
+                "note": "fair_art host call: b uploaded, x downloaded", "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+        A.close()
+    return 0
+
+
+def run_adjoint(args):
+    """Differentiation workload (secondary lines): 16 parallel-beam problems
+    N=256, 360 angles over [0, pi), 363 bins sharing one matrix, random-ellipse
+    phantoms (seed 3), K=20 SIRT steps with the nonnegativity projection, loss
+    0.5 ||x_K - x_true||^2; one fair_sirt_adjoint call returns x_K and the
+    gradients for all 16 problems. FP64 and FP32, beside the oracle's FP64
+    adjoint of one problem on one core scaled to 16."""
+    import fortran_airtools_gb300 as F
+    from oracle import oracle as O
+    n, nth, p, K, nb = 256, 360, 363, 20, 16
+    th = np.pi * np.arange(nth) / nth
+    A = F.paralleltomo(F.Data(n=n, p=p, nth=nth, theta=th))
+    m = A.m
+    X = np.stack([F.phantomgallery.random_ellipses(n, seed=3 + s) for s in range(nb)], 1)
+    B = np.stack([noisy(A.matvecmul(X[:, c]), seed=3 + c) for c in range(nb)], 1)
+    lam = np.full(nb, 1.5)
+    o = F.airms.options(lbound=0.0)
+    cpu = None
+    for prec in ("f64", "f32"):
+        A.set_precision(prec)
+        xK, _, _, _ = F.airms.sirt_adjoint("cimmino", A, B, K, lam, np.zeros((A.n, nb)), opts=o)
+        GX = xK - X
+        F.airms.sirt_adjoint("cimmino", A, B, K, lam, GX, opts=o)  # warm-up
+        t0 = time.perf_counter()
+        F.airms.sirt_adjoint("cimmino", A, B, K, lam, GX, opts=o)
+        dt = time.perf_counter() - t0
+        if cpu is None and not args.no_cpu:
+            vA, IA, JA = A.arrays()
+            R = O.OracleCSR(m, A.n, IA, JA, vA)
+            t0 = time.perf_counter()
+            O.sirt_adjoint("cimmino", R, B[:, 0], K, 1.5, GX[:, 0], opts=O.options(lbound=0.0))
+            c1 = time.perf_counter() - t0
+            cpu = {"value": 1.0 / (c1 * nb), "unit": "batch gradients/s", "cores": 1,
+                   "kind": "port", "sample": "one problem's FP64 adjoint, scaled to 16 problems"}
+        print(json.dumps({"metric": "adjoint of K=20 SIRT steps, 16 problems", "value": 1.0 / dt,
+                          "unit": "batch gradients/s", "ms_per_batch": dt * 1e3,
+                          "workload": f"parallel N={n}, {nth} angles, {p} bins, 16 right-hand sides",
+                          "dtype": prec, "nnz": A.nnz, "cpu_baseline": cpu,
+                          "note": "fair_sirt_adjoint host call: forward with sqrt(K) checkpoints, "
+                                  "recomputation and reverse sweep"}), flush=True)
+    A.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -365,6 +462,8 @@ def main():
     ap.add_argument("--n", type=int, default=1024, help="image size N (profiling cases)")
     ap.add_argument("--angles", type=int, default=720)
     ap.add_argument("--bins", type=int, default=1448)
+    ap.add_argument("--workload", choices=["sirt", "kaczmarz", "adjoint"], default="sirt",
+                    help="sirt: the headline line; kaczmarz, adjoint: secondary lines")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -373,6 +472,10 @@ def main():
     WORKLOAD = (f"parallel-beam N={N}, {NTH} angles over [0,pi), {P} bins; SIRT (Cimmino)")
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "kaczmarz":
+        return run_kaczmarz(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_ours(args)
 
 
