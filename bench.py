@@ -409,14 +409,14 @@ def run_kaczmarz(args):
 
 def run_adjoint(args):
     """Differentiation workload (secondary lines): 16 parallel-beam problems
-    N=256, 360 angles over [0, pi), 363 bins sharing one matrix, random-ellipse
+    N=256, 360 angles over [0, pi), 362 bins sharing one matrix, random-ellipse
     phantoms (seed 3), K=20 SIRT steps with the nonnegativity projection, loss
     0.5 ||x_K - x_true||^2; one fair_sirt_adjoint call returns x_K and the
     gradients for all 16 problems. FP64 and FP32, beside the oracle's FP64
     adjoint of one problem on one core scaled to 16."""
     import fortran_airtools_gb300 as F
     from oracle import oracle as O
-    n, nth, p, K, nb = 256, 360, 363, 20, 16
+    n, nth, p, K, nb = 256, 360, 362, 20, 16
     th = np.pi * np.arange(nth) / nth
     A = F.paralleltomo(F.Data(n=n, p=p, nth=nth, theta=th))
     m = A.m

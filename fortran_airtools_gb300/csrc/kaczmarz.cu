@@ -1,15 +1,42 @@
 // kaczmarz.cu -- the ordered row-action sweep of basic_sweep
-// (AIRMs.f90:813-858) as one thread block that walks the rows strictly in the
-// reference's order; the threads of the block share each row's dot product
-// (csr_matrowvec, sparse_matrices.f90:252-270) and its bounded update
-// (add_mult_row, :795-822). Row i+1 starts only after row i's update is
-// visible to the whole block (one barrier per row), so the iterate follows the
-// reference's sequence of projections; only the summation order inside a dot
-// product differs (a tree instead of a left-to-right sum).
+// (AIRMs.f90:813-858) on the GPU.
+//
+// The sweep is strictly sequential (adjacent rays share pixels), so one
+// thread block walks the reference's row order; its W warps share each row's
+// dot product (csr_matrowvec, sparse_matrices.f90:252-270) and bounded update
+// (add_mult_row, :795-822). Row k+1 starts only after row k's update is
+// visible, so the iterate follows the reference's sequence of projections.
+// Three roundings differ from the reference: the order of the sums inside a
+// dot product, the update as one fused multiply-add, and the coefficient
+// formed as (b_i - a_i.x) * (omega / nrA_i) instead of
+// omega * (b_i - a_i.x) / nrA_i (AIRMs.f90:842).
+//
+// On GB300 every FP64 warp instruction holds its SM sub-partition's FP64 pipe
+// for 64 cycles (measured: a dependent and an independent chain of DFMA both
+// issue one per 64 cycles per warp), whatever its active lanes, and a
+// row-action sweep runs on one SM; a row is a dependent chain of about ten
+// FP64 operations (dot product, reduction tree, coefficient, update). The kernel therefore spends FP64 instructions only
+// where the arithmetic needs them:
+//  * a row's entries are spread densely over the block (len / (32 W)
+//    instructions per lane, skipped by a block-uniform branch past the end);
+//  * partial sums go to shared memory and one warp finishes the sum
+//    (W - 1 + 5 additions) and the coefficient, instead of every warp;
+//  * omega / nrA_i, b_i and each step's entry range come from a parallel
+//    schedule kernel, together with the row sampled by row probability
+//    (AIRMs.f90:830-835);
+//  * the box constraints are applied with integer comparisons on an
+//    order-preserving key of the IEEE bits (the gfortran MAX/MIN semantics:
+//    a NaN operand loses, +0 and -0 compare equal).
+// The step record two rows ahead and the next row's column indices and
+// values are prefetched while the current row is worked on, and the gathered
+// values of x stay in registers for the update.
 //
 // When the iterate fits in shared memory it is kept there for the whole
 // sweep; otherwise it stays in global memory (L2-resident at these sizes).
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "fair_internal.cuh"
 
@@ -17,15 +44,13 @@ namespace fair {
 
 namespace {
 
-constexpr int kSweepThreads = 256;
-constexpr int kSweepWarps = kSweepThreads / 32;
-constexpr int kCache = 8;  // row entries held in registers per thread
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
+struct RowStep {
+    int64_t s;    // first entry of the row
+    int32_t len;  // entries
+    int32_t pad;
+    double b;     // b(ri)
+    double w;     // omega / nrA(ri)
+};
 
 // first index i in [0, m) with cumul[i] >= u (the linear scan of
 // AIRMs.f90:831-835 finds the same row on the nondecreasing cumul); m-1 if none
@@ -38,101 +63,230 @@ __device__ __forceinline__ int32_t sample_row(const double *cumul, int32_t m, do
     return L < m ? L : m - 1;
 }
 
-template <bool SMEM_X, bool ROWPROB>
-__global__ void __launch_bounds__(kSweepThreads) k_sweep(
-    const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
-    const double *__restrict__ val, const double *__restrict__ b,
-    const double *__restrict__ nrA, const double *__restrict__ cumul, int32_t m, int32_t n,
-    double *xg, const int32_t *__restrict__ ord, int32_t nord, int dir, double omg, int bmode,
-    double lb, double ub, uint64_t seed, uint64_t ctr) {
-    extern __shared__ double xs[];
-    __shared__ double red[kSweepWarps];
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    double *x = SMEM_X ? xs : xg;
-    if (SMEM_X) {
-        for (int32_t j = tid; j < n; j += kSweepThreads) xs[j] = xg[j];
-        __syncthreads();
-    }
-    for (int32_t ii = 0; ii < nord; ++ii) {
-        int32_t ri;
-        if (ROWPROB) ri = sample_row(cumul, m, uniform01(seed, ctr + (uint64_t)ii));
-        else ri = __ldg(ord + (dir > 0 ? ii : nord - 1 - ii)) - 1;
-        const int64_t s = __ldg(rowptr + ri), e = __ldg(rowptr + ri + 1);
-        int32_t cc[kCache];
-        double vv[kCache];
-        double part = 0.0;
-#pragma unroll
-        for (int q = 0; q < kCache; ++q) {
-            int64_t j = s + tid + (int64_t)q * kSweepThreads;
-            if (j < e) {
-                cc[q] = __ldg(col + j);
-                vv[q] = __ldg(val + j);
-                part += x[cc[q]] * vv[q];
-            }
-        }
-        for (int64_t j = s + tid + (int64_t)kCache * kSweepThreads; j < e; j += kSweepThreads)
-            part += x[__ldg(col + j)] * __ldg(val + j);
-        part = warp_sum(part);
-        if (lane == 0) red[wid] = part;
-        __syncthreads();
-        double inp = 0.0;
-#pragma unroll
-        for (int w = 0; w < kSweepWarps; ++w) inp += red[w];
-        // coeff = omg*(b(ri) - inp)/nrA(ri), AIRMs.f90:842
-        const double coeff = __ddiv_rn(__dmul_rn(omg, __dsub_rn(__ldg(b + ri), inp)), __ldg(nrA + ri));
-#pragma unroll
-        for (int q = 0; q < kCache; ++q) {
-            int64_t j = s + tid + (int64_t)q * kSweepThreads;
-            if (j < e) {
-                double t = __dadd_rn(x[cc[q]], __dmul_rn(coeff, vv[q]));
-                if (bmode & 2) t = fmax_f(t, lb);
-                if (bmode & 1) t = fmin_f(t, ub);
-                x[cc[q]] = t;
-            }
-        }
-        for (int64_t j = s + tid + (int64_t)kCache * kSweepThreads; j < e; j += kSweepThreads) {
-            int32_t c = __ldg(col + j);
-            double t = __dadd_rn(x[c], __dmul_rn(coeff, __ldg(val + j)));
-            if (bmode & 2) t = fmax_f(t, lb);
-            if (bmode & 1) t = fmin_f(t, ub);
-            x[c] = t;
-        }
-        __syncthreads();
-    }
-    if (SMEM_X) {
-        for (int32_t j = tid; j < n; j += kSweepThreads) xg[j] = xs[j];
+__global__ void k_sweep_schedule(const int32_t *ord, int32_t nord, int dir, int rowprob,
+                                 const double *cumul, int32_t m, uint64_t seed, uint64_t ctr,
+                                 const int64_t *rowptr, const double *b, const double *nrA,
+                                 double omg, RowStep *steps) {
+    for (int32_t ii = blockIdx.x * blockDim.x + threadIdx.x; ii < nord;
+         ii += gridDim.x * blockDim.x) {
+        int32_t ri = rowprob ? sample_row(cumul, m, uniform01(seed, ctr + (uint64_t)ii))
+                             : ord[dir > 0 ? ii : nord - 1 - ii] - 1;
+        int64_t s = rowptr[ri];
+        steps[ii] = RowStep{s, (int32_t)(rowptr[ri + 1] - s), 0, b[ri], __ddiv_rn(omg, nrA[ri])};
     }
 }
 
-template <bool SMEM_X, bool ROWPROB>
-int launch_sweep(const SweepDev &S, int dir, size_t smem, cudaStream_t s) {
-    auto kern = k_sweep<SMEM_X, ROWPROB>;
-    if (SMEM_X) FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem));
+// Order-preserving key of a non-NaN double: key(-x) = -key(x), key(+-0) = 0.
+__host__ __device__ __forceinline__ long long okey(long long bits) {
+    long long mag = bits & 0x7FFFFFFFFFFFFFFFLL;
+    return bits < 0 ? -mag : mag;
+}
+__device__ __forceinline__ bool is_nan_bits(long long bits) {
+    return (bits & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
+}
+
+struct Box {
+    int mode;  // bit0: upper bound, bit1: lower bound
+    long long klb, kub;
+    double lb, ub;
+    // add_mult_row (sparse_matrices.f90:812-818): MAX(t, lb) first, then
+    // MIN(t, ub); MAX/MIN return the non-NaN operand
+    __device__ __forceinline__ double apply(double t) const {
+        if (mode & 2) {
+            long long tb = __double_as_longlong(t);
+            if (klb > okey(tb) || is_nan_bits(tb)) t = lb;
+        }
+        if (mode & 1) {
+            long long tb = __double_as_longlong(t);
+            if (kub < okey(tb) || is_nan_bits(tb)) t = ub;
+        }
+        return t;
+    }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int W, int CACHE, bool SMEM_X>
+__global__ void __launch_bounds__(32 * W) k_sweep(const RowStep *__restrict__ steps, int32_t nord,
+                                                  const int32_t *__restrict__ col,
+                                                  const double *__restrict__ val, double *xg,
+                                                  int32_t n, Box box) {
+    constexpr int T = 32 * W;
+    extern __shared__ double xs[];
+    __shared__ double part_s[W > 1 ? T : 1];
+    __shared__ double coeff_s;
+    const int tid = threadIdx.x, lane = tid & 31;
+    double *x = SMEM_X ? xs : xg;
+    if (SMEM_X) {
+        for (int32_t j = tid; j < n; j += T) xs[j] = xg[j];
+        __syncthreads();
+    }
+    if (nord <= 0) return;
+    const RowStep none{0, 0, 0, 0.0, 0.0};
+    // three-stage pipeline: the step record two rows ahead, the entries of
+    // the next row, the current row
+    RowStep cur = steps[0];
+    RowStep nxt = nord > 1 ? steps[1] : none;
+    int32_t cc[CACHE];
+    double vv[CACHE];
+    int nq = (cur.len + T - 1) / T;
+#pragma unroll
+    for (int q = 0; q < CACHE; ++q) {
+        if (q >= nq) break;
+        int k = tid + q * T;
+        cc[q] = k < cur.len ? __ldg(col + cur.s + k) : 0;
+        vv[q] = k < cur.len ? __ldg(val + cur.s + k) : 0.0;
+    }
+    for (int32_t ii = 0; ii < nord; ++ii) {
+        const RowStep nxt2 = ii + 2 < nord ? steps[ii + 2] : none;
+        const int nqn = (nxt.len + T - 1) / T;
+        int32_t nc[CACHE];
+        double nv[CACHE];
+#pragma unroll
+        for (int q = 0; q < CACHE; ++q) {
+            if (q >= nqn) break;
+            int k = tid + q * T;
+            nc[q] = k < nxt.len ? __ldg(col + nxt.s + k) : 0;
+            nv[q] = k < nxt.len ? __ldg(val + nxt.s + k) : 0.0;
+        }
+        // dot product of the row with x (two independent accumulators)
+        double xo[CACHE];
+        double p0 = 0.0, p1 = 0.0;
+#pragma unroll
+        for (int q = 0; q < CACHE; ++q) {
+            if (q >= nq) break;
+            int k = tid + q * T;
+            xo[q] = k < cur.len ? x[cc[q]] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < CACHE; ++q) {
+            if (q >= nq) break;
+            if (q & 1) p1 = fma(xo[q], vv[q], p1); else p0 = fma(xo[q], vv[q], p0);
+        }
+        for (int k = tid + CACHE * T; k < cur.len; k += T)
+            p0 = fma(x[__ldg(col + cur.s + k)], __ldg(val + cur.s + k), p0);
+        const double part = nq > 1 ? p0 + p1 : p0;
+        double coeff;
+        if (W > 1) {
+            part_s[tid] = part;
+            __syncthreads();
+            if (tid < 32) {
+                double t = part_s[lane];
+#pragma unroll
+                for (int w = 1; w < W; ++w) t += part_s[lane + 32 * w];
+                t = warp_sum(t);
+                if (lane == 0) coeff_s = __dmul_rn(__dsub_rn(cur.b, t), cur.w);
+            }
+            __syncthreads();
+            coeff = coeff_s;
+        } else {
+            coeff = __dmul_rn(__dsub_rn(cur.b, warp_sum(part)), cur.w);
+        }
+#pragma unroll
+        for (int q = 0; q < CACHE; ++q) {
+            if (q >= nq) break;
+            int k = tid + q * T;
+            if (k < cur.len) x[cc[q]] = box.apply(fma(coeff, vv[q], xo[q]));
+        }
+        for (int k = tid + CACHE * T; k < cur.len; k += T) {
+            int32_t c = __ldg(col + cur.s + k);
+            x[c] = box.apply(fma(coeff, __ldg(val + cur.s + k), x[c]));
+        }
+        if (W > 1) __syncthreads(); else __syncwarp();
+        cur = nxt;
+        nxt = nxt2;
+        nq = nqn;
+#pragma unroll
+        for (int q = 0; q < CACHE; ++q) { cc[q] = nc[q]; vv[q] = nv[q]; }
+    }
+    if (SMEM_X) {
+        __syncthreads();
+        for (int32_t j = tid; j < n; j += T) xg[j] = xs[j];
+    }
+}
+
+template <int W, int CACHE>
+int launch(const SweepDev &S, const RowStep *steps, bool smem, size_t smem_bytes, const Box &box,
+           cudaStream_t s) {
     const DevCSR &A = *S.A;
-    kern<<<1, kSweepThreads, smem, s>>>(A.rowptr.as<int64_t>(), A.col.as<int32_t>(),
-                                        A.v64.as<double>(), S.b, S.nrA, S.cumul, A.m, A.n, S.x,
-                                        S.ord, S.nord, dir, S.omg, S.bmode, S.lb, S.ub, S.seed,
-                                        S.ctr);
+    if (smem) {
+        auto kern = k_sweep<W, CACHE, true>;
+        FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem_bytes));
+        kern<<<1, 32 * W, smem_bytes, s>>>(steps, S.nord, A.col.as<int32_t>(), A.v64.as<double>(),
+                                          S.x, A.n, box);
+    } else {
+        k_sweep<W, CACHE, false><<<1, 32 * W, 0, s>>>(steps, S.nord, A.col.as<int32_t>(),
+                                                     A.v64.as<double>(), S.x, A.n, box);
+    }
     FAIR_CUDA(cudaGetLastError());
     return FAIR_OK;
+}
+
+long long host_key(double v) {
+    long long bits;
+    memcpy(&bits, &v, sizeof bits);
+    return okey(bits);
+}
+
+// Warps per row: FAIR_SWEEP_WARPS (1, 2, 4 or 8) when set, else 2 when x is
+// in shared memory and 8 when it is in global memory (more gathers in
+// flight). Measured on GB300, fan beam N=128 (x in shared memory): 0.76M,
+// 0.90M, 0.88M, 0.80M rows/s for 1, 2, 4, 8 warps; N=512 (x in global
+// memory): 0.18M, 0.32M, 0.41M, 0.42M rows/s.
+int sweep_warps(bool smem) {
+    const char *env = getenv("FAIR_SWEEP_WARPS");
+    if (env) {
+        int w = atoi(env);
+        if (w == 1 || w == 2 || w == 4 || w == 8) return w;
+    }
+    return smem ? 2 : 8;
 }
 
 }  // namespace
 
 int kaczmarz_sweep(const SweepDev &S, int dir, cudaStream_t s) {
     if (S.nord <= 0) return FAIR_OK;
+    static thread_local DevBuf stepbuf;  // schedule of one sweep (grown on demand)
+    FAIR_TRY(stepbuf.grow(sizeof(RowStep) * (size_t)S.nord));
+    RowStep *steps = stepbuf.as<RowStep>();
+    const DevCSR &A = *S.A;
+    int grid = (int)std::min<int64_t>(((int64_t)S.nord + 255) / 256, (int64_t)sm_count() * 8);
+    k_sweep_schedule<<<grid, 256, 0, s>>>(S.ord, S.nord, dir, S.rand_rowprob ? 1 : 0, S.cumul, A.m,
+                                          S.seed, S.ctr, A.rowptr.as<int64_t>(), S.b, S.nrA,
+                                          S.omg, steps);
+    FAIR_CUDA(cudaGetLastError());
+    Box box;
+    // a NaN bound leaves t unchanged unless t is NaN (MAX/MIN semantics); the
+    // bound is then dropped, which differs only in the NaN payload
+    box.mode = (S.bmode & 2) && !std::isnan(S.lb) ? 2 : 0;
+    box.mode |= (S.bmode & 1) && !std::isnan(S.ub) ? 1 : 0;
+    box.lb = S.lb;
+    box.ub = S.ub;
+    box.klb = host_key(S.lb);
+    box.kub = host_key(S.ub);
     int dev = 0, optin = 0;
     FAIR_CUDA(cudaGetDevice(&dev));
     FAIR_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    size_t need = sizeof(double) * (size_t)S.A->n;
-    bool smem = need + 1024 <= (size_t)optin;
-    if (smem) {
-        return S.rand_rowprob ? launch_sweep<true, true>(S, dir, need, s)
-                              : launch_sweep<true, false>(S, dir, need, s);
+    const size_t need = sizeof(double) * (size_t)A.n;
+    const bool smem = need + 4096 <= (size_t)optin;
+    const int W = sweep_warps(smem);
+    // entries per lane held in registers (longer rows finish in a loop)
+    const int per_lane = (A.max_row + 32 * W - 1) / (32 * W);
+    switch (W) {
+    case 1: return per_lane <= 8 ? launch<1, 8>(S, steps, smem, need, box, s)
+                                 : launch<1, 16>(S, steps, smem, need, box, s);
+    case 2: return per_lane <= 8 ? launch<2, 8>(S, steps, smem, need, box, s)
+                                 : launch<2, 16>(S, steps, smem, need, box, s);
+    case 4: return per_lane <= 4 ? launch<4, 4>(S, steps, smem, need, box, s)
+                                 : launch<4, 8>(S, steps, smem, need, box, s);
+    default: return per_lane <= 2 ? launch<8, 2>(S, steps, smem, need, box, s)
+                                  : launch<8, 4>(S, steps, smem, need, box, s);
     }
-    return S.rand_rowprob ? launch_sweep<false, true>(S, dir, 0, s)
-                          : launch_sweep<false, false>(S, dir, 0, s);
 }
 
 }  // namespace fair
