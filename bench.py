@@ -114,12 +114,22 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-def algorithmic_bytes(nnz, m, n, prec):
-    """Bytes each SIRT pass must move once (matrix streamed, vectors once)."""
+def algorithmic_bytes(nnz, m, n, prec, packed=None):
+    """Bytes each SIRT pass must move once (matrix streamed, vectors once).
+    `packed` = (info of A, info of A') when the reduced form runs on the
+    packed index stream: 8 bytes of index per group of 4 entries, 4 padded
+    values per group, 16 bytes per escaped group."""
     sv = VAL_BYTES[prec]
     sx = 8 if prec == "f64" else 4
-    pass1 = nnz * (sv + 4) + (m + 1) * 8 + n * sx + m * 8 + m * 8 + m * sx
-    pass2 = nnz * (sv + 4) + (n + 1) * 8 + m * sx + 2 * n * 8 + (0 if prec == "f64" else n * 4)
+
+    def matrix(info):
+        if info is None or prec == "f64" or not info["has"]:
+            return nnz * (sv + 4)
+        return info["ngroups"] * (8 + 4 * sv) + info["nesc"] * 16
+
+    pa, pt = packed if packed else (None, None)
+    pass1 = matrix(pa) + (m + 1) * 8 + n * sx + m * 8 + m * 8 + m * sx
+    pass2 = matrix(pt) + (n + 1) * 8 + m * sx + 2 * n * 8 + (0 if prec == "f64" else n * 4)
     return pass1, pass2
 
 
@@ -240,9 +250,20 @@ def run_ours(args):
 
     forms = {}
     results = {}
-    for prec in ("f64", "f32", "f16", "q16"):
+    packed = {}
+    form_list = ["f64"] + [f for f in args.forms.split(",") if f and f != "f64"]
+    if args.prec not in form_list:
+        form_list.append(args.prec)
+    for prec in form_list:
         A.set_precision(prec)
         check(L.fair_sirt_prepare(h, b"cimmino", C.byref(opts)))
+        cfg = (C.c_int32 * 4)(8, 8, 1, 1)
+        if args.lanes:  # fixed lanes per row (and groups per lane) of the two passes
+            v = [int(t) for t in args.lanes.split(",")]
+            cfg[:] = (v + [1, 1])[:4] if len(v) == 2 else v[:4]
+            check(L.fair_sirt_set_lanes(h, cfg))
+        elif not args.no_tune:  # fastest lanes per row / groups per lane of each pass
+            check(L.fair_sirt_autotune(h, d_b.data_ptr(), d_x.data_ptr(), 3, cfg))
         with torch.cuda.stream(stream):
             d_x.zero_()
             check(L.fair_sirt_run_device(h, d_b.data_ptr(), d_x.data_ptr(), args.warmup))
@@ -278,23 +299,32 @@ def run_ours(args):
         check(L.fair_sirt_launches(h, args.steps, C.byref(launches)))
         forms[prec] = {"iter_per_s": world * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
                        "pass1_ms": ms1.value / kt, "pass2_ms": ms2.value / kt,
-                       "launches": launches.value, "clocks": clocks}
-    for prec in ("f32", "f16", "q16"):
+                       "launches": launches.value, "clocks": clocks,
+                       "pass_config": None if args.no_tune and not args.lanes else
+                       {"lanes_per_row": [cfg[0], cfg[1]], "groups_per_lane": [cfg[2], cfg[3]]}}
+        if prec != "f64":
+            pk = (A.packed_info(), A.packed_info(transposed=True))
+            if pk[0]["has"] or pk[1]["has"]:
+                packed[prec] = pk
+                forms[prec]["packed_index"] = {"A": pk[0], "AT": pk[1]}
+    for prec in form_list[1:]:
         r = results["f64"]
         forms[prec]["rel_err_vs_f64"] = float(np.linalg.norm(results[prec] - r) / np.linalg.norm(r))
 
     hp = args.prec
     head = forms[hp]
     peak, peak_kind = hbm_peak()
-    b1, b2 = algorithmic_bytes(nnz, m, n, hp)
+    b1, b2 = algorithmic_bytes(nnz, m, n, hp, packed.get(hp))
     dom = 2 if head["pass2_ms"] >= head["pass1_ms"] else 1
-    kname = {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + ("_f64" if hp == "f64" else "_lp")
+    pk = packed.get(hp)
+    kind = "_f64" if hp == "f64" else ("_pk" if pk and pk[dom - 1]["has"] else "_lp")
+    kname = {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kind
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     traffic = traffic_from_profiles(kname, hp, nnz)
     for prec in forms:
-        p1, p2 = algorithmic_bytes(nnz, m, n, prec)
+        p1, p2 = algorithmic_bytes(nnz, m, n, prec, packed.get(prec))
         f = forms[prec]
         f["iteration_gbs"] = (p1 + p2) / (f["ms_per_step"] / 1e3) / 1e9
         f["iteration_frac_of_hbm"] = f["iteration_gbs"] / peak
@@ -458,6 +488,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--prec", choices=["f64", "f32", "f16", "q16"], default="f64")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep 8 lanes per row instead of autotuning each pass")
+    ap.add_argument("--lanes", default="",
+                    help="fixed lanes per row of pass 1 and pass 2 and optionally groups per lane, "
+                         "e.g. 8,4 or 8,4,2,2 (no autotuning)")
+    ap.add_argument("--forms", default="f32,f16,q16",
+                    help="reduced forms timed after FP64 (comma list of f32, f16, q16)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
     ap.add_argument("--n", type=int, default=1024, help="image size N (profiling cases)")
     ap.add_argument("--angles", type=int, default=720)

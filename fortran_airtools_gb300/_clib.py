@@ -123,6 +123,9 @@ def _declare(L):
         "fair_shepplogan": ([i32, vp], C.c_int),
         "fair_sirt_adjoint": ([h, C.c_char_p, i32, vp, vp, i32, vp, P(Opts), vp, vp, vp, vp, vp],
                               C.c_int),
+        "fair_csr_packed_info": ([h, i32, P(i32), P(i64), P(i64), P(i32), P(i32)], C.c_int),
+        "fair_sirt_autotune": ([h, vp, vp, i32, vp], C.c_int),
+        "fair_sirt_set_lanes": ([h, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -59,6 +59,12 @@ void DevBuf::release() {
 void DevCSR::release() {
     rowptr.release(); col.release(); v64.release(); v32.release(); v16.release(); vq.release();
     has32 = has16 = hasq = false;
+    prow.release(); gidx.release(); gside.release(); pv32.release(); pv16.release(); pvq.release();
+    pk_tried = haspk = hasp32 = hasp16 = haspq = false;
+    for (int &g : sirt_lanes) g = 8;
+    for (int &g : sirt_groups) g = 1;
+    ngroups = nesc = 0;
+    stride_hint = tstride_hint = 0;
     m = n = 0;
     nnz = 0;
     max_row = 0;
@@ -1090,10 +1096,7 @@ int fair_sirt_prepare(fair_csr h, const char *sirt_method, const fair_opts *opti
     FAIR_TRY(h->s_r.grow(sizeof(double) * ((size_t)m + 1)));
     FAIR_TRY(h->s_x32.grow(sizeof(float) * ((size_t)n + 1)));
     FAIR_TRY(sirt_weights(h->A, h->AT, sart, h->s_M.as<double>(), h->s_D.as<double>(), s));
-    if (h->prec != FAIR_PREC_F64) {
-        FAIR_TRY(csr_make_lowprec(h->A, h->prec, s));
-        FAIR_TRY(csr_make_lowprec(h->AT, h->prec, s));
-    }
+    FAIR_TRY(sirt_make_forms(h->A, h->AT, h->prec, s));
     FAIR_CUDA(cudaStreamSynchronize(s));
     h->sirt_sart = sart;
     h->sirt_prec = h->prec;
@@ -1144,6 +1147,41 @@ int fair_sirt_run_device_timed(fair_csr h, const double *d_b, double *d_x, int32
     return sirt_iterations_timed(S, K, h->stream, ms_pass1, ms_pass2);
 }
 
+int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
+                       int32_t *config) {
+    ENTER(h);
+    if (reps < 1) { set_detail("reps >= 1 required"); return FAIR_ERR_ARG; }
+    SirtDev S;
+    FAIR_TRY(device_sirt(h, d_b, d_x, S));
+    FAIR_TRY(sirt_autotune(S, h->A, h->AT, reps, h->stream, nullptr));
+    if (config) {
+        config[0] = h->A.sirt_lanes[h->prec];
+        config[1] = h->AT.sirt_lanes[h->prec];
+        config[2] = h->A.sirt_groups[h->prec];
+        config[3] = h->AT.sirt_groups[h->prec];
+    }
+    return FAIR_OK;
+}
+
+int fair_sirt_set_lanes(fair_csr h, const int32_t *config) {
+    ENTER(h);
+    NEED_MATRIX(h);
+    if (!config) return FAIR_ERR_NULL;
+    auto lanes_ok = [](int32_t g) { return g == 4 || g == 8 || g == 16 || g == 32; };
+    auto groups_ok = [](int32_t g) { return g == 1 || g == 2; };
+    if (!lanes_ok(config[0]) || !lanes_ok(config[1]) || !groups_ok(config[2]) ||
+        !groups_ok(config[3])) {
+        set_detail("lanes per row must be 4, 8, 16 or 32 and groups per lane 1 or 2");
+        return FAIR_ERR_ARG;
+    }
+    FAIR_TRY(ensure_transpose(h));
+    h->A.sirt_lanes[h->prec] = config[0];
+    h->AT.sirt_lanes[h->prec] = config[1];
+    h->A.sirt_groups[h->prec] = config[2];
+    h->AT.sirt_groups[h->prec] = config[3];
+    return FAIR_OK;
+}
+
 int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const double *b,
                       const double *x0, int32_t K, const double *lambda, const fair_opts *options,
                       const double *gx, double *xK, double *gb, double *gx0, double *glam) {
@@ -1169,6 +1207,20 @@ int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches) {
     if (!h || !launches) return FAIR_ERR_NULL;
     // one FP32 shadow conversion per call in reduced precision, two passes per iteration
     *launches = (h->prec != FAIR_PREC_F64 ? 1 : 0) + 2 * (int64_t)K;
+    return FAIR_OK;
+}
+
+int fair_csr_packed_info(fair_csr h, int32_t which, int32_t *has, int64_t *ngroups,
+                         int64_t *nesc, int32_t *stride, int32_t *low_bits) {
+    if (!h || !has || !ngroups || !nesc || !stride || !low_bits) return FAIR_ERR_NULL;
+    if (which != 0 && which != 1) { set_detail("which must be 0 (A) or 1 (A')"); return FAIR_ERR_ARG; }
+    const DevCSR &M = which == 0 ? h->A : h->AT;
+    const bool ok = M.haspk && (which == 0 || h->at_valid);
+    *has = ok ? 1 : 0;
+    *ngroups = ok ? M.ngroups : 0;
+    *nesc = ok ? M.nesc : 0;
+    *stride = ok ? M.pk_S : 0;
+    *low_bits = ok ? M.pk_L : 0;
     return FAIR_OK;
 }
 

@@ -51,6 +51,8 @@ struct DevCSR {
     int64_t nnz = 0;
     int32_t max_row = 0;        // longest row (nonzeros)
     int lanes_per_row = 8;      // G of the row engine (4, 8, 16 or 32)
+    int sirt_lanes[4] = {8, 8, 8, 8};  // G of the SIRT passes per form (autotuned)
+    int sirt_groups[4] = {1, 1, 1, 1}; // packed groups per lane and step (1 or 2)
     // allocate col and v64 for nnz entries plus the pad (pad zeroed)
     int alloc_entries(int64_t nnz_, cudaStream_t s);
     DevBuf rowptr;        // int64 [m+1]
@@ -62,6 +64,19 @@ struct DevCSR {
     bool has32 = false, has16 = false, hasq = false;
     bool qsigned = false;  // vq holds int16 (some value negative) instead of uint16
     double qscale = 1.0;   // value = qscale * vq
+    // Packed index stream of the reduced-precision SIRT passes (csr_make_packed):
+    // rows padded to whole groups of 4 entries, one PkGroup word per group,
+    // padded value copies with 4 values per group.
+    int32_t stride_hint = 0;   // column step across the image (N for a ray matrix)
+    int32_t tstride_hint = 0;  // the same for the transpose (bins per angle)
+    bool pk_tried = false, haspk = false;
+    int pk_S = 0, pk_L = 7;    // step code: delta = lo + hi * S, lo the low L bits
+    int64_t ngroups = 0, nesc = 0;
+    DevBuf prow;               // int64 [m+1] group offsets
+    DevBuf gidx;               // uint2 [ngroups]
+    DevBuf gside;              // int4 [nesc] columns of groups without a step code
+    DevBuf pv32, pv16, pvq;    // padded float / half / 16-bit fixed-point values
+    bool hasp32 = false, hasp16 = false, haspq = false;
     void release();
     bool empty() const { return rowptr.p == nullptr; }
 };
@@ -88,6 +103,13 @@ int csr_build_transpose(const DevCSR &A, DevCSR &AT, cudaStream_t s);
 // After an upload of 1-based JA: convert to 0-based, validate, find max row.
 int csr_check_upload(DevCSR &A, cudaStream_t s);
 int csr_make_lowprec(DevCSR &A, int prec, cudaStream_t s);
+// Packed index stream plus padded values for `prec` (f32/f16/q16); leaves
+// haspk false when too many groups need the escape table. Set
+// FAIR_PACKED=0 to disable.
+int csr_make_packed(DevCSR &A, int prec, cudaStream_t s);
+bool packed_enabled();
+// Reduced-precision copies (and packed streams) of A and A' for SIRT (solvers.cu).
+int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s);
 int csr_scale(DevCSR &A, double c, cudaStream_t s);
 int csr_row_norms(const DevCSR &A, int p, double *d_out, cudaStream_t s);
 int csr_row_dot(const DevCSR &A, int32_t row, const double *d_x, double *d_out, cudaStream_t s);
@@ -120,6 +142,10 @@ int sirt_weights(const DevCSR &A, const DevCSR &AT, bool sart, double *d_M, doub
 int sirt_iterations(const SirtDev &S, int K, cudaStream_t s);
 // Same with CUDA events around each pass; summed pass durations in ms.
 int sirt_iterations_timed(const SirtDev &S, int K, cudaStream_t s, float *ms1, float *ms2);
+// Times each SIRT pass for every lanes-per-row choice and keeps the fastest
+// in A.sirt_lanes[prec] / AT.sirt_lanes[prec] (x and r are overwritten).
+int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_t s,
+                  float *ms_best);
 int sirt_prepare_shadow(const SirtDev &S, cudaStream_t s);
 
 // Gradient descent and power method pieces (solvers.cu).

@@ -368,6 +368,8 @@ int build_geometry(const GeomTables &T, DevCSR &A, cudaStream_t s) {
     A.release();
     A.m = (int32_t)m;
     A.n = ncols;
+    A.stride_hint = T.N;   // pixel (x, y) is column x*N + (N - y)
+    A.tstride_hint = T.p;  // ray (angle i, bin j) is row i*p + j
 
     DevBuf counts, special, nsp, err;
     FAIR_TRY(counts.grow(sizeof(int32_t) * (m > 0 ? m : 1)));

@@ -70,19 +70,33 @@ __device__ __forceinline__ void finish_chunks(unsigned *sched, int64_t nwarps, i
 }
 
 // 16-bit fixed-point values: the integer codes are accumulated as floats and
-// the matrix scale is applied once per row in the epilogue.
+// the matrix scale is applied once per row in the epilogue. A code u becomes
+// a float without the conversion pipe: the bytes of u under the exponent of
+// 2^23 (one byte permute) are the float 2^23 + u, exact, minus 2^23 (one FP32
+// add). Signed codes are first offset by 2^15 (flip of the sign bit).
+// (The difference of the two exact floats is an integer below 2^24: exact.)
+__device__ __forceinline__ float u16_lo(uint32_t w, float bias) {
+    return __int_as_float((int)__byte_perm(w, 0x4B00u, 0x5410u)) - bias;
+}
+__device__ __forceinline__ float u16_hi(uint32_t w, float bias) {
+    return __int_as_float((int)__byte_perm(w, 0x4B00u, 0x5432u)) - bias;
+}
 template <> struct VLoad<uint16_t, float> {
     static __device__ __forceinline__ void ld(const uint16_t *p, float (&o)[4]) {
+        constexpr float b = 8388608.0f;  // 2^23
         uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
-        o[0] = (float)(t.x & 0xffffu); o[1] = (float)(t.x >> 16);
-        o[2] = (float)(t.y & 0xffffu); o[3] = (float)(t.y >> 16);
+        o[0] = u16_lo(t.x, b); o[1] = u16_hi(t.x, b);
+        o[2] = u16_lo(t.y, b); o[3] = u16_hi(t.y, b);
     }
 };
 template <> struct VLoad<int16_t, float> {
     static __device__ __forceinline__ void ld(const int16_t *p, float (&o)[4]) {
+        constexpr float b = 8421376.0f;  // 2^23 + 2^15
         uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
-        o[0] = (float)(int16_t)(t.x & 0xffffu); o[1] = (float)(int16_t)(t.x >> 16);
-        o[2] = (float)(int16_t)(t.y & 0xffffu); o[3] = (float)(int16_t)(t.y >> 16);
+        t.x ^= 0x80008000u;
+        t.y ^= 0x80008000u;
+        o[0] = u16_lo(t.x, b); o[1] = u16_hi(t.x, b);
+        o[2] = u16_lo(t.y, b); o[3] = u16_hi(t.y, b);
     }
 };
 
@@ -143,6 +157,140 @@ __device__ __forceinline__ void chunk_rows(const int64_t *__restrict__ rowptr, i
 #pragma unroll
                 for (int t = 0; t < 4; ++t) vv[t] = vn[t];
                 k = kn;
+            }
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            ACC r = __shfl_sync(0xffffffffu, acc, ((lane - sub) & (R - 1)) * G);
+            if (lane >= sub && lane < sub + R) mine = r;
+        }
+        const int64_t row = base + lane;
+        if (row < m) epi(row, mine);
+    }
+    finish_chunks(sched, nwarps, lane);
+}
+
+// ---- packed index stream ------------------------------------------------------
+// One 8-byte word per group of 4 consecutive entries of a row (rows padded to
+// whole groups): .x = column of the group's first entry; .y bits 0-23 = three
+// 8-bit step codes (column of entry k minus column of entry k-1, k = 1..3) or,
+// with bit 26 set, an index into a side table holding the three columns;
+// bits 24-25 = entries in the group - 1. A step code is a signed low part of
+// L bits and a signed high part of 8-L bits, delta = lo + hi*S, where S is the
+// matrix's column step across the image: N for a ray matrix (a ray moves to a
+// 4- or 8-neighbour pixel, delta in {+-1, +-N, +-N+-1}), the bins per angle
+// for its transpose (the next ray through a pixel is the next bin or a bin
+// of the next angle). With 16-bit values a group costs 16 bytes instead of 24.
+constexpr uint32_t kPkEsc = 1u << 26;
+
+__host__ __device__ inline bool pk_encode(int64_t d, int S, int L, uint32_t &code) {
+    int64_t hi = 0;
+    if (S > 0) hi = d >= 0 ? (d + S / 2) / S : -((-d + S / 2) / S);
+    const int64_t lo = d - hi * S;
+    const int64_t lmin = -(int64_t(1) << (L - 1)), lmax = (int64_t(1) << (L - 1)) - 1;
+    const int64_t hmin = -(int64_t(1) << (7 - L)), hmax = (int64_t(1) << (7 - L)) - 1;
+    if (lo < lmin || lo > lmax || hi < hmin || hi > hmax) return false;
+    code = (uint32_t)(((hi << L) | (lo & ((int64_t(1) << L) - 1))) & 0xFF);
+    return true;
+}
+
+__device__ __forceinline__ int pk_step(uint32_t b, int S, int L) {
+    const int lo = (int)(b << (32 - L)) >> (32 - L);
+    const int hi = (int)(b << 24) >> (24 + L);
+    return lo + hi * S;
+}
+
+// Columns of one packed group (entries beyond the group's count repeat the
+// previous column).
+__device__ __forceinline__ void pk_decode(uint2 w, const int4 *__restrict__ gside, int S, int L,
+                                          int (&c)[4]) {
+    c[0] = (int)w.x;
+    if (w.y & kPkEsc) {
+        const int4 t = __ldg(gside + (w.y & 0xFFFFFFu));
+        c[1] = t.x; c[2] = t.y; c[3] = t.z;
+    } else {
+        c[1] = c[0] + pk_step(w.y & 0xFFu, S, L);
+        c[2] = c[1] + pk_step((w.y >> 8) & 0xFFu, S, L);
+        c[3] = c[2] + pk_step((w.y >> 16) & 0xFFu, S, L);
+    }
+}
+
+// chunk_rows over the packed index stream: every lane takes NG groups (4*NG
+// entries) per step, each one 8-byte index word and one vector load of
+// values, and issues the 4*NG gathers of a step together.
+template <typename VT, typename ACC, int G, int NG, class Epi>
+__device__ __forceinline__ void chunk_rows_pk(const int64_t *__restrict__ prow, int32_t m,
+                                              const uint2 *__restrict__ gidx,
+                                              const int4 *__restrict__ gside, int S, int L,
+                                              const VT *__restrict__ val,
+                                              const float *__restrict__ x, Epi &epi,
+                                              unsigned *sched) {
+    constexpr int R = 32 / G;
+    const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nchunks = ((int64_t)m + 31) >> 5;
+    for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
+         ch = next_chunk(sched, ch, nwarps, lane)) {
+        const int64_t base = ch << 5;
+        ACC mine = 0;
+#pragma unroll 1
+        for (int sub = 0; sub < 32; sub += R) {
+            const int64_t row = base + sub + g;
+            int64_t g0 = 0;
+            int ng = 0;  // groups in the row
+            if (row < m) {
+                g0 = __ldg(prow + row);
+                ng = (int)(__ldg(prow + row + 1) - g0);
+            }
+            const uint2 *wp = gidx + g0;
+            const VT *vp = val + 4 * g0;
+            ACC acc = 0;
+            uint2 w[NG];
+            ACC vv[NG][4];
+#pragma unroll
+            for (int q = 0; q < NG; ++q) {
+                const int j = gl + q * G;
+                w[q] = make_uint2(0u, 0u);
+                vv[q][0] = vv[q][1] = vv[q][2] = vv[q][3] = 0;
+                if (j < ng) {
+                    w[q] = __ldcs(wp + j);
+                    VLoad<VT, ACC>::ld(vp + 4 * j, vv[q]);
+                }
+            }
+            for (int j = gl; j < ng; j += NG * G) {
+                const int jn = j + NG * G;
+                uint2 wn[NG];
+                ACC vn[NG][4];
+#pragma unroll
+                for (int q = 0; q < NG; ++q) {
+                    wn[q] = make_uint2(0u, 0u);
+                    vn[q][0] = vn[q][1] = vn[q][2] = vn[q][3] = 0;
+                    if (jn + q * G < ng) {
+                        wn[q] = __ldcs(wp + jn + q * G);
+                        VLoad<VT, ACC>::ld(vp + 4 * (jn + q * G), vn[q]);
+                    }
+                }
+                int c[NG][4];
+                ACC xv[NG][4];
+#pragma unroll
+                for (int q = 0; q < NG; ++q) {
+                    pk_decode(w[q], gside, S, L, c[q]);
+                    // entries past the group's count (and groups past the row)
+                    // read nothing and add zero
+                    const int cnt = j + q * G < ng ? (int)((w[q].y >> 24) & 3u) : -1;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) xv[q][t] = t <= cnt ? (ACC)__ldg(x + c[q][t]) : (ACC)0;
+                }
+#pragma unroll
+                for (int q = 0; q < NG; ++q)
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) acc += xv[q][t] * vv[q][t];
+#pragma unroll
+                for (int q = 0; q < NG; ++q) {
+                    w[q] = wn[q];
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) vv[q][t] = vn[q][t];
+                }
             }
 #pragma unroll
             for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);

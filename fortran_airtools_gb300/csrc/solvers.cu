@@ -133,6 +133,25 @@ __global__ void __launch_bounds__(256) k_sirt_resid_lp(const int64_t *rowptr, in
                                                        unsigned *sched) {
     chunk_rows<VT, float, float, G>(rowptr, m, col, v, x, epi, sched);
 }
+// Packed index stream (rows.cuh) with padded values.
+struct PkArgs {
+    const int64_t *prow;
+    const uint2 *gidx;
+    const int4 *gside;
+    int S, L;
+};
+template <typename VT, int G, int NG>
+__global__ void __launch_bounds__(256) k_sirt_resid_pk(PkArgs P, int32_t m, const VT *v,
+                                                       const float *x, EpiResidLP epi,
+                                                       unsigned *sched) {
+    chunk_rows_pk<VT, float, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, x, epi, sched);
+}
+template <typename VT, int G, int NG>
+__global__ void __launch_bounds__(256) k_sirt_update_pk(PkArgs P, int32_t m, const VT *v,
+                                                        const float *r, EpiUpdateLP epi,
+                                                        unsigned *sched) {
+    chunk_rows_pk<VT, float, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, r, epi, sched);
+}
 template <int G>
 __global__ void __launch_bounds__(256) k_sirt_update_f64(const int64_t *rowptr, int32_t m,
                                                          const int32_t *col, const double *v,
@@ -339,23 +358,43 @@ int sirt_prepare_shadow(const SirtDev &S, cudaStream_t s) {
     return FAIR_OK;
 }
 
+// One reduced-precision pass; `pvals` (padded values) selects the packed
+// index stream when the matrix has one.
 template <typename VT>
-static void resid_lp(const SirtDev &S, const DevCSR &M, const VT *vals, double scale,
-                     cudaStream_t s) {
-    EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
-    FAIR_G_DISPATCH(M.lanes_per_row,
-                    (k_sirt_resid_lp<VT, g_><<<chunk_grid(k_sirt_resid_lp<VT, g_>, M.m), 256, 0, s>>>(
-                        M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals, S.x32, e, S.sched)));
-}
-
-template <typename VT>
-static void update_lp(const SirtDev &S, const DevCSR &M, const VT *vals, double scale,
-                      cudaStream_t s) {
-    EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale};
-    FAIR_G_DISPATCH(M.lanes_per_row,
-                    (k_sirt_update_lp<VT, g_><<<chunk_grid(k_sirt_update_lp<VT, g_>, M.m), 256, 0, s>>>(
-                        M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals,
-                        (const float *)S.r, e, S.sched)));
+static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
+                    const VT *pvals, double scale, cudaStream_t s) {
+    const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
+    const int G = M.sirt_lanes[S.prec], NG = M.sirt_groups[S.prec];
+    if (pass == 1) {
+        EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
+        if (pvals && NG == 2)
+            FAIR_G_DISPATCH(G,
+                            (k_sirt_resid_pk<VT, g_, 2><<<chunk_grid(k_sirt_resid_pk<VT, g_, 2>, M.m), 256, 0, s>>>(
+                                P, M.m, pvals, S.x32, e, S.sched)))
+        else if (pvals)
+            FAIR_G_DISPATCH(G,
+                            (k_sirt_resid_pk<VT, g_, 1><<<chunk_grid(k_sirt_resid_pk<VT, g_, 1>, M.m), 256, 0, s>>>(
+                                P, M.m, pvals, S.x32, e, S.sched)))
+        else
+            FAIR_G_DISPATCH(G,
+                            (k_sirt_resid_lp<VT, g_><<<chunk_grid(k_sirt_resid_lp<VT, g_>, M.m), 256, 0, s>>>(
+                                M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals, S.x32, e, S.sched)))
+    } else {
+        EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale};
+        if (pvals && NG == 2)
+            FAIR_G_DISPATCH(G,
+                            (k_sirt_update_pk<VT, g_, 2><<<chunk_grid(k_sirt_update_pk<VT, g_, 2>, M.m), 256, 0, s>>>(
+                                P, M.m, pvals, (const float *)S.r, e, S.sched)))
+        else if (pvals)
+            FAIR_G_DISPATCH(G,
+                            (k_sirt_update_pk<VT, g_, 1><<<chunk_grid(k_sirt_update_pk<VT, g_, 1>, M.m), 256, 0, s>>>(
+                                P, M.m, pvals, (const float *)S.r, e, S.sched)))
+        else
+            FAIR_G_DISPATCH(G,
+                            (k_sirt_update_lp<VT, g_><<<chunk_grid(k_sirt_update_lp<VT, g_>, M.m), 256, 0, s>>>(
+                                M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals,
+                                (const float *)S.r, e, S.sched)))
+    }
 }
 
 // One pass of a SIRT iteration: pass 1 = residual over A, pass 2 = update over A'.
@@ -363,39 +402,50 @@ static void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
     const DevCSR &M = pass == 1 ? *S.A : *S.AT;
     if (M.m == 0) return;
     if (S.prec == FAIR_PREC_F64) {
+        const int G = M.sirt_lanes[FAIR_PREC_F64];
         const int64_t *rp = M.rowptr.as<int64_t>();
         const int32_t *cl = M.col.as<int32_t>();
         if (pass == 1) {
             EpiResidF64 e{S.b, S.Minv, (double *)S.r};
-            FAIR_G_DISPATCH(M.lanes_per_row, (k_sirt_resid_f64<g_><<<chunk_grid(k_sirt_resid_f64<g_>, M.m), 256, 0, s>>>(
+            FAIR_G_DISPATCH(G, (k_sirt_resid_f64<g_><<<chunk_grid(k_sirt_resid_f64<g_>, M.m), 256, 0, s>>>(
                                                   rp, M.m, cl, M.v64.as<double>(), S.x, e, S.sched)));
         } else {
             EpiUpdateF64 e{S.D, S.x, S.omg, S.lb, S.ub, S.bmode};
-            FAIR_G_DISPATCH(M.lanes_per_row, (k_sirt_update_f64<g_><<<chunk_grid(k_sirt_update_f64<g_>, M.m), 256, 0, s>>>(
+            FAIR_G_DISPATCH(G, (k_sirt_update_f64<g_><<<chunk_grid(k_sirt_update_f64<g_>, M.m), 256, 0, s>>>(
                                                   rp, M.m, cl, M.v64.as<double>(), (const double *)S.r, e, S.sched)));
         }
         return;
     }
+    const bool pk = M.haspk && packed_enabled();
     if (S.prec == FAIR_PREC_F32) {
-        if (pass == 1) resid_lp(S, M, M.v32.as<float>(), 1.0, s);
-        else update_lp(S, M, M.v32.as<float>(), 1.0, s);
+        lp_pass(S, M, pass, M.v32.as<float>(), pk && M.hasp32 ? M.pv32.as<float>() : nullptr, 1.0, s);
     } else if (S.prec == FAIR_PREC_F16) {
-        if (pass == 1) resid_lp(S, M, M.v16.as<__half>(), 1.0, s);
-        else update_lp(S, M, M.v16.as<__half>(), 1.0, s);
+        lp_pass(S, M, pass, M.v16.as<__half>(), pk && M.hasp16 ? M.pv16.as<__half>() : nullptr,
+                1.0, s);
     } else if (M.qsigned) {
-        if (pass == 1) resid_lp(S, M, M.vq.as<int16_t>(), M.qscale, s);
-        else update_lp(S, M, M.vq.as<int16_t>(), M.qscale, s);
+        lp_pass(S, M, pass, M.vq.as<int16_t>(), pk && M.haspq ? M.pvq.as<int16_t>() : nullptr,
+                M.qscale, s);
     } else {
-        if (pass == 1) resid_lp(S, M, M.vq.as<uint16_t>(), M.qscale, s);
-        else update_lp(S, M, M.vq.as<uint16_t>(), M.qscale, s);
+        lp_pass(S, M, pass, M.vq.as<uint16_t>(), pk && M.haspq ? M.pvq.as<uint16_t>() : nullptr,
+                M.qscale, s);
     }
 }
 
-int sirt_iterations(const SirtDev &S, int K, cudaStream_t s) {
-    if (S.prec != FAIR_PREC_F64) {
-        FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(*S.A), S.prec, s));
-        FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(*S.AT), S.prec, s));
+// The derived value copies (and packed index streams) a reduced-precision
+// SIRT needs on A and A'.
+int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s) {
+    if (prec == FAIR_PREC_F64) return FAIR_OK;
+    FAIR_TRY(csr_make_lowprec(A, prec, s));
+    FAIR_TRY(csr_make_lowprec(AT, prec, s));
+    if (packed_enabled()) {
+        FAIR_TRY(csr_make_packed(A, prec, s));
+        FAIR_TRY(csr_make_packed(AT, prec, s));
     }
+    return FAIR_OK;
+}
+
+int sirt_iterations(const SirtDev &S, int K, cudaStream_t s) {
+    FAIR_TRY(sirt_make_forms(const_cast<DevCSR &>(*S.A), const_cast<DevCSR &>(*S.AT), S.prec, s));
     for (int it = 0; it < K; ++it) {
         sirt_pass(S, 1, s);
         sirt_pass(S, 2, s);
@@ -404,11 +454,54 @@ int sirt_iterations(const SirtDev &S, int K, cudaStream_t s) {
     return FAIR_OK;
 }
 
-int sirt_iterations_timed(const SirtDev &S, int K, cudaStream_t s, float *ms1, float *ms2) {
-    if (S.prec != FAIR_PREC_F64) {
-        FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(*S.A), S.prec, s));
-        FAIR_TRY(csr_make_lowprec(const_cast<DevCSR &>(*S.AT), S.prec, s));
+int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_t s,
+                  float *ms_best) {
+    FAIR_TRY(sirt_make_forms(A, AT, S.prec, s));
+    FAIR_TRY(sirt_prepare_shadow(S, s));
+    static const int lanes[4] = {4, 8, 16, 32};
+    cudaEvent_t ev[2];
+    for (auto &e : ev) FAIR_CUDA(cudaEventCreate(&e));
+    int st = FAIR_OK;
+    for (int pass = 1; pass <= 2 && st == FAIR_OK; ++pass) {
+        DevCSR &M = pass == 1 ? A : AT;
+        // groups per lane and step: 1 or 2 on the packed stream, else 1
+        const bool pk = S.prec != FAIR_PREC_F64 && M.haspk && packed_enabled();
+        int best_g = M.sirt_lanes[S.prec], best_ng = M.sirt_groups[S.prec];
+        float best_ms = -1.f;
+        // two rounds over the candidates; each keeps its faster round
+        float t[2][4];
+        for (int round = 0; round < 2 && st == FAIR_OK; ++round)
+            for (int ng = 1; ng <= (pk ? 2 : 1) && st == FAIR_OK; ++ng)
+                for (int c = 0; c < 4 && st == FAIR_OK; ++c) {
+                    M.sirt_lanes[S.prec] = lanes[c];
+                    M.sirt_groups[S.prec] = ng;
+                    sirt_pass(S, pass, s);  // warm-up
+                    cudaEventRecord(ev[0], s);
+                    for (int r = 0; r < reps; ++r) sirt_pass(S, pass, s);
+                    cudaEventRecord(ev[1], s);
+                    cudaError_t e = cudaEventSynchronize(ev[1]);
+                    if (e != cudaSuccess) { st = cuda_fail(e, "autotune", __FILE__, __LINE__); break; }
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+                    ms /= reps;
+                    float &tc = t[ng - 1][c];
+                    tc = round == 0 ? ms : std::min(tc, ms);
+                    if (round == 1 && (best_ms < 0.f || tc < best_ms)) {
+                        best_ms = tc;
+                        best_g = lanes[c];
+                        best_ng = ng;
+                    }
+                }
+        M.sirt_lanes[S.prec] = best_g;
+        M.sirt_groups[S.prec] = best_ng;
+        if (ms_best) ms_best[pass - 1] = best_ms;
     }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return st;
+}
+
+int sirt_iterations_timed(const SirtDev &S, int K, cudaStream_t s, float *ms1, float *ms2) {
+    FAIR_TRY(sirt_make_forms(const_cast<DevCSR &>(*S.A), const_cast<DevCSR &>(*S.AT), S.prec, s));
     cudaEvent_t ev[3];
     for (auto &e : ev) FAIR_CUDA(cudaEventCreate(&e));
     float t1 = 0.f, t2 = 0.f;

@@ -455,6 +455,8 @@ int csr_build_transpose(const DevCSR &A, DevCSR &AT, cudaStream_t s) {
     AT.m = A.n;
     AT.n = A.m;
     AT.nnz = A.nnz;
+    AT.stride_hint = A.tstride_hint;
+    AT.tstride_hint = A.stride_hint;
     const int64_t nnz = A.nnz;
     DevBuf cnt, fill, tsrc;
     FAIR_TRY(cnt.grow(sizeof(int32_t) * ((size_t)A.n + 1)));
@@ -584,6 +586,7 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
     A.has32 = false;
     A.has16 = false;
     A.hasq = false;
+    A.hasp32 = A.hasp16 = A.haspq = false;
     return FAIR_OK;
 }
 

@@ -57,8 +57,18 @@ class CSRMatrix:
         return self.info()[2]
 
     def set_precision(self, prec: str):
-        """Value storage used by products and SIRT: 'f64', 'f32' or 'f16'."""
+        """Value storage used by products and SIRT: 'f64', 'f32', 'f16' or 'q16'."""
         check(lib().fair_csr_set_precision(self._h, PREC[prec]))
+
+    def packed_info(self, transposed: bool = False) -> dict:
+        """Packed index stream of A (or A'), built by the first reduced-precision
+        SIRT: {'has', 'ngroups', 'nesc', 'stride', 'low_bits'}."""
+        has, S, L = C.c_int32(), C.c_int32(), C.c_int32()
+        ng, ne = C.c_int64(), C.c_int64()
+        check(lib().fair_csr_packed_info(self._h, 1 if transposed else 0, C.byref(has),
+                                         C.byref(ng), C.byref(ne), C.byref(S), C.byref(L)))
+        return {"has": bool(has.value), "ngroups": ng.value, "nesc": ne.value,
+                "stride": S.value, "low_bits": L.value}
 
     def set_stream(self, cuda_stream_ptr: int | None):
         check(lib().fair_csr_set_stream(self._h, cuda_stream_ptr))

@@ -50,6 +50,29 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
                       const double *x0, int32_t K, const double *lambda, const fair_opts *options,
                       const double *gx, double *xK, double *gb, double *gx0, double *glam);
 
+/* Autotuner of the SIRT passes (no reference counterpart): after
+ * fair_sirt_prepare, times each pass over A and A' with 4, 8, 16 and 32 lanes
+ * per row and, on a packed index stream, 1 or 2 groups of 4 entries per lane
+ * and step (reps launches each, CUDA events on the handle's stream), and
+ * keeps the fastest for the handle's current precision. config (may be NULL)
+ * receives {lanes A, lanes A', groups A, groups A'}. d_b as in
+ * fair_sirt_run_device; d_x is scratch (overwritten). */
+int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
+                       int32_t *config);
+
+/* Sets {lanes A, lanes A', groups A, groups A'} of the SIRT passes for the
+ * handle's current precision: lanes per row 4, 8, 16 or 32; groups per lane
+ * 1 or 2 (used on the packed index stream). No reference counterpart. */
+int fair_sirt_set_lanes(fair_csr h, const int32_t *config);
+
+/* Packed index stream of A (which = 0) or A' (which = 1), built by the first
+ * reduced-precision SIRT on the handle (no reference counterpart): has = 1
+ * when built, the groups of 4 entries, the groups stored in the escape
+ * table, and the step code's stride S and low-part width L. The packed
+ * stream is used unless the environment sets FAIR_PACKED=0. */
+int fair_csr_packed_info(fair_csr h, int32_t which, int32_t *has, int64_t *ngroups,
+                         int64_t *nesc, int32_t *stride, int32_t *low_bits);
+
 /* Capacity, in doubles, of the fixed device array behind
  * fair_matvecmul_noalloc (32 MiB): n + m of the matrix must fit in it. */
 #define FAIR_NOALLOC_MAX_ENTRIES 4194304

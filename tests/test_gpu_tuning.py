@@ -1,0 +1,61 @@
+"""Lanes-per-row tuning of the SIRT passes (fair_sirt_set_lanes,
+fair_sirt_autotune): every choice gives the oracle's iterate within the
+precision's bar, and the autotuner returns one of the supported choices."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def prob(fair, oracle):
+    n, nth, p = 40, 50, 58
+    th = np.pi * np.arange(nth) / nth
+    A = fair.paralleltomo(fair.Data(n=n, p=p, nth=nth, theta=th))
+    R = oracle.paralleltomo(n, nth, p, th)
+    b = oracle.matvecmul(R, fair.phantomgallery.shepplogan(n))
+    return A, R, b
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-10), ("f32", 1e-5), ("q16", 1e-4)])
+@pytest.mark.parametrize("cfg", [(4, 32, 1, 2), (16, 4, 2, 1), (32, 16, 2, 2), (8, 8, 1, 1)])
+def test_lanes_choice(prob, fair, oracle, prec, tol, cfg):
+    from fortran_airtools_gb300._clib import check, lib
+    A, R, b = prob
+    A.set_precision(prec)
+    try:
+        check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(*cfg)))
+        x = fair.airms.sirt("sart", A, b, 20, opts=fair.airms.options(lbound=0.0))
+    finally:
+        check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, 1, 1)))
+        A.set_precision("f64")
+    xr = oracle.sirt("sart", R, b, 20, opts=oracle.options(lbound=0.0))
+    assert rel_err(x, xr) < tol
+
+
+def test_autotune(prob, fair, oracle):
+    import torch
+    from fortran_airtools_gb300._clib import check, lib
+    A, R, b = prob
+    L = lib()
+    L.fair_sirt_prepare.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
+    opts = fair.airms.options()
+    A.set_precision("f32")
+    try:
+        check(L.fair_sirt_prepare(A.handle, b"cimmino", C.byref(opts)))
+        d_b = torch.from_numpy(b).cuda()
+        d_x = torch.zeros(R.n, dtype=torch.float64, device="cuda")
+        cfg = (C.c_int32 * 4)()
+        check(L.fair_sirt_autotune(A.handle, d_b.data_ptr(), d_x.data_ptr(), 2, cfg))
+        assert cfg[0] in (4, 8, 16, 32) and cfg[1] in (4, 8, 16, 32)
+        assert cfg[2] in (1, 2) and cfg[3] in (1, 2)
+        x = fair.airms.sirt("cimmino", A, b, 15)
+    finally:
+        A.set_precision("f64")
+    assert rel_err(x, oracle.sirt("cimmino", R, b, 15)) < 1e-5
+    with pytest.raises(fair.FairError):
+        check(L.fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(6, 8, 1, 1)))
