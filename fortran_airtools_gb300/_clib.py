@@ -125,6 +125,20 @@ def _declare(L):
                               C.c_int),
         "fair_csr_packed_info": ([h, i32, P(i32), P(i64), P(i64), P(i32), P(i32)], C.c_int),
         "fair_sirt_autotune": ([h, vp, vp, i32, vp], C.c_int),
+        "fair_batch_create": ([P(h), i32], C.c_int),
+        "fair_batch_destroy": ([h], C.c_int),
+        "fair_batch_set_stream": ([h, vp], C.c_int),
+        "fair_batch_add": ([h, h, i32], C.c_int),
+        "fair_batch_info": ([h, P(i32), P(i64), P(i64), P(i64), P(i64)], C.c_int),
+        "fair_batch_offsets": ([h, vp, vp], C.c_int),
+        "fair_batch_pass_bytes": ([h, i32, P(i64), P(i64)], C.c_int),
+        "fair_batch_sirt": ([h, C.c_char_p, vp, i32, vp, P(Opts), vp], C.c_int),
+        "fair_batch_prepare": ([h, C.c_char_p, P(Opts)], C.c_int),
+        "fair_batch_run_device": ([h, vp, vp, i32], C.c_int),
+        "fair_batch_run_device_unbatched": ([h, vp, vp, i32], C.c_int),
+        "fair_batch_launches": ([h, i32, P(i64)], C.c_int),
+        "fair_batch_autotune": ([h, vp, vp, i32, vp], C.c_int),
+        "fair_batch_set_config": ([h, vp], C.c_int),
         "fair_sirt_set_lanes": ([h, vp], C.c_int),
     }
     for name, (args, res) in sig.items():

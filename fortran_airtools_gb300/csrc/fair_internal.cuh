@@ -140,6 +140,9 @@ struct SirtDev {
 int sirt_weights(const DevCSR &A, const DevCSR &AT, bool sart, double *d_M, double *d_D,
                  cudaStream_t s);
 int sirt_iterations(const SirtDev &S, int K, cudaStream_t s);
+// One SIRT pass (1: residual over A, 2: update over A') with the forms
+// already made; enqueues one kernel.
+void sirt_pass(const SirtDev &S, int pass, cudaStream_t s);
 // Same with CUDA events around each pass; summed pass durations in ms.
 int sirt_iterations_timed(const SirtDev &S, int K, cudaStream_t s, float *ms1, float *ms2);
 // Times each SIRT pass for every lanes-per-row choice and keeps the fastest

@@ -100,69 +100,81 @@ template <> struct VLoad<int16_t, float> {
     }
 };
 
+// Row sums of one chunk (rows base..base+31): returns, in lane l, the sum of
+// row base+l. All lanes of the warp call it together.
+// VT: stored value type; XT: gathered vector type; ACC: accumulator type.
+template <typename VT, typename XT, typename ACC, int G>
+__device__ __forceinline__ ACC csr_chunk_sums(const int64_t *__restrict__ rowptr, int32_t m,
+                                              const int32_t *__restrict__ col,
+                                              const VT *__restrict__ val,
+                                              const XT *__restrict__ x, int64_t base) {
+    constexpr int R = 32 / G;
+    const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
+    ACC mine = 0;
+#pragma unroll 1
+    for (int sub = 0; sub < 32; sub += R) {
+        const int64_t row = base + sub + g;
+        int64_t s = 0, e = 0;
+        if (row < m) {
+            s = __ldg(rowptr + row);
+            e = __ldg(rowptr + row + 1);
+        }
+        ACC acc = 0;
+        int64_t k = (s & ~(int64_t)3) + 4 * gl;
+        int4 cc = make_int4(0, 0, 0, 0);
+        ACC vv[4] = {0, 0, 0, 0};
+        if (k < e) {
+            cc = __ldcs(reinterpret_cast<const int4 *>(col + k));
+            VLoad<VT, ACC>::ld(val + k, vv);
+        }
+        while (k < e) {
+            const int64_t kn = k + 4 * G;
+            int4 cn = make_int4(0, 0, 0, 0);
+            ACC vn[4] = {0, 0, 0, 0};
+            if (kn < e) {
+                cn = __ldcs(reinterpret_cast<const int4 *>(col + kn));
+                VLoad<VT, ACC>::ld(val + kn, vn);
+            }
+            if (k >= s && k + 3 < e) {
+                acc += (ACC)__ldg(x + cc.x) * vv[0];
+                acc += (ACC)__ldg(x + cc.y) * vv[1];
+                acc += (ACC)__ldg(x + cc.z) * vv[2];
+                acc += (ACC)__ldg(x + cc.w) * vv[3];
+            } else {
+                if (k >= s && k < e) acc += (ACC)__ldg(x + cc.x) * vv[0];
+                if (k + 1 >= s && k + 1 < e) acc += (ACC)__ldg(x + cc.y) * vv[1];
+                if (k + 2 >= s && k + 2 < e) acc += (ACC)__ldg(x + cc.z) * vv[2];
+                if (k + 3 >= s && k + 3 < e) acc += (ACC)__ldg(x + cc.w) * vv[3];
+            }
+            cc = cn;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) vv[t] = vn[t];
+            k = kn;
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        ACC r = __shfl_sync(0xffffffffu, acc, ((lane - sub) & (R - 1)) * G);
+        if (lane >= sub && lane < sub + R) mine = r;
+    }
+    return mine;
+}
+
 // Sum over the rows of every chunk owned by this warp; calls epi(row, sum)
 // from the lane that owns `row` (all lanes of the warp call epi together).
-// VT: stored value type; XT: gathered vector type; ACC: accumulator type.
 template <typename VT, typename XT, typename ACC, int G, class Epi>
 __device__ __forceinline__ void chunk_rows(const int64_t *__restrict__ rowptr, int32_t m,
                                            const int32_t *__restrict__ col,
                                            const VT *__restrict__ val,
                                            const XT *__restrict__ x, Epi &epi,
                                            unsigned *sched = nullptr) {
-    constexpr int R = 32 / G;
-    const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
+    const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t nchunks = ((int64_t)m + 31) >> 5;
     for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
          ch = next_chunk(sched, ch, nwarps, lane)) {
         const int64_t base = ch << 5;
-        ACC mine = 0;
-#pragma unroll 1
-        for (int sub = 0; sub < 32; sub += R) {
-            const int64_t row = base + sub + g;
-            int64_t s = 0, e = 0;
-            if (row < m) {
-                s = __ldg(rowptr + row);
-                e = __ldg(rowptr + row + 1);
-            }
-            ACC acc = 0;
-            int64_t k = (s & ~(int64_t)3) + 4 * gl;
-            int4 cc = make_int4(0, 0, 0, 0);
-            ACC vv[4] = {0, 0, 0, 0};
-            if (k < e) {
-                cc = __ldcs(reinterpret_cast<const int4 *>(col + k));
-                VLoad<VT, ACC>::ld(val + k, vv);
-            }
-            while (k < e) {
-                const int64_t kn = k + 4 * G;
-                int4 cn = make_int4(0, 0, 0, 0);
-                ACC vn[4] = {0, 0, 0, 0};
-                if (kn < e) {
-                    cn = __ldcs(reinterpret_cast<const int4 *>(col + kn));
-                    VLoad<VT, ACC>::ld(val + kn, vn);
-                }
-                if (k >= s && k + 3 < e) {
-                    acc += (ACC)__ldg(x + cc.x) * vv[0];
-                    acc += (ACC)__ldg(x + cc.y) * vv[1];
-                    acc += (ACC)__ldg(x + cc.z) * vv[2];
-                    acc += (ACC)__ldg(x + cc.w) * vv[3];
-                } else {
-                    if (k >= s && k < e) acc += (ACC)__ldg(x + cc.x) * vv[0];
-                    if (k + 1 >= s && k + 1 < e) acc += (ACC)__ldg(x + cc.y) * vv[1];
-                    if (k + 2 >= s && k + 2 < e) acc += (ACC)__ldg(x + cc.z) * vv[2];
-                    if (k + 3 >= s && k + 3 < e) acc += (ACC)__ldg(x + cc.w) * vv[3];
-                }
-                cc = cn;
-#pragma unroll
-                for (int t = 0; t < 4; ++t) vv[t] = vn[t];
-                k = kn;
-            }
-#pragma unroll
-            for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            ACC r = __shfl_sync(0xffffffffu, acc, ((lane - sub) & (R - 1)) * G);
-            if (lane >= sub && lane < sub + R) mine = r;
-        }
+        const ACC mine = csr_chunk_sums<VT, XT, ACC, G>(rowptr, m, col, val, x, base);
         const int64_t row = base + lane;
         if (row < m) epi(row, mine);
     }
@@ -214,9 +226,86 @@ __device__ __forceinline__ void pk_decode(uint2 w, const int4 *__restrict__ gsid
     }
 }
 
-// chunk_rows over the packed index stream: every lane takes NG groups (4*NG
-// entries) per step, each one 8-byte index word and one vector load of
-// values, and issues the 4*NG gathers of a step together.
+// Row sums of one chunk over the packed index stream: every lane takes NG
+// groups (4*NG entries) per step, each one 8-byte index word and one vector
+// load of values, and issues the 4*NG gathers of a step together.
+template <typename VT, typename ACC, int G, int NG>
+__device__ __forceinline__ ACC pk_chunk_sums(const int64_t *__restrict__ prow, int32_t m,
+                                             const uint2 *__restrict__ gidx,
+                                             const int4 *__restrict__ gside, int S, int L,
+                                             const VT *__restrict__ val,
+                                             const float *__restrict__ x, int64_t base) {
+    constexpr int R = 32 / G;
+    const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
+    ACC mine = 0;
+#pragma unroll 1
+    for (int sub = 0; sub < 32; sub += R) {
+        const int64_t row = base + sub + g;
+        int64_t g0 = 0;
+        int ng = 0;  // groups in the row
+        if (row < m) {
+            g0 = __ldg(prow + row);
+            ng = (int)(__ldg(prow + row + 1) - g0);
+        }
+        const uint2 *wp = gidx + g0;
+        const VT *vp = val + 4 * g0;
+        ACC acc = 0;
+        uint2 w[NG];
+        ACC vv[NG][4];
+#pragma unroll
+        for (int q = 0; q < NG; ++q) {
+            const int j = gl + q * G;
+            w[q] = make_uint2(0u, 0u);
+            vv[q][0] = vv[q][1] = vv[q][2] = vv[q][3] = 0;
+            if (j < ng) {
+                w[q] = __ldcs(wp + j);
+                VLoad<VT, ACC>::ld(vp + 4 * j, vv[q]);
+            }
+        }
+        for (int j = gl; j < ng; j += NG * G) {
+            const int jn = j + NG * G;
+            uint2 wn[NG];
+            ACC vn[NG][4];
+#pragma unroll
+            for (int q = 0; q < NG; ++q) {
+                wn[q] = make_uint2(0u, 0u);
+                vn[q][0] = vn[q][1] = vn[q][2] = vn[q][3] = 0;
+                if (jn + q * G < ng) {
+                    wn[q] = __ldcs(wp + jn + q * G);
+                    VLoad<VT, ACC>::ld(vp + 4 * (jn + q * G), vn[q]);
+                }
+            }
+            int c[NG][4];
+            ACC xv[NG][4];
+#pragma unroll
+            for (int q = 0; q < NG; ++q) {
+                pk_decode(w[q], gside, S, L, c[q]);
+                // entries past the group's count (and groups past the row)
+                // read nothing and add zero
+                const int cnt = j + q * G < ng ? (int)((w[q].y >> 24) & 3u) : -1;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) xv[q][t] = t <= cnt ? (ACC)__ldg(x + c[q][t]) : (ACC)0;
+            }
+#pragma unroll
+            for (int q = 0; q < NG; ++q)
+#pragma unroll
+                for (int t = 0; t < 4; ++t) acc += xv[q][t] * vv[q][t];
+#pragma unroll
+            for (int q = 0; q < NG; ++q) {
+                w[q] = wn[q];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) vv[q][t] = vn[q][t];
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        ACC r = __shfl_sync(0xffffffffu, acc, ((lane - sub) & (R - 1)) * G);
+        if (lane >= sub && lane < sub + R) mine = r;
+    }
+    return mine;
+}
+
+// chunk_rows over the packed index stream.
 template <typename VT, typename ACC, int G, int NG, class Epi>
 __device__ __forceinline__ void chunk_rows_pk(const int64_t *__restrict__ prow, int32_t m,
                                               const uint2 *__restrict__ gidx,
@@ -224,79 +313,14 @@ __device__ __forceinline__ void chunk_rows_pk(const int64_t *__restrict__ prow, 
                                               const VT *__restrict__ val,
                                               const float *__restrict__ x, Epi &epi,
                                               unsigned *sched) {
-    constexpr int R = 32 / G;
-    const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
+    const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t nchunks = ((int64_t)m + 31) >> 5;
     for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
          ch = next_chunk(sched, ch, nwarps, lane)) {
         const int64_t base = ch << 5;
-        ACC mine = 0;
-#pragma unroll 1
-        for (int sub = 0; sub < 32; sub += R) {
-            const int64_t row = base + sub + g;
-            int64_t g0 = 0;
-            int ng = 0;  // groups in the row
-            if (row < m) {
-                g0 = __ldg(prow + row);
-                ng = (int)(__ldg(prow + row + 1) - g0);
-            }
-            const uint2 *wp = gidx + g0;
-            const VT *vp = val + 4 * g0;
-            ACC acc = 0;
-            uint2 w[NG];
-            ACC vv[NG][4];
-#pragma unroll
-            for (int q = 0; q < NG; ++q) {
-                const int j = gl + q * G;
-                w[q] = make_uint2(0u, 0u);
-                vv[q][0] = vv[q][1] = vv[q][2] = vv[q][3] = 0;
-                if (j < ng) {
-                    w[q] = __ldcs(wp + j);
-                    VLoad<VT, ACC>::ld(vp + 4 * j, vv[q]);
-                }
-            }
-            for (int j = gl; j < ng; j += NG * G) {
-                const int jn = j + NG * G;
-                uint2 wn[NG];
-                ACC vn[NG][4];
-#pragma unroll
-                for (int q = 0; q < NG; ++q) {
-                    wn[q] = make_uint2(0u, 0u);
-                    vn[q][0] = vn[q][1] = vn[q][2] = vn[q][3] = 0;
-                    if (jn + q * G < ng) {
-                        wn[q] = __ldcs(wp + jn + q * G);
-                        VLoad<VT, ACC>::ld(vp + 4 * (jn + q * G), vn[q]);
-                    }
-                }
-                int c[NG][4];
-                ACC xv[NG][4];
-#pragma unroll
-                for (int q = 0; q < NG; ++q) {
-                    pk_decode(w[q], gside, S, L, c[q]);
-                    // entries past the group's count (and groups past the row)
-                    // read nothing and add zero
-                    const int cnt = j + q * G < ng ? (int)((w[q].y >> 24) & 3u) : -1;
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) xv[q][t] = t <= cnt ? (ACC)__ldg(x + c[q][t]) : (ACC)0;
-                }
-#pragma unroll
-                for (int q = 0; q < NG; ++q)
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) acc += xv[q][t] * vv[q][t];
-#pragma unroll
-                for (int q = 0; q < NG; ++q) {
-                    w[q] = wn[q];
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) vv[q][t] = vn[q][t];
-                }
-            }
-#pragma unroll
-            for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            ACC r = __shfl_sync(0xffffffffu, acc, ((lane - sub) & (R - 1)) * G);
-            if (lane >= sub && lane < sub + R) mine = r;
-        }
+        const ACC mine = pk_chunk_sums<VT, ACC, G, NG>(prow, m, gidx, gside, S, L, val, x, base);
         const int64_t row = base + lane;
         if (row < m) epi(row, mine);
     }

@@ -17,6 +17,7 @@
 
 #include "fair_internal.cuh"
 #include "rows.cuh"
+#include "sirt_epi.cuh"
 
 namespace fair {
 
@@ -26,13 +27,6 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-__device__ __forceinline__ double box(double t, int bmode, double lb, double ub) {
-    // AIRMs.f90:1093-1100: upper bound first, then lower bound
-    if (bmode & 1) t = fmin_f(t, ub);
-    if (bmode & 2) t = fmax_f(t, lb);
-    return t;
 }
 
 // Block sum of one double per thread into partials[blockIdx.x] (fixed order).
@@ -49,48 +43,7 @@ __device__ __forceinline__ void block_partial(double v, double *partials) {
     }
 }
 
-// ---- epilogues ----------------------------------------------------------------
-struct EpiResidF64 {  // r = (b - Ax) / M
-    const double *b, *M;
-    double *r;
-    __device__ void operator()(int64_t i, double acc) const {
-        r[i] = __ddiv_rn(__dsub_rn(b[i], acc), M[i]);
-    }
-};
-struct EpiResidLP {  // same, FP32 dot, FP64 weighting, FP32 residual
-    const double *b, *M;
-    float *r;
-    double scale;  // 1, or the fixed-point scale of 16-bit codes
-    __device__ void operator()(int64_t i, float acc) const {
-        r[i] = (float)__ddiv_rn(__dsub_rn(b[i], __dmul_rn((double)acc, scale)), M[i]);
-    }
-};
-struct EpiUpdateF64 {  // x = P(x + omg * (A'r) / D)
-    const double *D;
-    double *x;
-    double omg, lb, ub;
-    int bmode;
-    __device__ void operator()(int64_t j, double acc) const {
-        double g = __dmul_rn(omg, acc);
-        if (D) g = __ddiv_rn(g, D[j]);
-        x[j] = box(__dadd_rn(x[j], g), bmode, lb, ub);
-    }
-};
-struct EpiUpdateLP {
-    const double *D;
-    double *x;
-    float *x32;
-    double omg, lb, ub;
-    int bmode;
-    double scale;  // 1, or the fixed-point scale of 16-bit codes
-    __device__ void operator()(int64_t j, float acc) const {
-        double g = __dmul_rn(omg, __dmul_rn((double)acc, scale));
-        if (D) g = __ddiv_rn(g, D[j]);
-        double t = box(__dadd_rn(x[j], g), bmode, lb, ub);
-        x[j] = t;
-        x32[j] = (float)t;
-    }
-};
+// ---- epilogues (SIRT ones in sirt_epi.cuh) ----------------------------------------
 struct EpiGdUpdate {  // xn = P(x - step * A'r), partial sum of (xn - x)^2
     const double *x;
     double *xn;
@@ -98,7 +51,7 @@ struct EpiGdUpdate {  // xn = P(x - step * A'r), partial sum of (xn - x)^2
     int bmode;
     double part = 0.0;
     __device__ void operator()(int64_t j, double acc) {
-        double t = box(__dsub_rn(x[j], __dmul_rn(step, acc)), bmode, lb, ub);
+        double t = sirt_box(__dsub_rn(x[j], __dmul_rn(step, acc)), bmode, lb, ub);
         xn[j] = t;
         double d = t - x[j];
         part += d * d;
@@ -398,7 +351,7 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
 }
 
 // One pass of a SIRT iteration: pass 1 = residual over A, pass 2 = update over A'.
-static void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
+void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
     const DevCSR &M = pass == 1 ? *S.A : *S.AT;
     if (M.m == 0) return;
     if (S.prec == FAIR_PREC_F64) {

@@ -54,13 +54,17 @@ def grains(N: int, cells: int, seed: int = 2) -> np.ndarray:
     vals = rng.uniform(0.0, 1.0, cells)
     X, Y = _grid01(N)
     P = np.stack([X.ravel(), Y.ravel()], 1)
-    best = np.full(P.shape[0], np.inf)
-    lab = np.zeros(P.shape[0], np.int64)
-    for k in range(cells):
-        d = (P[:, 0] - pts[k, 0]) ** 2 + (P[:, 1] - pts[k, 1]) ** 2
-        upd = d < best
-        best[upd] = d[upd]
-        lab[upd] = k
+    try:  # nearest seed by k-d tree when scipy is present
+        from scipy.spatial import cKDTree
+        lab = cKDTree(pts).query(P)[1]
+    except ImportError:
+        best = np.full(P.shape[0], np.inf)
+        lab = np.zeros(P.shape[0], np.int64)
+        for k in range(cells):
+            d = (P[:, 0] - pts[k, 0]) ** 2 + (P[:, 1] - pts[k, 1]) ** 2
+            upd = d < best
+            best[upd] = d[upd]
+            lab[upd] = k
     return vectorise(vals[lab].reshape(N, N))
 
 

@@ -82,6 +82,9 @@ def test_no_gpu_is_an_error(fair):
     with pytest.raises(fair.FairError) as ei:
         fair.CSRMatrix()
     assert ei.value.status == 10
+    with pytest.raises(fair.FairError) as ei:
+        fair.Batch("f32")
+    assert ei.value.status == 10
 
 
 def test_missing_library_raises(monkeypatch):

@@ -1,0 +1,146 @@
+"""Batched SIRT/SART over problems of different sizes (include/fair_batch.h).
+
+A batched iteration runs, problem by problem, the single-problem engine and
+epilogue with the same lanes per row and groups per lane, so with the same
+configuration the batch must reproduce fair_sirt on each problem bit for
+bit (FP64 and the packed FP32 form); against the oracle the bars are the
+single-problem ones (FP64 1e-10; f32 1e-5; f16 5e-3; q16 1e-4).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+GEOMS = [  # (kind, N, nth, p)
+    ("fan", 24, 40, 35), ("par", 32, 30, 46), ("fan", 40, 64, 57), ("par", 16, 20, 24),
+    ("fan", 32, 50, 46),
+]
+
+
+def build(fair, oracle, kind, n, nth, p):
+    if kind == "fan":
+        th = 2 * np.pi * np.arange(nth) / nth
+        A = fair.fanlineartomo(fair.Data(n=n, p=p, nth=nth, r=2.0, dw=p / n, sd=2.0, theta=th))
+        R = oracle.fanlineartomo(n, nth, p, 2.0, p / n, 2.0, th)
+    else:
+        th = np.pi * np.arange(nth) / nth
+        A = fair.paralleltomo(fair.Data(n=n, p=p, nth=nth, theta=th))
+        R = oracle.paralleltomo(n, nth, p, th)
+    return A, R
+
+
+@pytest.fixture(scope="module")
+def problems(fair, oracle):
+    out = []
+    for i, g in enumerate(GEOMS):
+        A, R = build(fair, oracle, *g)
+        x = fair.phantomgallery.grains(g[1], 20 + 10 * i, seed=i)
+        b = oracle.matvecmul(R, x)
+        out.append((A, R, b))
+    return out
+
+
+def make_batch(fair, problems, prec, take=False):
+    B = fair.Batch(prec)
+    for A, _, _ in problems:
+        B.add(A, take=take)
+    return B
+
+
+@pytest.mark.parametrize("method", ["sart", "cimmino"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_batch_equals_single(problems, fair, oracle, prec, method):
+    B = make_batch(fair, problems, prec)
+    B.set_config([8, 8, 1, 1])  # the single-problem defaults
+    o = fair.airms.options(lbound=0.0, ubound=1.0)
+    ball = np.concatenate([b for _, _, b in problems])
+    X = B.sirt(method, ball, 25, opts=o)
+    ro, co = B.offsets()
+    assert ro[-1] == ball.size
+    for p, (A, R, b) in enumerate(problems):
+        A.set_precision(prec)
+        try:
+            xs = fair.airms.sirt(method, A, b, 25, opts=o)
+        finally:
+            A.set_precision("f64")
+        assert np.array_equal(X[co[p]:co[p + 1]], xs)
+        xr = oracle.sirt(method, R, b, 25, opts=oracle.options(lbound=0.0, ubound=1.0))
+        assert rel_err(X[co[p]:co[p + 1]], xr) < (1e-10 if prec == "f64" else 1e-5)
+    B.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("f16", 5e-3), ("q16", 1e-4)])
+def test_batch_16bit(problems, fair, oracle, prec, tol):
+    B = make_batch(fair, problems, prec)
+    ball = np.concatenate([b for _, _, b in problems])
+    X = B.sirt("sart", ball, 30, opts=fair.airms.options(lbound=0.0, ubound=1.0))
+    _, co = B.offsets()
+    for p, (A, R, b) in enumerate(problems):
+        xr = oracle.sirt("sart", R, b, 30, opts=oracle.options(lbound=0.0, ubound=1.0))
+        assert rel_err(X[co[p]:co[p + 1]], xr) < tol
+    B.close()
+
+
+def test_device_api_graph_reuse_and_unbatched(problems, fair):
+    import torch
+    B = make_batch(fair, problems, "f32")
+    ball = np.concatenate([b for _, _, b in problems])
+    info = B.info()
+    assert info["problems"] == len(problems) and info["nnz"] > 0 and info["device_bytes"] > 0
+    o = fair.airms.options(lbound=0.0, ubound=1.0)
+    ref = B.sirt("sart", ball, 12, opts=o)
+    B.prepare("sart", o)
+    stream = torch.cuda.Stream()
+    B.set_stream(stream.cuda_stream)
+    d_b = torch.from_numpy(ball).cuda()
+    outs = []
+    for K, batched in ((12, True), (12, True), (7, True), (12, False)):
+        d_x = torch.zeros(info["cols"], dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        B.run_device(d_b.data_ptr(), d_x.data_ptr(), K, batched=batched)
+        stream.synchronize()
+        outs.append((K, d_x.cpu().numpy()))
+    assert np.array_equal(outs[0][1], ref) and np.array_equal(outs[1][1], ref)
+    assert np.array_equal(outs[3][1], ref)  # problem-by-problem launches, same numbers
+    assert not np.array_equal(outs[2][1], ref)
+    scratch = torch.zeros(info["cols"], dtype=torch.float64, device="cuda")
+    cfg = B.autotune(d_b.data_ptr(), scratch.data_ptr())
+    assert cfg[0] in (4, 8, 16, 32) and cfg[1] in (4, 8, 16, 32) and cfg[2] in (1, 2)
+    x = B.sirt("sart", ball, 12, opts=o)
+    assert rel_err(x, ref) < 1e-6
+    B.close()
+
+
+def test_take_moves_matrix(fair, oracle):
+    A, R = build(fair, oracle, "par", 16, 12, 24)
+    B = fair.Batch("f64")
+    B.add(A, take=True)
+    with pytest.raises(fair.FairError):
+        A.matvecmul(np.ones(R.n))
+    b = oracle.matvecmul(R, np.linspace(0, 1, R.n))
+    x = B.sirt("cimmino", b, 10)
+    assert rel_err(x, oracle.sirt("cimmino", R, b, 10)) < 1e-10
+    B.close()
+
+
+def test_batch_errors(fair):
+    B = fair.Batch("f32")
+    with pytest.raises(fair.FairError):
+        B.prepare("sart")  # empty batch
+    with pytest.raises(fair.FairError):
+        B.set_config([6, 8, 1, 1])
+    rng = np.random.default_rng(5)
+    m, n, per = 300, 5000, 60
+    JA = np.concatenate([np.sort(rng.choice(n, per, replace=False)) + 1 for _ in range(m)])
+    IA = np.arange(0, per * (m + 1), per, dtype=np.int32)
+    A = fair.CSRMatrix.construct(m, n, rng.random(m * per) + 0.1, IA, JA.astype(np.int32))
+    with pytest.raises(fair.FairError):
+        B.add(A)  # no packed stream for random columns
+    with pytest.raises(fair.FairError):
+        fair.Batch("f32").prepare("landweber")
+    B.close()
+    A.close()
