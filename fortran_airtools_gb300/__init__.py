@@ -12,11 +12,12 @@ All O(nnz) work runs in hand-written CUDA kernels; without the library the
 import of any of these modules raises at first use.
 """
 from ._clib import FairError, Opts, lib  # noqa: F401
-from . import airms, batch, phantomgallery, sparse_matrices, system_generation  # noqa: F401
+from . import airms, batch, mfree, phantomgallery, sparse_matrices, system_generation  # noqa: F401
 from .batch import Batch  # noqa: F401
+from .mfree import MatrixFree  # noqa: F401
 from .sparse_matrices import CSRMatrix  # noqa: F401
 from .system_generation import Data, fanlineartomo, linspace, paralleltomo  # noqa: F401
 
-__all__ = ["FairError", "Opts", "lib", "airms", "batch", "phantomgallery", "sparse_matrices",
-           "system_generation", "Batch", "CSRMatrix", "Data", "fanlineartomo", "linspace",
-           "paralleltomo"]
+__all__ = ["FairError", "Opts", "lib", "airms", "batch", "mfree", "phantomgallery",
+           "sparse_matrices", "system_generation", "Batch", "CSRMatrix", "Data", "MatrixFree",
+           "fanlineartomo", "linspace", "paralleltomo"]

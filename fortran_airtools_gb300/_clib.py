@@ -125,6 +125,17 @@ def _declare(L):
                               C.c_int),
         "fair_csr_packed_info": ([h, i32, P(i32), P(i64), P(i64), P(i32), P(i32)], C.c_int),
         "fair_sirt_autotune": ([h, vp, vp, i32, vp], C.c_int),
+        "fair_mf_create_parallel": ([P(h), P(Data), i32], C.c_int),
+        "fair_mf_destroy": ([h], C.c_int),
+        "fair_mf_set_stream": ([h, vp], C.c_int),
+        "fair_mf_info": ([h, P(i32), P(i32)], C.c_int),
+        "fair_mf_project": ([h, vp, vp], C.c_int),
+        "fair_mf_nnz": ([h, P(i64)], C.c_int),
+        "fair_mf_backproject": ([h, vp, vp], C.c_int),
+        "fair_mf_sirt": ([h, C.c_char_p, vp, i32, vp, P(Opts), vp], C.c_int),
+        "fair_mf_sirt_prepare": ([h, C.c_char_p, P(Opts)], C.c_int),
+        "fair_mf_sirt_run_device": ([h, vp, vp, i32], C.c_int),
+        "fair_mf_sirt_run_device_timed": ([h, vp, vp, i32, P(C.c_float), P(C.c_float)], C.c_int),
         "fair_batch_create": ([P(h), i32], C.c_int),
         "fair_batch_destroy": ([h], C.c_int),
         "fair_batch_set_stream": ([h, vp], C.c_int),

@@ -1,0 +1,549 @@
+// mfree.cu -- matrix-free parallel-beam projector / backprojector pair and
+// SIRT on it (include/fair_mf.h).
+//
+// Geometry of paralleltomo (system_generation.f90:309-492): ray (angle i,
+// bin j) is the line with unit normal n_i = (cos th_i, sin th_i) at offset
+// x0_j = j - (p-1)/2 (linspace(-(p-1)/2, (p-1)/2, p), unit bins), direction
+// (-sin, cos). Pixel (ix, iy) (ix from the left, iy from the bottom, both
+// 0..N-1) is the unit square centred at (ix + 1/2 - N/2, iy + 1/2 - N/2) and
+// is column ix*N + (N-1-iy) of the matrix (JA = floor(xm)*N + (N - floor(ym))).
+//
+// The ray's length inside a unit square is a function of the signed distance
+// d between the square's centre and the line (the chord of a unit square):
+// with c = max(|cos|, |sin|), s = min(...):
+//   L = 1/c                      for |d| <= (c - s)/2,
+//   L = ((c + s)/2 - |d|)/(c s)  for (c - s)/2 < |d| < (c + s)/2,  else 0,
+// which is the segment length the ray tracer measures between consecutive
+// crossings; segments of 1e-10 or less are dropped, as there. An axis-aligned
+// ray on a grid line (s = 0, |d| = 1/2) belongs to the pixel on the positive
+// side, as the reference's floor-of-midpoint rule gives.
+//
+// d = ix*cos + iy*sin + K_i - j with K_i = (1/2 - N/2)(cos + sin) + (p-1)/2,
+// evaluated in 64-bit fixed point with 46 fractional bits (N <= 8192 and
+// p <= 16384 keep every term below 2^60): exact integer
+// arithmetic, so every kernel computes bit-identical entries whatever the
+// order it meets the (ray, pixel) pairs in. The projector runs one thread
+// per ray and walks the image along the ray's faster axis (per column when
+// |sin| >= |cos|, else per row), testing the 2-3 pixels of each column (row)
+// that a float estimate brackets, conservatively; the backprojector runs one
+// thread per pixel and, per angle, the 1-3 rays whose offsets bracket the
+// pixel's. Both keep only pairs with L > 0, so they sum the same entries: an
+// exact adjoint pair, deterministic, without atomics.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "fair_internal.cuh"
+#include "fair_mf.h"
+#include "sirt_epi.cuh"
+
+namespace fair {
+
+namespace {
+
+constexpr int kFix = 46;
+constexpr double kOne = 70368744177664.0;  // 2^46
+
+struct MfAngle {
+    long long C, S, K;   // cos, sin, K_i in fixed point
+    long long H1, H2;    // (c - s)/2, (c + s)/2 in fixed point
+    long long Hcut;      // |d| >= Hcut leaves a segment of at most 1e-10: dropped
+    float Cf, Sf, Kf;    // float copies for the bracketing estimates
+    float inv_fast;      // 1/sin (per-column walk) or 1/cos (per-row walk)
+    float inv_c;         // 1/c
+    float scale_ramp;    // 2 * 2^-46 / (c s) (0 when s = 0; applied to the halved distance)
+    int tie;             // s = 0: +1 / -1 = sign of d that keeps |d| = 1/2; 0 otherwise
+    int by_column;       // 1: walk columns (|sin| >= |cos|)
+    double inv_c64, scale_ramp64;
+};
+
+// Conversion of 0 <= v < 2^47 to float / 2 (the last bit is below float
+// precision): two exact 23-bit halves through the 2^23 exponent trick.
+__device__ __forceinline__ float fix_to_float_half(long long v) {
+    const long long w = v >> 1;
+    const unsigned hi = (unsigned)(w >> 23), lo = (unsigned)(w & 0x7FFFFF);
+    const float fh = __int_as_float((int)(0x4B000000u | hi)) - 8388608.0f;
+    const float fl = __int_as_float((int)(0x4B000000u | lo)) - 8388608.0f;
+    return fmaf(fh, 8388608.0f, fl);
+}
+
+template <typename T> struct Chord;
+template <> struct Chord<float> {
+    static __device__ __forceinline__ float of(const MfAngle &A, long long d) {
+        const long long u = d < 0 ? -d : d;
+        if (u >= A.Hcut) {
+            // an axis-aligned ray on the pixel's edge belongs to the positive side
+            if (u == A.H2 && A.tie != 0 && (d > 0 ? 1 : -1) == A.tie) return A.inv_c;
+            return 0.f;
+        }
+        if (u <= A.H1) return A.inv_c;
+        return fix_to_float_half(A.H2 - u) * A.scale_ramp;
+    }
+};
+template <> struct Chord<double> {
+    static __device__ __forceinline__ double of(const MfAngle &A, long long d) {
+        const long long u = d < 0 ? -d : d;
+        if (u >= A.Hcut) {
+            // an axis-aligned ray on the pixel's edge belongs to the positive side
+            if (u == A.H2 && A.tie != 0 && (d > 0 ? 1 : -1) == A.tie) return A.inv_c64;
+            return 0.0;
+        }
+        if (u <= A.H1) return A.inv_c64;
+        return (double)(A.H2 - u) * A.scale_ramp64;
+    }
+};
+
+// ---- epilogues of the projector (per ray) and backprojector (per pixel) ---------
+template <typename T> struct EpiStore {  // y = A x (or A' r)
+    T *y;
+    __device__ void operator()(int64_t i, T acc) const { y[i] = acc; }
+};
+struct EpiCimminoW {  // M = m * sum_j a_ij^2 (the sum arrives in acc)
+    double *M;
+    double m;
+    __device__ void operator()(int64_t i, double acc) const { M[i] = m * acc; }
+};
+
+// Per ray r: MODE 0 sums a_rj * x_j, MODE 1 sums a_rj, MODE 2 sums a_rj^2,
+// MODE 3 counts the pixels with a_rj > 0 (x unused for MODE 1-3).
+template <typename XT, typename ACC, int MODE, class Epi>
+__global__ void __launch_bounds__(128) k_mf_project(const MfAngle *__restrict__ ang, int nth,
+                                                    int p, int N, const XT *__restrict__ x,
+                                                    Epi epi) {
+    const int64_t m = (int64_t)nth * p;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(r / p), j = (int)(r - (int64_t)i * p);
+        const MfAngle A = ang[i];
+        const long long K = A.K - ((long long)j << kFix);
+        const float Kf = A.Kf - (float)j;
+        ACC acc = 0;
+        // walk the faster axis: d = t*F + u*Q + K with t the walked index
+        const long long F = A.by_column ? A.C : A.S, Q = A.by_column ? A.S : A.C;
+        const float Ff = A.by_column ? A.Cf : A.Sf;
+        // the pixels u of step t with |d| <= H2 lie in [(-h2 - fA)/Q, (h2 - fA)/Q];
+        // fA (float) is within 1e-3 of t*F + K here, so widening h2 by 2e-3
+        // brackets every one of them (|Q| >= 0.7); the exact test is Chord
+        const float h2 = (float)(A.H2 * (1.0 / kOne)) + 2e-3f;
+        long long base = K;  // t = 0
+        for (int t = 0; t < N; ++t, base += F) {
+            const float fA = fmaf((float)t, Ff, Kf);
+            const float t1 = (-h2 - fA) * A.inv_fast, t2 = (h2 - fA) * A.inv_fast;
+            int lo = (int)ceilf(fminf(t1, t2)), hi = (int)floorf(fmaxf(t1, t2));
+            lo = max(lo, 0);
+            hi = min(hi, N - 1);
+            long long d = base + (long long)lo * Q;
+            for (int u = lo; u <= hi; ++u, d += Q) {
+                const ACC w = Chord<ACC>::of(A, d);
+                if (w > (ACC)0) {
+                    const int ix = A.by_column ? t : u, iy = A.by_column ? u : t;
+                    if (MODE == 0) acc += w * (ACC)__ldg(x + (int64_t)ix * N + (N - 1 - iy));
+                    else if (MODE == 1) acc += w;
+                    else if (MODE == 2) acc += w * w;
+                    else acc += (ACC)1;
+                }
+            }
+        }
+        epi(r, acc);
+    }
+}
+
+// Sum over the rays through pixel q of a_rq * y_r, for every pixel; MODE 1
+// sums a_rq (y unused).
+template <typename YT, typename ACC, int MODE, class Epi>
+__global__ void __launch_bounds__(128) k_mf_backproject(const MfAngle *__restrict__ ang,
+                                                        int nth, int p, int N,
+                                                        const YT *__restrict__ y, Epi epi) {
+    const int64_t n = (int64_t)N * N;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(q / N), iy = N - 1 - (int)(q - (int64_t)ix * N);
+        ACC acc = 0;
+        for (int i = 0; i < nth; ++i) {
+            const MfAngle &A = ang[i];
+            const long long base = (long long)ix * A.C + (long long)iy * A.S + A.K;
+            // rays j with |base - j 2^40| <= H2
+            const long long jlo = -((A.H2 - base) >> kFix), jhi = (base + A.H2) >> kFix;
+            const int j0 = (int)max(jlo, 0LL), j1 = (int)min(jhi, (long long)p - 1);
+            long long d = base - ((long long)j0 << kFix);
+            for (int j = j0; j <= j1; ++j, d -= (1LL << kFix)) {
+                const ACC w = Chord<ACC>::of(A, d);
+                if (w > (ACC)0) {
+                    if (MODE == 0) acc += w * (ACC)__ldg(y + (int64_t)i * p + j);
+                    else acc += w;
+                }
+            }
+        }
+        epi(q, acc);
+    }
+}
+
+int grid_for(int64_t items, int threads) {
+    int64_t b = (items + threads - 1) / threads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm_count() * 32));
+}
+
+}  // namespace
+}  // namespace fair
+
+struct fair_mf_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int prec = FAIR_PREC_F32;
+    int N = 0, p = 0, nth = 0;
+    fair::DevBuf ang;                  // MfAngle [nth]
+    fair::DevBuf w_in, w_out;          // host-call staging (FP64)
+    fair::DevBuf v_a, v_b;             // reduced-precision staging
+    // SIRT state
+    bool ready = false, sart = false;
+    double omg = 1.0, lb = 0.0, ub = 0.0;
+    int bmode = 0;
+    fair::DevBuf M_sart, M_cim, D;     // FP64 weights (computed on first use)
+    bool have_sart = false, have_cim = false;
+    fair::DevBuf x32, r, w_b, w_x;
+    std::mutex mu;
+};
+
+namespace fair {
+namespace {
+
+int mf_weights(fair_mf A, bool sart, cudaStream_t s) {
+    const int64_t m = (int64_t)A->nth * A->p, n = (int64_t)A->N * A->N;
+    const MfAngle *ang = A->ang.as<MfAngle>();
+    if (sart && !A->have_sart) {
+        FAIR_TRY(A->M_sart.grow(sizeof(double) * (m + 1)));
+        FAIR_TRY(A->D.grow(sizeof(double) * (n + 1)));
+        EpiStore<double> e1{A->M_sart.as<double>()};
+        k_mf_project<double, double, 1><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N,
+                                                                          nullptr, e1);
+        EpiStore<double> e2{A->D.as<double>()};
+        k_mf_backproject<double, double, 1><<<grid_for(n, 128), 128, 0, s>>>(ang, A->nth, A->p,
+                                                                              A->N, nullptr, e2);
+        FAIR_CUDA(cudaGetLastError());
+        A->have_sart = true;
+    }
+    if (!sart && !A->have_cim) {
+        FAIR_TRY(A->M_cim.grow(sizeof(double) * (m + 1)));
+        EpiCimminoW e{A->M_cim.as<double>(), (double)m};
+        k_mf_project<double, double, 2><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N,
+                                                                          nullptr, e);
+        FAIR_CUDA(cudaGetLastError());
+        A->have_cim = true;
+    }
+    return FAIR_OK;
+}
+
+// One projector / backprojector pass of a SIRT iteration.
+void mf_pass(fair_mf A, int pass, const double *d_b, double *d_x, cudaStream_t s) {
+    const int64_t m = (int64_t)A->nth * A->p, n = (int64_t)A->N * A->N;
+    const MfAngle *ang = A->ang.as<MfAngle>();
+    const double *M = A->sart ? A->M_sart.as<double>() : A->M_cim.as<double>();
+    const double *D = A->sart ? A->D.as<double>() : nullptr;
+    if (A->prec == FAIR_PREC_F64) {
+        if (pass == 1) {
+            EpiResidF64 e{d_b, M, A->r.as<double>()};
+            k_mf_project<double, double, 0><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p,
+                                                                              A->N, d_x, e);
+        } else {
+            EpiUpdateF64 e{D, d_x, A->omg, A->lb, A->ub, A->bmode};
+            k_mf_backproject<double, double, 0><<<grid_for(n, 128), 128, 0, s>>>(
+                ang, A->nth, A->p, A->N, A->r.as<double>(), e);
+        }
+    } else {
+        if (pass == 1) {
+            EpiResidLP e{d_b, M, A->r.as<float>(), 1.0};
+            k_mf_project<float, float, 0><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N,
+                                                                            A->x32.as<float>(), e);
+        } else {
+            EpiUpdateLP e{D, d_x, A->x32.as<float>(), A->omg, A->lb, A->ub, A->bmode, 1.0};
+            k_mf_backproject<float, float, 0><<<grid_for(n, 128), 128, 0, s>>>(
+                ang, A->nth, A->p, A->N, A->r.as<float>(), e);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace fair
+
+#define MENTER(A)                                                  \
+    do {                                                           \
+        if (!(A)) { fair::set_detail("null operator"); return FAIR_ERR_NULL; } \
+        FAIR_CUDA(cudaSetDevice((A)->device));                     \
+    } while (0)
+
+extern "C" {
+
+int fair_mf_create_parallel(fair_mf *out, const fair_data *dat, int32_t prec) {
+    if (!out || !dat || !dat->theta) return FAIR_ERR_NULL;
+    *out = nullptr;
+    if (prec != FAIR_PREC_F64 && prec != FAIR_PREC_F32) {
+        fair::set_detail("the matrix-free operator runs in FP64 or FP32");
+        return FAIR_ERR_ARG;
+    }
+    const int N = dat->n, p = dat->p, nth = dat->nth;
+    if (N < 1 || p < 2 || nth < 1) { fair::set_detail("n >= 1, p >= 2, nth >= 1 required"); return FAIR_ERR_ARG; }
+    if ((int64_t)nth * p > INT32_MAX || N > 8192 || p > 16384) {
+        fair::set_detail("the matrix-free operator needs n <= 8192, p <= 16384, nth*p < 2^31");
+        return FAIR_ERR_ARG;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        fair::set_detail(e != cudaSuccess ? cudaGetErrorString(e) : "no CUDA device");
+        return FAIR_ERR_NOGPU;
+    }
+    fair_mf A = new (std::nothrow) fair_mf_s();
+    if (!A) return FAIR_ERR_ALLOC;
+    cudaGetDevice(&A->device);
+    A->prec = prec;
+    A->N = N;
+    A->p = p;
+    A->nth = nth;
+    e = cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete A;
+        return fair::cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+    }
+    A->own_stream = true;
+    // per-angle constants (cos/sin from the host libm, as paralleltomo)
+    std::vector<fair::MfAngle> t(nth);
+    for (int i = 0; i < nth; ++i) {
+        const double C = cos(dat->theta[i]), S = sin(dat->theta[i]);
+        const double K = (0.5 - 0.5 * N) * (C + S) + 0.5 * (p - 1);
+        const double c = std::max(fabs(C), fabs(S)), s = std::min(fabs(C), fabs(S));
+        fair::MfAngle &a = t[i];
+        a.C = llround(C * fair::kOne);
+        a.S = llround(S * fair::kOne);
+        a.K = llround(K * fair::kOne);
+        a.H1 = llround(0.5 * (c - s) * fair::kOne);
+        a.H2 = llround(0.5 * (c + s) * fair::kOne);
+        a.Cf = (float)C;
+        a.Sf = (float)S;
+        a.Kf = (float)K;
+        a.by_column = fabs(S) >= fabs(C) ? 1 : 0;
+        a.inv_fast = (float)(1.0 / (a.by_column ? S : C));
+        a.inv_c = (float)(1.0 / c);
+        a.inv_c64 = 1.0 / c;
+        a.scale_ramp = s > 0 ? (float)(2.0 / (fair::kOne * c * s)) : 0.f;
+        a.scale_ramp64 = s > 0 ? 1.0 / (fair::kOne * c * s) : 0.0;
+        a.tie = 0;
+        if (a.S == 0) a.tie = C > 0 ? 1 : -1;        // vertical ray, normal (+-1, 0)
+        else if (a.C == 0) a.tie = S > 0 ? 1 : -1;   // horizontal ray, normal (0, +-1)
+        if (a.tie != 0) a.H1 = a.H2;                 // s = 0: no ramp
+        // segments of 1e-10 or less are dropped, as the ray tracer does
+        // (system_generation.f90:393-394)
+        a.Hcut = a.tie != 0 ? a.H2 : a.H2 - (long long)floor(1e-10 * c * s * fair::kOne);
+    }
+    if (A->ang.grow(sizeof(fair::MfAngle) * nth) != FAIR_OK ||
+        cudaMemcpy(A->ang.p, t.data(), sizeof(fair::MfAngle) * nth, cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+        fair_mf_destroy(A);
+        return FAIR_ERR_ALLOC;
+    }
+    *out = A;
+    return FAIR_OK;
+}
+
+int fair_mf_destroy(fair_mf A) {
+    if (!A) return FAIR_OK;
+    cudaSetDevice(A->device);
+    cudaStreamSynchronize(A->stream);
+    for (fair::DevBuf *d : {&A->ang, &A->w_in, &A->w_out, &A->v_a, &A->v_b, &A->M_sart,
+                            &A->M_cim, &A->D, &A->x32, &A->r, &A->w_b, &A->w_x})
+        d->release();
+    if (A->own_stream) cudaStreamDestroy(A->stream);
+    delete A;
+    return FAIR_OK;
+}
+
+int fair_mf_set_stream(fair_mf A, void *cuda_stream) {
+    MENTER(A);
+    std::lock_guard<std::mutex> lk(A->mu);
+    FAIR_CUDA(cudaStreamSynchronize(A->stream));
+    if (A->own_stream) cudaStreamDestroy(A->stream);
+    if (cuda_stream) {
+        A->stream = (cudaStream_t)cuda_stream;
+        A->own_stream = false;
+    } else {
+        FAIR_CUDA(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
+        A->own_stream = true;
+    }
+    return FAIR_OK;
+}
+
+int fair_mf_info(fair_mf A, int32_t *m, int32_t *n) {
+    if (!A) return FAIR_ERR_NULL;
+    if (m) *m = A->nth * A->p;
+    if (n) *n = A->N * A->N;
+    return FAIR_OK;
+}
+
+static int mf_apply(fair_mf A, bool back, const double *in, double *out) {
+    MENTER(A);
+    if (!in || !out) return FAIR_ERR_NULL;
+    std::lock_guard<std::mutex> lk(A->mu);
+    const int64_t m = (int64_t)A->nth * A->p, n = (int64_t)A->N * A->N;
+    const int64_t nin = back ? m : n, nout = back ? n : m;
+    cudaStream_t s = A->stream;
+    FAIR_TRY(A->w_in.grow(sizeof(double) * (nin + 1)));
+    FAIR_TRY(A->w_out.grow(sizeof(double) * (nout + 1)));
+    FAIR_CUDA(cudaMemcpyAsync(A->w_in.p, in, sizeof(double) * nin, cudaMemcpyHostToDevice, s));
+    const fair::MfAngle *ang = A->ang.as<fair::MfAngle>();
+    if (A->prec == FAIR_PREC_F64) {
+        fair::EpiStore<double> e{A->w_out.as<double>()};
+        if (back)
+            fair::k_mf_backproject<double, double, 0><<<fair::grid_for(n, 128), 128, 0, s>>>(
+                ang, A->nth, A->p, A->N, A->w_in.as<double>(), e);
+        else
+            fair::k_mf_project<double, double, 0><<<fair::grid_for(m, 128), 128, 0, s>>>(
+                ang, A->nth, A->p, A->N, A->w_in.as<double>(), e);
+        FAIR_CUDA(cudaGetLastError());
+    } else {
+        FAIR_TRY(A->v_a.grow(sizeof(float) * (nin + 1)));
+        FAIR_TRY(A->v_b.grow(sizeof(float) * (nout + 1)));
+        FAIR_TRY(fair::vec_to_f32(A->w_in.as<double>(), nin, A->v_a.as<float>(), s));
+        fair::EpiStore<float> e{A->v_b.as<float>()};
+        if (back)
+            fair::k_mf_backproject<float, float, 0><<<fair::grid_for(n, 128), 128, 0, s>>>(
+                ang, A->nth, A->p, A->N, A->v_a.as<float>(), e);
+        else
+            fair::k_mf_project<float, float, 0><<<fair::grid_for(m, 128), 128, 0, s>>>(
+                ang, A->nth, A->p, A->N, A->v_a.as<float>(), e);
+        FAIR_CUDA(cudaGetLastError());
+        FAIR_TRY(fair::vec_to_f64(A->v_b.as<float>(), nout, A->w_out.as<double>(), s));
+    }
+    FAIR_CUDA(cudaMemcpyAsync(out, A->w_out.p, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    return FAIR_OK;
+}
+
+int fair_mf_nnz(fair_mf A, int64_t *nnz) {
+    MENTER(A);
+    if (!nnz) return FAIR_ERR_NULL;
+    std::lock_guard<std::mutex> lk(A->mu);
+    const int64_t m = (int64_t)A->nth * A->p;
+    cudaStream_t s = A->stream;
+    FAIR_TRY(A->w_out.grow(sizeof(double) * (m + 1)));
+    fair::EpiStore<double> e{A->w_out.as<double>()};
+    fair::k_mf_project<double, double, 3><<<fair::grid_for(m, 128), 128, 0, s>>>(
+        A->ang.as<fair::MfAngle>(), A->nth, A->p, A->N, nullptr, e);
+    FAIR_CUDA(cudaGetLastError());
+    std::vector<double> c(m);
+    FAIR_CUDA(cudaMemcpyAsync(c.data(), A->w_out.p, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    int64_t t = 0;
+    for (double v : c) t += (int64_t)v;
+    *nnz = t;
+    return FAIR_OK;
+}
+
+int fair_mf_project(fair_mf A, const double *x, double *y) { return mf_apply(A, false, x, y); }
+int fair_mf_backproject(fair_mf A, const double *y, double *x) { return mf_apply(A, true, y, x); }
+
+int fair_mf_sirt_prepare(fair_mf A, const char *sirt_method, const fair_opts *options) {
+    MENTER(A);
+    if (!sirt_method) return FAIR_ERR_NULL;
+    bool sart;
+    if (!strcmp(sirt_method, "cimmino")) sart = false;
+    else if (!strcmp(sirt_method, "sart")) sart = true;
+    else { fair::set_detail("Not a recognised SIRT method."); return FAIR_ERR_METHOD; }
+    std::lock_guard<std::mutex> lk(A->mu);
+    fair_opts o;
+    if (options) o = *options;
+    else FAIR_TRY(fair_opts_initialise(&o));
+    A->sart = sart;
+    A->omg = o.relaxpar;
+    A->lb = o.lbound;
+    A->ub = o.ubound;
+    A->bmode = (o.upb ? 1 : 0) | (o.lwrb ? 2 : 0);
+    const int64_t m = (int64_t)A->nth * A->p, n = (int64_t)A->N * A->N;
+    const bool red = A->prec != FAIR_PREC_F64;
+    FAIR_TRY(A->r.grow((red ? sizeof(float) : sizeof(double)) * (m + 1)));
+    if (red) FAIR_TRY(A->x32.grow(sizeof(float) * (n + 1)));
+    FAIR_TRY(fair::mf_weights(A, sart, A->stream));
+    FAIR_CUDA(cudaStreamSynchronize(A->stream));
+    A->ready = true;
+    return FAIR_OK;
+}
+
+static int mf_iterations(fair_mf A, const double *d_b, double *d_x, int32_t K, float *ms1,
+                         float *ms2) {
+    if (!A->ready) {
+        fair::set_detail("call fair_mf_sirt_prepare first");
+        return FAIR_ERR_STATE;
+    }
+    if (!d_b || !d_x) return FAIR_ERR_NULL;
+    if (K < 0) { fair::set_detail("K >= 0 required"); return FAIR_ERR_ARG; }
+    cudaStream_t s = A->stream;
+    const int64_t n = (int64_t)A->N * A->N;
+    if (A->prec != FAIR_PREC_F64) FAIR_TRY(fair::vec_to_f32(d_x, n, A->x32.as<float>(), s));
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    if (ms1)
+        for (auto &e : ev) FAIR_CUDA(cudaEventCreate(&e));
+    float t1 = 0.f, t2 = 0.f;
+    int st = FAIR_OK;
+    for (int it = 0; it < K; ++it) {
+        if (ms1) cudaEventRecord(ev[0], s);
+        fair::mf_pass(A, 1, d_b, d_x, s);
+        if (ms1) cudaEventRecord(ev[1], s);
+        fair::mf_pass(A, 2, d_b, d_x, s);
+        if (ms1) {
+            cudaEventRecord(ev[2], s);
+            cudaError_t e = cudaEventSynchronize(ev[2]);
+            if (e != cudaSuccess) { st = fair::cuda_fail(e, "matrix-free pass", __FILE__, __LINE__); break; }
+            float a = 0.f, b = 0.f;
+            cudaEventElapsedTime(&a, ev[0], ev[1]);
+            cudaEventElapsedTime(&b, ev[1], ev[2]);
+            t1 += a;
+            t2 += b;
+        }
+    }
+    if (ms1) {
+        for (auto &e : ev) cudaEventDestroy(e);
+        *ms1 = t1;
+        *ms2 = t2;
+    }
+    if (st != FAIR_OK) return st;
+    FAIR_CUDA(cudaGetLastError());
+    return FAIR_OK;
+}
+
+int fair_mf_sirt_run_device(fair_mf A, const double *d_b, double *d_x, int32_t K) {
+    MENTER(A);
+    std::lock_guard<std::mutex> lk(A->mu);
+    return mf_iterations(A, d_b, d_x, K, nullptr, nullptr);
+}
+
+int fair_mf_sirt_run_device_timed(fair_mf A, const double *d_b, double *d_x, int32_t K,
+                                  float *ms_project, float *ms_backproject) {
+    MENTER(A);
+    if (!ms_project || !ms_backproject) return FAIR_ERR_NULL;
+    std::lock_guard<std::mutex> lk(A->mu);
+    return mf_iterations(A, d_b, d_x, K, ms_project, ms_backproject);
+}
+
+int fair_mf_sirt(fair_mf A, const char *sirt_method, const double *b, int32_t K,
+                 const double *x0, const fair_opts *options, double *x) {
+    MENTER(A);
+    if (!b || !x) return FAIR_ERR_NULL;
+    FAIR_TRY(fair_mf_sirt_prepare(A, sirt_method, options));
+    std::lock_guard<std::mutex> lk(A->mu);
+    const int64_t m = (int64_t)A->nth * A->p, n = (int64_t)A->N * A->N;
+    cudaStream_t s = A->stream;
+    FAIR_TRY(A->w_b.grow(sizeof(double) * (m + 1)));
+    FAIR_TRY(A->w_x.grow(sizeof(double) * (n + 1)));
+    FAIR_CUDA(cudaMemcpyAsync(A->w_b.p, b, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    if (x0) FAIR_CUDA(cudaMemcpyAsync(A->w_x.p, x0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    else FAIR_CUDA(cudaMemsetAsync(A->w_x.p, 0, sizeof(double) * n, s));
+    FAIR_TRY(mf_iterations(A, A->w_b.as<double>(), A->w_x.as<double>(), K, nullptr, nullptr));
+    FAIR_CUDA(cudaMemcpyAsync(x, A->w_x.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    return FAIR_OK;
+}
+
+}  // extern "C"
