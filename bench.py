@@ -223,11 +223,6 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     L = lib()
-    L.fair_sirt_prepare.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
-    L.fair_sirt_run_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
-    L.fair_sirt_run_device_timed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
-                                             C.POINTER(C.c_float), C.POINTER(C.c_float)]
-    L.fair_sirt_launches.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]
 
     def barrier():
         if world > 1:
@@ -660,8 +655,6 @@ def run_mfree(args):
             A.set_stream(stream.cuda_stream)
             A.set_precision("f32")
             L = lib()
-            L.fair_sirt_prepare.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
-            L.fair_sirt_run_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
             check(L.fair_sirt_prepare(A.handle, b"cimmino", C.byref(opts)))
             cfg = (C.c_int32 * 4)()
             check(L.fair_sirt_autotune(A.handle, d_b.data_ptr(), d_x.data_ptr(), 3, cfg))

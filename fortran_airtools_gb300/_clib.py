@@ -125,6 +125,22 @@ def _declare(L):
                               C.c_int),
         "fair_csr_packed_info": ([h, i32, P(i32), P(i64), P(i64), P(i32), P(i32)], C.c_int),
         "fair_sirt_autotune": ([h, vp, vp, i32, vp], C.c_int),
+        "fair_sirt_prepare": ([h, C.c_char_p, P(Opts)], C.c_int),
+        "fair_sirt_run_device": ([h, vp, vp, i32], C.c_int),
+        "fair_sirt_run_device_timed": ([h, vp, vp, i32, P(C.c_float), P(C.c_float)], C.c_int),
+        "fair_sirt_launches": ([h, i32, P(i64)], C.c_int),
+        "fair_spmv_device": ([h, i32, vp, vp], C.c_int),
+        "fair_matvecmul_noalloc": ([h, vp, i64, vp], C.c_int),
+        "fair_write_csr_file": ([C.c_char_p, i32, i32, i32, vp, vp, vp], C.c_int),
+        "fair_read_csr_file_sizes": ([C.c_char_p, P(i32), P(i32), P(i32)], C.c_int),
+        "fair_read_csr_file": ([C.c_char_p, vp, vp, vp], C.c_int),
+        "fair_store_matrix": ([h, C.c_char_p], C.c_int),
+        "fair_read_csr_matrix": ([h, C.c_char_p], C.c_int),
+        "fair_read_data_sizes": ([C.c_char_p, P(i32), P(i32), P(i32)], C.c_int),
+        "fair_read_data": ([C.c_char_p, vp, vp, vp], C.c_int),
+        "fair_read_ordering": ([C.c_char_p, P(i32), vp, i32], C.c_int),
+        "fair_read_ref": ([C.c_char_p, i64, vp], C.c_int),
+        "fair_write_values": ([C.c_char_p, vp, i64], C.c_int),
         "fair_mf_create_parallel": ([P(h), P(Data), i32], C.c_int),
         "fair_mf_destroy": ([h], C.c_int),
         "fair_mf_set_stream": ([h, vp], C.c_int),

@@ -2,7 +2,9 @@
 
 Every translation unit under csrc/ is compiled for sm_103a only (one
 -gencode, no PTX for other targets) in parallel, then linked into
-fortran_airtools_gb300/_lib/libfair_gb300.so against the shared CUDA runtime.
+fortran_airtools_gb300/_lib/libfair_gb300.so against the shared CUDA runtime;
+the main.exe drop-in (cli/fair_main.cpp) is linked against it as
+_lib/fair_main.
 Host code is compiled with -ffp-contract=off so that host-side geometry
 tables round every product separately (aarch64 g++ would otherwise fuse
 multiply-adds).
@@ -78,7 +80,20 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    build_cli(nvcc)
     return lib
+
+
+def build_cli(nvcc: str) -> str:
+    """The main.exe drop-in, linked against the library beside it."""
+    exe = os.path.join(OUT_DIR, "fair_main")
+    cmd = [nvcc, "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "cli", "fair_main.cpp"),
+           "-I", os.path.join(ROOT, "include"), "-L", OUT_DIR, "-lfair_gb300",
+           "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("fair_main build failed:\n" + r.stdout + r.stderr)
+    return exe
 
 
 if __name__ == "__main__":

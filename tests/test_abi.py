@@ -33,6 +33,15 @@ def test_library_exports_every_declared_symbol(fair):
     assert not missing, missing
 
 
+def test_every_symbol_has_a_signature(fair):
+    """Every entry point is declared with argtypes in the bindings: an
+    undeclared one would take pointer arguments as 32-bit ints."""
+    import fortran_airtools_gb300._clib as clib
+    src = open(clib.__file__).read()
+    missing = [n for n in declared_symbols() if f'"{n}"' not in src]
+    assert not missing, missing
+
+
 def test_error_strings(fair):
     L = fair.lib()
     assert L.fair_error_string(1) == b"Vector input size incorrect."

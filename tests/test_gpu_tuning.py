@@ -42,7 +42,6 @@ def test_autotune(prob, fair, oracle):
     from fortran_airtools_gb300._clib import check, lib
     A, R, b = prob
     L = lib()
-    L.fair_sirt_prepare.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
     opts = fair.airms.options()
     A.set_precision("f32")
     try:
