@@ -613,7 +613,10 @@ def run_mfree(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     out = {}
-    for n, nth, p in ((2048, 1440, 2896), (1024, 720, 1448)):
+    sizes = [(2048, 1440, 2896), (1024, 720, 1448)]
+    if args.mf_sizes:
+        sizes = [s for s in sizes if str(s[0]) in args.mf_sizes.split(",")]
+    for n, nth, p in sizes:
         th = np.pi * np.arange(nth) / nth
         d = F.Data(n=n, p=p, nth=nth, theta=th)
         M64 = F.MatrixFree(d, "f64")
@@ -673,10 +676,11 @@ def run_mfree(args):
             res["stored_f32"] = {"iter_per_s": K / (ms_s / 1e3), "ms_per_iteration": ms_s / K,
                                  "pass_config": list(cfg)}
             A.close()
+        res["geometry"] = f"parallel beam N={n}, {nth} angles over [0,pi), {p} bins"
         out[f"N={n}"] = res
-    big = out["N=2048"]
+    big = out.get("N=2048") or next(iter(out.values()))
     line = {"metric": "matrix-free SIRT iter/s (Cimmino, FP32)",
-            "workload": "parallel beam N=2048, 1440 angles over [0,pi), 2896 bins",
+            "workload": big["geometry"],
             "value": big["iter_per_s"], "unit": "iter/s", "iterations": K, "dtype": "f32",
             "ms_per_iteration": big["ms_per_iteration"], "nnz_if_stored": big["nnz"],
             "stored_fp64_bytes_per_copy": big["nnz"] * 12,
@@ -711,6 +715,8 @@ def main():
                     help="sirt: the headline line; kaczmarz, adjoint, batch, mfree: secondary lines")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--batch-prec", choices=["f64", "f32", "f16", "q16"], default="f32")
+    ap.add_argument("--mf-sizes", default="",
+                    help="matrix-free cases to run, by N (comma list of 2048, 1024; default both)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
