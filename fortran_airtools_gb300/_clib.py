@@ -141,6 +141,9 @@ def _declare(L):
         "fair_read_ordering": ([C.c_char_p, P(i32), vp, i32], C.c_int),
         "fair_read_ref": ([C.c_char_p, i64, vp], C.c_int),
         "fair_write_values": ([C.c_char_p, vp, i64], C.c_int),
+        "fair_phantom": ([C.c_char_p, i32, vp], C.c_int),
+        "fair_phantom_device": ([C.c_char_p, i32, vp, vp], C.c_int),
+        "fair_add_white_noise_device": ([vp, vp, vp, i64, d, vp], C.c_int),
         "fair_mf_create_parallel": ([P(h), P(Data), i32], C.c_int),
         "fair_mf_destroy": ([h], C.c_int),
         "fair_mf_set_stream": ([h, vp], C.c_int),

@@ -16,8 +16,9 @@
 // Added here: -I[inputfile] runs the input-file mode of main.f90:222-271
 // (read_data, angle culling by -c, -f reference solution, the grid scaling,
 // fanlineartomo, A scaled by grid_size/N, b = -log(T)), which the shipped
-// binary never reaches. Phantoms: 'shepplogan' (the reference's table);
-// the gallery's other phantoms are not part of this build. The environment
+// binary never reaches. Phantoms (computed on the GPU): 'shepplogan',
+// 'smooth', 'grains', '3phases'; the gallery's others are not part of this
+// build. The environment
 // variable FAIR_SEED seeds the library's random stream (the reference's
 // random_number is unseeded).
 #include <chrono>
@@ -30,6 +31,7 @@
 
 #include "fair_gpu.h"
 #include "fair_io.h"
+#include "fair_phantom.h"
 
 namespace {
 
@@ -265,11 +267,12 @@ int main(int argc, char **argv) {
             if (verbose) printf(" Constructing matrix...\n");
             check(fair_paralleltomo(&dat, A), "paralleltomo");
         }
-        if (inputphantom != "shepplogan")
-            stop("Phantom " + inputphantom + " is not part of this build; use 'shepplogan'.");
+        if (!one_of(inputphantom, {"shepplogan", "smooth", "grains", "3phases"}))
+            stop("Phantom " + inputphantom + " is not part of this build; use 'shepplogan', "
+                 "'smooth', 'grains' or '3phases'.");
         const int64_t npix = (int64_t)dat.n * dat.n;
         xref.resize(npix);
-        check(fair_shepplogan(dat.n, xref.data()), "shepplogan");
+        check(fair_phantom(inputphantom.c_str(), dat.n, xref.data()), "choose_phantom");
         int32_t m, n;
         int64_t nnz;
         check(fair_csr_info(A, &m, &n, &nnz), "info");

@@ -102,6 +102,15 @@ static std::mutex g_rng_mu;
 static uint64_t g_seed = 0, g_ctr = 0;
 
 static double rng_next() { return uniform01(g_seed, g_ctr++); }
+
+// `count` consecutive draws of the library stream, for a consumer that
+// evaluates them itself (on the device): the stream's seed and first counter.
+void rng_take(uint64_t count, uint64_t *seed, uint64_t *ctr) {
+    std::lock_guard<std::mutex> lk(g_rng_mu);
+    *seed = g_seed;
+    *ctr = g_ctr;
+    g_ctr += count;
+}
 static uint64_t rng_reserve(uint64_t k) {
     uint64_t c = g_ctr;
     g_ctr += k;

@@ -208,6 +208,8 @@ int sm_count();
 constexpr int kReduceBlocks = 4096;  // partial-sum slots used by reductions (>= any grid)
 
 // ---- project random stream ---------------------------------------------------------
+// Reserve `count` draws of the library stream (fair_host.cu): seed and first counter.
+void rng_take(uint64_t count, uint64_t *seed, uint64_t *ctr);
 __host__ __device__ inline uint64_t splitmix64(uint64_t seed, uint64_t k) {
     uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ULL;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;

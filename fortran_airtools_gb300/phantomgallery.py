@@ -21,6 +21,20 @@ def shepplogan(N: int) -> np.ndarray:
     return v
 
 
+def phantom(name: str, N: int) -> np.ndarray:
+    """choose_phantom (phantomgallery.f90:84-114) evaluated on the GPU:
+    'shepplogan', 'smooth', 'grains' (uniform seeds) or '3phases', the random
+    ones drawing from the library stream in the reference's order."""
+    v = np.empty(N * N, np.float64)
+    check(lib().fair_phantom(name.encode(), int(N), ptr(v)))
+    return v
+
+
+def add_white_noise_device(d_b: int, d_bt: int, d_e: int, m: int, eta: float, stream=None):
+    """add_white_noise (system_generation.f90:709-745) on device vectors."""
+    check(lib().fair_add_white_noise_device(d_bt, d_e, d_b, int(m), float(eta), stream))
+
+
 def vectorise(img: np.ndarray) -> np.ndarray:
     """Column-major vectorisation (phantomgallery.f90:672-690)."""
     return np.asarray(img, np.float64).reshape(-1, order="F").copy()

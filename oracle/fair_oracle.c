@@ -963,6 +963,104 @@ done:
 
 /* shepplogan, phantomgallery.f90:116-164 on the meshgrid of :17-56, returned
  * already vectorised column by column (vectorise, :672-690). */
+/* Max-normalise (x = x/maxval(x)). */
+static void normalise_max(double *v, int64_t n) {
+    double mx = v[0];
+    for (int64_t k = 1; k < n; ++k) if (v[k] > mx) mx = v[k];
+    for (int64_t k = 0; k < n; ++k) v[k] = v[k] / mx;
+}
+
+/* smooth, phantomgallery.f90:166-199 (p = 4). intmeshgrid: xc(i,j) = j+1,
+ * yc(i,j) = i+1. Rows 2-4 of the centres are default-real (single
+ * precision) literals times N, as written in the reference. */
+void or_smooth(int N, double *v) {
+    const double sigma = 0.25 * N;
+    const double c1[4] = {0.6 * N, (double)(0.5f * (float)N), (double)(0.2f * (float)N),
+                          (double)(0.8f * (float)N)};
+    const double c2[4] = {0.6 * N, (double)(0.3f * (float)N), (double)(0.7f * (float)N),
+                          (double)(0.2f * (float)N)};
+    const double a[4] = {1.0, 0.5, 0.7, 0.9};
+    const double sx = 1.2 * sigma, sx2 = sx * sx, sy2 = sigma * sigma;
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            double xc = j + 1, yc = i + 1, acc = 0.0;
+            for (int k = 0; k < 4; ++k) {
+                double dx = xc - c1[k], dy = yc - c2[k];
+                acc = acc + a[k] * exp(-(dx * dx) / sx2 - (dy * dy) / sy2);
+            }
+            v[(int64_t)j * N + i] = acc;
+        }
+    normalise_max(v, (int64_t)N * N);
+}
+
+/* grains, phantomgallery.f90:529-600 ('uniform'): p = int(3 sqrt(N)) seeds
+ * drawn into x0(2,p) in element order, then p values drawn (unused); image =
+ * index of the nearest seed (first on ties), max-normalised. Distances are
+ * sqrt(dx^2 + dy^2) (the reference's norm2 scales). */
+void or_grains(int N, double *v) {
+    const int p = (int)(3 * sqrt(N * 1.0));
+    double *sx = malloc(sizeof(double) * p), *sy = malloc(sizeof(double) * p);
+    for (int k = 0; k < p; ++k) {
+        double ux = or_random_number(), uy = or_random_number();
+        sx[k] = 1.5 * (2.0 * ux - 1.0);
+        sy[k] = 1.5 * (2.0 * uy - 1.0);
+    }
+    for (int k = 0; k < p; ++k) (void)or_random_number();  /* vals */
+    double *lx = malloc(sizeof(double) * N), *ly = malloc(sizeof(double) * N);
+    or_linspace(-1.0, 1.0, N, lx);
+    or_linspace(1.0, -1.0, N, ly);
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            double dmin = 1.7976931348623157e308;
+            int kmin = 0;
+            for (int k = 0; k < p; ++k) {
+                double dx = lx[j] - sx[k], dy = ly[i] - sy[k];
+                double d = sqrt(dx * dx + dy * dy);
+                if (d < dmin) { dmin = d; kmin = k + 1; }
+            }
+            v[(int64_t)j * N + i] = kmin;
+        }
+    normalise_max(v, (int64_t)N * N);
+    free(sx); free(sy); free(lx); free(ly);
+}
+
+/* threephases, phantomgallery.f90:201-254 (p = 100): two sets of p random
+ * centres (c(p,2) filled column by column, times N) on the mesh
+ * linspace(1, N) in both directions; the second sum divides the cubes by a
+ * square, as the reference does (:243). */
+void or_threephases(int N, double *v) {
+    const int p = 100;
+    double *c1x = malloc(sizeof(double) * p), *c1y = malloc(sizeof(double) * p);
+    double *c2x = malloc(sizeof(double) * p), *c2y = malloc(sizeof(double) * p);
+    for (int k = 0; k < p; ++k) c1x[k] = or_random_number() * N;
+    for (int k = 0; k < p; ++k) c1y[k] = or_random_number() * N;
+    for (int k = 0; k < p; ++k) c2x[k] = or_random_number() * N;
+    for (int k = 0; k < p; ++k) c2y[k] = or_random_number() * N;
+    double *lx = malloc(sizeof(double) * N), *ly = malloc(sizeof(double) * N);
+    or_linspace(1.0, (double)N, N, lx);
+    or_linspace(1.0, (double)N, N, ly);
+    const double s1 = 0.025 * N, s2 = 0.025 * N;
+    const double s1c = (2.5 * s1) * (2.5 * s1) * (2.5 * s1), s2s = (2.5 * s2) * (2.5 * s2);
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            double xc = lx[j], yc = ly[i], im1 = 0.0, im2 = 0.0;
+            for (int k = 0; k < p; ++k) {
+                double ax = fabs(xc - c1x[k]), ay = fabs(yc - c1y[k]);
+                im1 = im1 + exp(-(ax * ax * ax) / s1c - (ay * ay * ay) / s1c);
+            }
+            for (int k = 0; k < p; ++k) {
+                double ax = fabs(xc - c2x[k]), ay = fabs(yc - c2y[k]);
+                im2 = im2 + exp(-(ax * ax * ax) / s2s - (ay * ay * ay) / s2s);
+            }
+            im1 = im1 < 0.35 ? 0.0 : 2.0;
+            im2 = im2 < 0.55 ? 0.0 : 1.0;
+            double t = im1 + im2;
+            v[(int64_t)j * N + i] = t == 3.0 ? 1.0 : t;
+        }
+    normalise_max(v, (int64_t)N * N);
+    free(c1x); free(c1y); free(c2x); free(c2y); free(lx); free(ly);
+}
+
 void or_shepplogan(int N, double *v) {
     static const double e[10][6] = {
         {1, .69, .92, 0, 0, 0},          {-.8, .6624, .874, 0, -.0184, 0},

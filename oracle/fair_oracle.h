@@ -98,6 +98,9 @@ int or_twin_art(const char *method, const char *stoprule, const or_csr *A,
 
 /* ---- phantomgallery.f90 ---- */
 void or_shepplogan(int N, double *x_colmajor);
+void or_smooth(int N, double *v);
+void or_grains(int N, double *v);
+void or_threephases(int N, double *v);
 
 #ifdef __cplusplus
 }

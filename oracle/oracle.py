@@ -102,6 +102,8 @@ def _declare(L):
     L.or_twin_art.argtypes = [C.c_char_p, C.c_char_p, P(_CSR), vp, vp, i32, vp, vp, vp,
                               i32, i32, P(_Opts), vp, P(C.c_int), vp, vp, vp]
     L.or_shepplogan.argtypes = [i32, vp]
+    for f in ('or_smooth', 'or_grains', 'or_threephases'):
+        getattr(L, f).argtypes = [i32, vp]
 
 
 def _p(a):
@@ -350,6 +352,17 @@ def twin_art(method, stoprule, A: OracleCSR, b, Kin, x0=None, y0=None, order=Non
                              C.byref(opts) if opts is not None else None, _p(xout),
                              C.byref(fi), _p(Xs), _p(Ys), _p(EG)))
     return xout, fi.value, Xs.T, Ys.T, EG
+
+
+def phantom(name, N):
+    """smooth (phantomgallery.f90:166-199), grains (:529-600), 3phases
+    (:201-254), drawing from the oracle's stream; shepplogan (:116-164)"""
+    if name == "shepplogan":
+        return shepplogan(N)
+    f = {"smooth": "or_smooth", "grains": "or_grains", "3phases": "or_threephases"}[name]
+    v = np.empty(N * N, np.float64)
+    getattr(lib(), f)(N, _p(v))
+    return v
 
 
 def shepplogan(N):

@@ -107,3 +107,21 @@ def test_input_file_mode(oracle, tmp_path):
     sol = np.loadtxt(tmp_path / "sol.txt")
     xr = oracle.sirt("sart", R, -np.log(T), 10, opts=oracle.options(lbound=0.0))
     assert rel_err(sol, xr) < 1e-10
+
+
+def test_random_phantom_test_mode(test_problem, oracle, tmp_path):
+    """-tgrains: the phantom's seeds are drawn before the noise, from the
+    same stream, as choose_phantom precedes add_white_noise (main.f90:213-215)."""
+    R, _, _, seed = test_problem
+    for s in range(seed, seed + 8):
+        oracle.random_seed(s)
+        x = oracle.phantom("grains", 256)
+        try:
+            bt, _ = oracle.add_white_noise(oracle.matvecmul(R, x), 5e-3)
+        except Exception:
+            continue
+        run(["-tgrains", "-K4", "-Mcimmino"], tmp_path, s)
+        sol = np.loadtxt(tmp_path / "sol.txt")
+        assert rel_err(sol, oracle.sirt("cimmino", R, bt, 4)) < 1e-10
+        return
+    pytest.skip("no seed with a converging noise draw")
