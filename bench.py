@@ -59,6 +59,32 @@ def env_rank():
         int(os.environ.get("LOCAL_RANK", 0))
 
 
+def dist_init(world, backend):
+    """One process per GPU (torchrun): the process group for the barrier and the
+    max-over-ranks time; replicas exchange nothing else."""
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world, device):
+    """The slowest rank's value (times are taken as the max over ranks)."""
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def hbm_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -218,15 +244,12 @@ def run_ours(args):
     from fortran_airtools_gb300._clib import check, lib
 
     rank, world, local = env_rank()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist_init(world, "nccl")
     torch.cuda.set_device(local)
     L = lib()
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+        dist_barrier(world)
 
     stream = torch.cuda.Stream()
     th = theta()
@@ -276,11 +299,7 @@ def run_ours(args):
         stream.synchronize()
         torch.cuda.synchronize()
         clocks = sampler.stop() if sampler else None
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device=f"cuda:{local}")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), world, f"cuda:{local}")
         results[prec] = d_x.cpu().numpy()
         # per-pass launch durations (CUDA events around each kernel)
         ms1, ms2 = C.c_float(), C.c_float()
@@ -330,11 +349,7 @@ def run_ours(args):
     barrier()
     t0 = time.perf_counter()
     F.airms.sirt("cimmino", A, bt, args.steps, opts=opts)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, f"cuda:{local}")
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
