@@ -58,6 +58,9 @@ struct MfAngle {
     int tie;             // s = 0: +1 / -1 = sign of d that keeps |d| = 1/2; 0 otherwise
     int by_column;       // 1: walk columns (|sin| >= |cos|)
     double inv_c64, scale_ramp64;
+    // FP32 entries: |d| truncated to 30 fractional bits, thresholds likewise
+    int H1s, H2s, Hcuts;
+    float scale_ramp30;  // 2^-30 / (c s) (0 when s = 0)
 };
 
 // Conversion of 0 <= v < 2^47 to float / 2 (the last bit is below float
@@ -71,16 +74,21 @@ __device__ __forceinline__ float fix_to_float_half(long long v) {
 }
 
 template <typename T> struct Chord;
+// FP32 entries: the exact distance is truncated to 30 fractional bits (far
+// below FP32 precision) and the chord is evaluated in 32-bit integers; both
+// kernels truncate the same exact value, so they still agree bit for bit.
 template <> struct Chord<float> {
     static __device__ __forceinline__ float of(const MfAngle &A, long long d) {
-        const long long u = d < 0 ? -d : d;
-        if (u >= A.Hcut) {
+        const long long ad = d < 0 ? -d : d;
+        if (ad >= (1LL << 47)) return 0.f;  // more than two pixels away
+        const int u = (int)(ad >> 16);
+        if (u >= A.Hcuts) {
             // an axis-aligned ray on the pixel's edge belongs to the positive side
-            if (u == A.H2 && A.tie != 0 && (d > 0 ? 1 : -1) == A.tie) return A.inv_c;
+            if (u == A.H2s && A.tie != 0 && (d > 0 ? 1 : -1) == A.tie) return A.inv_c;
             return 0.f;
         }
-        if (u <= A.H1) return A.inv_c;
-        return fix_to_float_half(A.H2 - u) * A.scale_ramp;
+        if (u <= A.H1s) return A.inv_c;
+        return (float)(A.H2s - u) * A.scale_ramp30;
     }
 };
 template <> struct Chord<double> {
@@ -152,32 +160,45 @@ __global__ void __launch_bounds__(128) k_mf_project(const MfAngle *__restrict__ 
 }
 
 // Sum over the rays through pixel q of a_rq * y_r, for every pixel; MODE 1
-// sums a_rq (y unused).
+// sums a_rq (y unused). A thread takes two vertically adjacent pixels of one
+// image column (iy and iy - 1), which share the per-angle set-up.
+template <typename YT, typename ACC, int MODE>
+__device__ __forceinline__ void bp_rays(const MfAngle &A, long long base, int i, int p,
+                                        const YT *__restrict__ y, ACC &acc) {
+    // rays j with |base - j 2^46| <= H2
+    const long long jlo = -((A.H2 - base) >> kFix), jhi = (base + A.H2) >> kFix;
+    const int j0 = (int)max(jlo, 0LL), j1 = (int)min(jhi, (long long)p - 1);
+    long long d = base - ((long long)j0 << kFix);
+    for (int j = j0; j <= j1; ++j, d -= (1LL << kFix)) {
+        const ACC w = Chord<ACC>::of(A, d);
+        if (w > (ACC)0) {
+            if (MODE == 0) acc += w * (ACC)__ldg(y + (int64_t)i * p + j);
+            else acc += w;
+        }
+    }
+}
+
 template <typename YT, typename ACC, int MODE, class Epi>
 __global__ void __launch_bounds__(128) k_mf_backproject(const MfAngle *__restrict__ ang,
                                                         int nth, int p, int N,
                                                         const YT *__restrict__ y, Epi epi) {
-    const int64_t n = (int64_t)N * N;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int ix = (int)(q / N), iy = N - 1 - (int)(q - (int64_t)ix * N);
-        ACC acc = 0;
+    const int half = (N + 1) / 2;  // pixel pairs per image column
+    const int64_t npairs = (int64_t)N * half;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < npairs;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(t / half), k = (int)(t - (int64_t)ix * half);
+        const int iy0 = N - 1 - 2 * k;     // pixel q0 = ix*N + 2k
+        const bool two = iy0 >= 1;         // and q0 + 1 (iy0 - 1) when it exists
+        ACC acc0 = 0, acc1 = 0;
         for (int i = 0; i < nth; ++i) {
             const MfAngle &A = ang[i];
-            const long long base = (long long)ix * A.C + (long long)iy * A.S + A.K;
-            // rays j with |base - j 2^40| <= H2
-            const long long jlo = -((A.H2 - base) >> kFix), jhi = (base + A.H2) >> kFix;
-            const int j0 = (int)max(jlo, 0LL), j1 = (int)min(jhi, (long long)p - 1);
-            long long d = base - ((long long)j0 << kFix);
-            for (int j = j0; j <= j1; ++j, d -= (1LL << kFix)) {
-                const ACC w = Chord<ACC>::of(A, d);
-                if (w > (ACC)0) {
-                    if (MODE == 0) acc += w * (ACC)__ldg(y + (int64_t)i * p + j);
-                    else acc += w;
-                }
-            }
+            const long long base0 = (long long)ix * A.C + (long long)iy0 * A.S + A.K;
+            bp_rays<YT, ACC, MODE>(A, base0, i, p, y, acc0);
+            if (two) bp_rays<YT, ACC, MODE>(A, base0 - A.S, i, p, y, acc1);
         }
-        epi(q, acc);
+        const int64_t q0 = (int64_t)ix * N + 2 * k;
+        epi(q0, acc0);
+        if (two) epi(q0 + 1, acc1);
     }
 }
 
@@ -221,8 +242,8 @@ int mf_weights(fair_mf A, bool sart, cudaStream_t s) {
         k_mf_project<double, double, 1><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N,
                                                                           nullptr, e1);
         EpiStore<double> e2{A->D.as<double>()};
-        k_mf_backproject<double, double, 1><<<grid_for(n, 128), 128, 0, s>>>(ang, A->nth, A->p,
-                                                                              A->N, nullptr, e2);
+        k_mf_backproject<double, double, 1><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
+            ang, A->nth, A->p, A->N, nullptr, e2);
         FAIR_CUDA(cudaGetLastError());
         A->have_sart = true;
     }
@@ -250,7 +271,7 @@ void mf_pass(fair_mf A, int pass, const double *d_b, double *d_x, cudaStream_t s
                                                                               A->N, d_x, e);
         } else {
             EpiUpdateF64 e{D, d_x, A->omg, A->lb, A->ub, A->bmode};
-            k_mf_backproject<double, double, 0><<<grid_for(n, 128), 128, 0, s>>>(
+            k_mf_backproject<double, double, 0><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
                 ang, A->nth, A->p, A->N, A->r.as<double>(), e);
         }
     } else {
@@ -260,7 +281,7 @@ void mf_pass(fair_mf A, int pass, const double *d_b, double *d_x, cudaStream_t s
                                                                             A->x32.as<float>(), e);
         } else {
             EpiUpdateLP e{D, d_x, A->x32.as<float>(), A->omg, A->lb, A->ub, A->bmode, 1.0};
-            k_mf_backproject<float, float, 0><<<grid_for(n, 128), 128, 0, s>>>(
+            k_mf_backproject<float, float, 0><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
                 ang, A->nth, A->p, A->N, A->r.as<float>(), e);
         }
     }
@@ -338,6 +359,11 @@ int fair_mf_create_parallel(fair_mf *out, const fair_data *dat, int32_t prec) {
         // segments of 1e-10 or less are dropped, as the ray tracer does
         // (system_generation.f90:393-394)
         a.Hcut = a.tie != 0 ? a.H2 : a.H2 - (long long)floor(1e-10 * c * s * fair::kOne);
+        a.H1s = (int)(a.H1 >> 16);
+        a.H2s = (int)(a.H2 >> 16);
+        a.Hcuts = (int)(a.Hcut >> 16);
+        if (a.tie == 0 && a.Hcuts >= a.H2s) a.Hcuts = a.H2s;  // s > 0: the ramp ends at H2s
+        a.scale_ramp30 = s > 0 ? (float)(1.0 / (1073741824.0 * c * s)) : 0.f;
     }
     if (A->ang.grow(sizeof(fair::MfAngle) * nth) != FAIR_OK ||
         cudaMemcpy(A->ang.p, t.data(), sizeof(fair::MfAngle) * nth, cudaMemcpyHostToDevice) !=
@@ -397,7 +423,7 @@ static int mf_apply(fair_mf A, bool back, const double *in, double *out) {
     if (A->prec == FAIR_PREC_F64) {
         fair::EpiStore<double> e{A->w_out.as<double>()};
         if (back)
-            fair::k_mf_backproject<double, double, 0><<<fair::grid_for(n, 128), 128, 0, s>>>(
+            fair::k_mf_backproject<double, double, 0><<<fair::grid_for(n / 2 + 1, 128), 128, 0, s>>>(
                 ang, A->nth, A->p, A->N, A->w_in.as<double>(), e);
         else
             fair::k_mf_project<double, double, 0><<<fair::grid_for(m, 128), 128, 0, s>>>(
@@ -409,7 +435,7 @@ static int mf_apply(fair_mf A, bool back, const double *in, double *out) {
         FAIR_TRY(fair::vec_to_f32(A->w_in.as<double>(), nin, A->v_a.as<float>(), s));
         fair::EpiStore<float> e{A->v_b.as<float>()};
         if (back)
-            fair::k_mf_backproject<float, float, 0><<<fair::grid_for(n, 128), 128, 0, s>>>(
+            fair::k_mf_backproject<float, float, 0><<<fair::grid_for(n / 2 + 1, 128), 128, 0, s>>>(
                 ang, A->nth, A->p, A->N, A->v_a.as<float>(), e);
         else
             fair::k_mf_project<float, float, 0><<<fair::grid_for(m, 128), 128, 0, s>>>(
