@@ -149,7 +149,7 @@ def algorithmic_bytes(nnz, m, n, prec, packed=None):
     sx = 8 if prec == "f64" else 4
 
     def matrix(info):
-        if info is None or prec == "f64" or not info["has"]:
+        if info is None or not info["has"]:
             return nnz * (sv + 4)
         return info["ngroups"] * (8 + 4 * sv) + info["nesc"] * 16
 
@@ -275,7 +275,7 @@ def run_ours(args):
     for prec in form_list:
         A.set_precision(prec)
         check(L.fair_sirt_prepare(h, b"cimmino", C.byref(opts)))
-        cfg = (C.c_int32 * 4)(8, 8, 1, 1)
+        cfg = (C.c_int32 * 4)(8, 8, *((0, 0) if prec == "f64" else (1, 1)))  # library defaults
         if args.lanes:  # fixed lanes per row (and groups per lane) of the two passes
             v = [int(t) for t in args.lanes.split(",")]
             cfg[:] = (v + [1, 1])[:4] if len(v) == 2 else v[:4]
@@ -316,11 +316,13 @@ def run_ours(args):
                        "launches": launches.value, "clocks": clocks,
                        "pass_config": None if args.no_tune and not args.lanes else
                        {"lanes_per_row": [cfg[0], cfg[1]], "groups_per_lane": [cfg[2], cfg[3]]}}
-        if prec != "f64":
-            pk = (A.packed_info(), A.packed_info(transposed=True))
-            if pk[0]["has"] or pk[1]["has"]:
-                packed[prec] = pk
-                forms[prec]["packed_index"] = {"A": pk[0], "AT": pk[1]}
+        # the passes that read the packed stream (groups per lane > 0)
+        pk = (A.packed_info(), A.packed_info(transposed=True))
+        use = [pk[i]["has"] and cfg[2 + i] > 0 for i in (0, 1)]
+        if any(use):
+            packed[prec] = tuple(pk[i] if use[i] else None for i in (0, 1))
+            forms[prec]["packed_index"] = {"A": pk[0] if use[0] else None,
+                                           "AT": pk[1] if use[1] else None}
     for prec in form_list[1:]:
         r = results["f64"]
         forms[prec]["rel_err_vs_f64"] = float(np.linalg.norm(results[prec] - r) / np.linalg.norm(r))
@@ -331,7 +333,8 @@ def run_ours(args):
     b1, b2 = algorithmic_bytes(nnz, m, n, hp, packed.get(hp))
     dom = 2 if head["pass2_ms"] >= head["pass1_ms"] else 1
     pk = packed.get(hp)
-    kind = "_f64" if hp == "f64" else ("_pk" if pk and pk[dom - 1]["has"] else "_lp")
+    on_pk = bool(pk and pk[dom - 1])
+    kind = ("_pk64" if on_pk else "_f64") if hp == "f64" else ("_pk" if on_pk else "_lp")
     kname = {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kind
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256) k_batch_pk(const BPass *__restrict__ P,
         const int p = owner(chunk0, np, ch);
         const BPass &d = P[p];
         const int64_t base = (ch - __ldg(chunk0 + p)) << 5;
-        const float mine = pk_chunk_sums<VT, float, G, NG>(
+        const float mine = pk_chunk_sums<VT, float, float, G, NG>(
             d.ptr, d.rows, (const uint2 *)d.idx, d.gside, d.S, d.L, (const VT *)d.val,
             (const float *)d.xin, base);
         const int64_t row = base + lane;
@@ -349,10 +349,13 @@ void compact(DevCSR &M, int prec) {
     M.has32 = M.has16 = M.hasq = false;
     if (prec == FAIR_PREC_F64) {
         M.prow.release(); M.gidx.release(); M.gside.release();
-        M.pv32.release(); M.pv16.release(); M.pvq.release();
-        M.haspk = M.hasp32 = M.hasp16 = M.haspq = false;
+        M.pv64.release(); M.pv32.release(); M.pv16.release(); M.pvq.release();
+        M.pf16.release(); M.pfq.release();
+        M.haspk = M.hasp64 = M.hasp32 = M.hasp16 = M.haspq = M.hasf16 = M.hasfq = false;
     } else {
         M.rowptr.release(); M.col.release(); M.v64.release();
+        M.pv64.release(); M.pf16.release(); M.pfq.release();
+        M.hasp64 = M.hasf16 = M.hasfq = false;
         if (prec != FAIR_PREC_F32) { M.pv32.release(); M.hasp32 = false; }
         if (prec != FAIR_PREC_F16) { M.pv16.release(); M.hasp16 = false; }
         if (prec != FAIR_PREC_Q16) { M.pvq.release(); M.haspq = false; }

@@ -59,10 +59,13 @@ void DevBuf::release() {
 void DevCSR::release() {
     rowptr.release(); col.release(); v64.release(); v32.release(); v16.release(); vq.release();
     has32 = has16 = hasq = false;
-    prow.release(); gidx.release(); gside.release(); pv32.release(); pv16.release(); pvq.release();
-    pk_tried = haspk = hasp32 = hasp16 = haspq = false;
+    prow.release(); gidx.release(); gside.release();
+    pv64.release(); pv32.release(); pv16.release(); pvq.release();
+    pf16.release(); pfq.release();
+    pk_tried = haspk = hasp64 = hasp32 = hasp16 = haspq = hasf16 = hasfq = false;
     for (int &g : sirt_lanes) g = 8;
     for (int &g : sirt_groups) g = 1;
+    sirt_groups[FAIR_PREC_F64] = 0;
     ngroups = nesc = 0;
     stride_hint = tstride_hint = 0;
     m = n = 0;
@@ -1177,10 +1180,10 @@ int fair_sirt_set_lanes(fair_csr h, const int32_t *config) {
     NEED_MATRIX(h);
     if (!config) return FAIR_ERR_NULL;
     auto lanes_ok = [](int32_t g) { return g == 4 || g == 8 || g == 16 || g == 32; };
-    auto groups_ok = [](int32_t g) { return g == 1 || g == 2; };
+    auto groups_ok = [](int32_t g) { return g >= 0 && g <= 4; };
     if (!lanes_ok(config[0]) || !lanes_ok(config[1]) || !groups_ok(config[2]) ||
         !groups_ok(config[3])) {
-        set_detail("lanes per row must be 4, 8, 16 or 32 and groups per lane 1 or 2");
+        set_detail("lanes per row must be 4, 8, 16 or 32 and the layout code 0-4");
         return FAIR_ERR_ARG;
     }
     FAIR_TRY(ensure_transpose(h));

@@ -52,7 +52,9 @@ struct DevCSR {
     int32_t max_row = 0;        // longest row (nonzeros)
     int lanes_per_row = 8;      // G of the row engine (4, 8, 16 or 32)
     int sirt_lanes[4] = {8, 8, 8, 8};  // G of the SIRT passes per form (autotuned)
-    int sirt_groups[4] = {1, 1, 1, 1}; // packed groups per lane and step (1 or 2)
+    // layout of the SIRT passes per form: 0 the CSR; 1, 2 the packed stream with
+    // that many groups per lane and step; 3, 4 the fused records (2-byte forms)
+    int sirt_groups[4] = {0, 1, 1, 1};
     // allocate col and v64 for nnz entries plus the pad (pad zeroed)
     int alloc_entries(int64_t nnz_, cudaStream_t s);
     DevBuf rowptr;        // int64 [m+1]
@@ -75,8 +77,10 @@ struct DevCSR {
     DevBuf prow;               // int64 [m+1] group offsets
     DevBuf gidx;               // uint2 [ngroups]
     DevBuf gside;              // int4 [nesc] columns of groups without a step code
-    DevBuf pv32, pv16, pvq;    // padded float / half / 16-bit fixed-point values
-    bool hasp32 = false, hasp16 = false, haspq = false;
+    DevBuf pv64, pv32, pv16, pvq;  // padded double / float / half / 16-bit values
+    bool hasp64 = false, hasp32 = false, hasp16 = false, haspq = false;
+    DevBuf pf16, pfq;          // fused 16-byte records {index word, 4 values} (2-byte forms)
+    bool hasf16 = false, hasfq = false;
     void release();
     bool empty() const { return rowptr.p == nullptr; }
 };
@@ -108,8 +112,10 @@ int csr_make_lowprec(DevCSR &A, int prec, cudaStream_t s);
 // FAIR_PACKED=0 to disable.
 int csr_make_packed(DevCSR &A, int prec, cudaStream_t s);
 bool packed_enabled();
+// Fused 16-byte records of the packed stream for a 2-byte form (f16, q16).
+int csr_make_fused(DevCSR &A, int prec, cudaStream_t s);
 // Reduced-precision copies (and packed streams) of A and A' for SIRT (solvers.cu).
-int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s);
+int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool pack_f64 = false);
 int csr_scale(DevCSR &A, double c, cudaStream_t s);
 int csr_row_norms(const DevCSR &A, int p, double *d_out, cudaStream_t s);
 int csr_row_dot(const DevCSR &A, int32_t row, const double *d_x, double *d_out, cudaStream_t s);

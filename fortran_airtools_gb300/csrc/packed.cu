@@ -128,6 +128,15 @@ __global__ void k_pk_values(const int64_t *rowptr, int32_t m, const int64_t *pro
     }
 }
 
+// Fused records of a 2-byte form: {index word, the group's four values}.
+__global__ void k_pk_fuse(const uint2 *gidx, const uint2 *vals, int64_t ng, uint4 *rec) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < ng;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const uint2 w = gidx[j], v = vals[j];
+        rec[j] = make_uint4(w.x, w.y, v.x, v.y);
+    }
+}
+
 int64_t isqrt64(int64_t v) {
     int64_t r = (int64_t)std::sqrt((double)v);
     while (r * r > v) --r;
@@ -216,12 +225,19 @@ bool packed_enabled() {
 }
 
 int csr_make_packed(DevCSR &A, int prec, cudaStream_t s) {
-    if (prec == FAIR_PREC_F64 || A.m == 0 || A.nnz == 0) return FAIR_OK;
+    if (A.m == 0 || A.nnz == 0) return FAIR_OK;
     if (!A.pk_tried) {
         A.pk_tried = true;
         FAIR_TRY(build_index(A, s));
     }
     if (!A.haspk) return FAIR_OK;
+    if (prec == FAIR_PREC_F64) {
+        if (!A.hasp64) {
+            FAIR_TRY(pad_values<double>(A, A.v64, A.pv64, s));
+            A.hasp64 = true;
+        }
+        return FAIR_OK;
+    }
     FAIR_TRY(csr_make_lowprec(A, prec, s));
     if (prec == FAIR_PREC_F32 && !A.hasp32) {
         FAIR_TRY(pad_values<float>(A, A.v32, A.pv32, s));
@@ -233,6 +249,21 @@ int csr_make_packed(DevCSR &A, int prec, cudaStream_t s) {
         FAIR_TRY(pad_values<uint16_t>(A, A.vq, A.pvq, s));
         A.haspq = true;
     }
+    return FAIR_OK;
+}
+
+int csr_make_fused(DevCSR &A, int prec, cudaStream_t s) {
+    if (!A.haspk || (prec != FAIR_PREC_F16 && prec != FAIR_PREC_Q16)) return FAIR_OK;
+    const bool h = prec == FAIR_PREC_F16;
+    if (h ? A.hasf16 : A.hasfq) return FAIR_OK;
+    FAIR_TRY(csr_make_packed(A, prec, s));
+    DevBuf &dst = h ? A.pf16 : A.pfq;
+    const DevBuf &src = h ? A.pv16 : A.pvq;
+    FAIR_TRY(dst.grow(sizeof(uint4) * (size_t)std::max<int64_t>(A.ngroups, 1)));
+    k_pk_fuse<<<pk_grid(A.ngroups), 256, 0, s>>>(A.gidx.as<uint2>(), src.as<uint2>(), A.ngroups,
+                                                 dst.as<uint4>());
+    FAIR_CUDA(cudaGetLastError());
+    (h ? A.hasf16 : A.hasfq) = true;
     return FAIR_OK;
 }
 

@@ -81,22 +81,41 @@ __device__ __forceinline__ float u16_lo(uint32_t w, float bias) {
 __device__ __forceinline__ float u16_hi(uint32_t w, float bias) {
     return __int_as_float((int)__byte_perm(w, 0x4B00u, 0x5432u)) - bias;
 }
+// Four 2-byte values held in two 32-bit words, to floats.
+template <typename VT> struct Conv2B;
+template <> struct Conv2B<uint16_t> {
+    static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
+        constexpr float b = 8388608.0f;  // 2^23
+        o[0] = u16_lo(a, b); o[1] = u16_hi(a, b);
+        o[2] = u16_lo(b2, b); o[3] = u16_hi(b2, b);
+    }
+};
+template <> struct Conv2B<int16_t> {
+    static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
+        constexpr float b = 8421376.0f;  // 2^23 + 2^15
+        a ^= 0x80008000u;
+        b2 ^= 0x80008000u;
+        o[0] = u16_lo(a, b); o[1] = u16_hi(a, b);
+        o[2] = u16_lo(b2, b); o[3] = u16_hi(b2, b);
+    }
+};
+template <> struct Conv2B<__half> {
+    static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
+        __half2 ha = *reinterpret_cast<__half2 *>(&a), hb = *reinterpret_cast<__half2 *>(&b2);
+        float2 fa = __half22float2(ha), fb = __half22float2(hb);
+        o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
+    }
+};
 template <> struct VLoad<uint16_t, float> {
     static __device__ __forceinline__ void ld(const uint16_t *p, float (&o)[4]) {
-        constexpr float b = 8388608.0f;  // 2^23
         uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
-        o[0] = u16_lo(t.x, b); o[1] = u16_hi(t.x, b);
-        o[2] = u16_lo(t.y, b); o[3] = u16_hi(t.y, b);
+        Conv2B<uint16_t>::to(t.x, t.y, o);
     }
 };
 template <> struct VLoad<int16_t, float> {
     static __device__ __forceinline__ void ld(const int16_t *p, float (&o)[4]) {
-        constexpr float b = 8421376.0f;  // 2^23 + 2^15
         uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
-        t.x ^= 0x80008000u;
-        t.y ^= 0x80008000u;
-        o[0] = u16_lo(t.x, b); o[1] = u16_hi(t.x, b);
-        o[2] = u16_lo(t.y, b); o[3] = u16_hi(t.y, b);
+        Conv2B<int16_t>::to(t.x, t.y, o);
     }
 };
 
@@ -226,15 +245,35 @@ __device__ __forceinline__ void pk_decode(uint2 w, const int4 *__restrict__ gsid
     }
 }
 
+// Group loaders of the packed stream: the index word and the four values of
+// group j. SplitLoad reads them from the index array and the padded value
+// array (two loads); FusedLoad reads the 16-byte record {index word, four
+// 2-byte values} of the fused layout (one load).
+template <typename VT, typename ACC> struct SplitLoad {
+    const uint2 *gidx;
+    const VT *val;
+    __device__ __forceinline__ void ld(int64_t j, uint2 &w, ACC (&v)[4]) const {
+        w = __ldcs(gidx + j);
+        VLoad<VT, ACC>::ld(val + 4 * j, v);
+    }
+};
+template <typename VT> struct FusedLoad {
+    const uint4 *rec;
+    __device__ __forceinline__ void ld(int64_t j, uint2 &w, float (&v)[4]) const {
+        const uint4 r = __ldcs(rec + j);
+        w = make_uint2(r.x, r.y);
+        Conv2B<VT>::to(r.z, r.w, v);
+    }
+};
+
 // Row sums of one chunk over the packed index stream: every lane takes NG
-// groups (4*NG entries) per step, each one 8-byte index word and one vector
-// load of values, and issues the 4*NG gathers of a step together.
-template <typename VT, typename ACC, int G, int NG>
-__device__ __forceinline__ ACC pk_chunk_sums(const int64_t *__restrict__ prow, int32_t m,
-                                             const uint2 *__restrict__ gidx,
-                                             const int4 *__restrict__ gside, int S, int L,
-                                             const VT *__restrict__ val,
-                                             const float *__restrict__ x, int64_t base) {
+// groups (4*NG entries) per step through the loader and issues the 4*NG
+// gathers of a step together.
+template <typename XT, typename ACC, int G, int NG, class LD>
+__device__ __forceinline__ ACC pk_chunk_sums_ld(const int64_t *__restrict__ prow, int32_t m,
+                                                const LD &ldr, const int4 *__restrict__ gside,
+                                                int S, int L, const XT *__restrict__ x,
+                                                int64_t base) {
     constexpr int R = 32 / G;
     const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
     ACC mine = 0;
@@ -247,8 +286,6 @@ __device__ __forceinline__ ACC pk_chunk_sums(const int64_t *__restrict__ prow, i
             g0 = __ldg(prow + row);
             ng = (int)(__ldg(prow + row + 1) - g0);
         }
-        const uint2 *wp = gidx + g0;
-        const VT *vp = val + 4 * g0;
         ACC acc = 0;
         uint2 w[NG];
         ACC vv[NG][4];
@@ -257,10 +294,7 @@ __device__ __forceinline__ ACC pk_chunk_sums(const int64_t *__restrict__ prow, i
             const int j = gl + q * G;
             w[q] = make_uint2(0u, 0u);
             vv[q][0] = vv[q][1] = vv[q][2] = vv[q][3] = 0;
-            if (j < ng) {
-                w[q] = __ldcs(wp + j);
-                VLoad<VT, ACC>::ld(vp + 4 * j, vv[q]);
-            }
+            if (j < ng) ldr.ld(g0 + j, w[q], vv[q]);
         }
         for (int j = gl; j < ng; j += NG * G) {
             const int jn = j + NG * G;
@@ -270,10 +304,7 @@ __device__ __forceinline__ ACC pk_chunk_sums(const int64_t *__restrict__ prow, i
             for (int q = 0; q < NG; ++q) {
                 wn[q] = make_uint2(0u, 0u);
                 vn[q][0] = vn[q][1] = vn[q][2] = vn[q][3] = 0;
-                if (jn + q * G < ng) {
-                    wn[q] = __ldcs(wp + jn + q * G);
-                    VLoad<VT, ACC>::ld(vp + 4 * (jn + q * G), vn[q]);
-                }
+                if (jn + q * G < ng) ldr.ld(g0 + jn + q * G, wn[q], vn[q]);
             }
             int c[NG][4];
             ACC xv[NG][4];
@@ -305,13 +336,46 @@ __device__ __forceinline__ ACC pk_chunk_sums(const int64_t *__restrict__ prow, i
     return mine;
 }
 
+// The split layout (index array + padded values).
+template <typename VT, typename XT, typename ACC, int G, int NG>
+__device__ __forceinline__ ACC pk_chunk_sums(const int64_t *__restrict__ prow, int32_t m,
+                                             const uint2 *__restrict__ gidx,
+                                             const int4 *__restrict__ gside, int S, int L,
+                                             const VT *__restrict__ val,
+                                             const XT *__restrict__ x, int64_t base) {
+    const SplitLoad<VT, ACC> ldr{gidx, val};
+    return pk_chunk_sums_ld<XT, ACC, G, NG>(prow, m, ldr, gside, S, L, x, base);
+}
+
+// chunk_rows over the fused 16-byte records (2-byte values).
+template <typename VT, int G, int NG, class Epi>
+__device__ __forceinline__ void chunk_rows_pkf(const int64_t *__restrict__ prow, int32_t m,
+                                               const uint4 *__restrict__ rec,
+                                               const int4 *__restrict__ gside, int S, int L,
+                                               const float *__restrict__ x, Epi &epi,
+                                               unsigned *sched) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nchunks = ((int64_t)m + 31) >> 5;
+    const FusedLoad<VT> ldr{rec};
+    for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
+         ch = next_chunk(sched, ch, nwarps, lane)) {
+        const int64_t base = ch << 5;
+        const float mine = pk_chunk_sums_ld<float, float, G, NG>(prow, m, ldr, gside, S, L, x, base);
+        const int64_t row = base + lane;
+        if (row < m) epi(row, mine);
+    }
+    finish_chunks(sched, nwarps, lane);
+}
+
 // chunk_rows over the packed index stream.
-template <typename VT, typename ACC, int G, int NG, class Epi>
+template <typename VT, typename XT, typename ACC, int G, int NG, class Epi>
 __device__ __forceinline__ void chunk_rows_pk(const int64_t *__restrict__ prow, int32_t m,
                                               const uint2 *__restrict__ gidx,
                                               const int4 *__restrict__ gside, int S, int L,
                                               const VT *__restrict__ val,
-                                              const float *__restrict__ x, Epi &epi,
+                                              const XT *__restrict__ x, Epi &epi,
                                               unsigned *sched) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -320,7 +384,7 @@ __device__ __forceinline__ void chunk_rows_pk(const int64_t *__restrict__ prow, 
     for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
          ch = next_chunk(sched, ch, nwarps, lane)) {
         const int64_t base = ch << 5;
-        const ACC mine = pk_chunk_sums<VT, ACC, G, NG>(prow, m, gidx, gside, S, L, val, x, base);
+        const ACC mine = pk_chunk_sums<VT, XT, ACC, G, NG>(prow, m, gidx, gside, S, L, val, x, base);
         const int64_t row = base + lane;
         if (row < m) epi(row, mine);
     }

@@ -97,13 +97,39 @@ template <typename VT, int G, int NG>
 __global__ void __launch_bounds__(256) k_sirt_resid_pk(PkArgs P, int32_t m, const VT *v,
                                                        const float *x, EpiResidLP epi,
                                                        unsigned *sched) {
-    chunk_rows_pk<VT, float, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, x, epi, sched);
+    chunk_rows_pk<VT, float, float, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, x, epi, sched);
 }
 template <typename VT, int G, int NG>
 __global__ void __launch_bounds__(256) k_sirt_update_pk(PkArgs P, int32_t m, const VT *v,
                                                         const float *r, EpiUpdateLP epi,
                                                         unsigned *sched) {
-    chunk_rows_pk<VT, float, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, r, epi, sched);
+    chunk_rows_pk<VT, float, float, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, r, epi, sched);
+}
+template <typename VT, int G, int NG>
+__global__ void __launch_bounds__(256) k_sirt_resid_pkf(PkArgs P, int32_t m, const uint4 *rec,
+                                                        const float *x, EpiResidLP epi,
+                                                        unsigned *sched) {
+    chunk_rows_pkf<VT, G, NG>(P.prow, m, rec, P.gside, P.S, P.L, x, epi, sched);
+}
+template <typename VT, int G, int NG>
+__global__ void __launch_bounds__(256) k_sirt_update_pkf(PkArgs P, int32_t m, const uint4 *rec,
+                                                         const float *r, EpiUpdateLP epi,
+                                                         unsigned *sched) {
+    chunk_rows_pkf<VT, G, NG>(P.prow, m, rec, P.gside, P.S, P.L, r, epi, sched);
+}
+template <int G, int NG>
+__global__ void __launch_bounds__(256) k_sirt_resid_pk64(PkArgs P, int32_t m, const double *v,
+                                                         const double *x, EpiResidF64 epi,
+                                                         unsigned *sched) {
+    chunk_rows_pk<double, double, double, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, x, epi,
+                                                 sched);
+}
+template <int G, int NG>
+__global__ void __launch_bounds__(256) k_sirt_update_pk64(PkArgs P, int32_t m, const double *v,
+                                                          const double *r, EpiUpdateF64 epi,
+                                                          unsigned *sched) {
+    chunk_rows_pk<double, double, double, G, NG>(P.prow, m, P.gidx, P.gside, P.S, P.L, v, r, epi,
+                                                 sched);
 }
 template <int G>
 __global__ void __launch_bounds__(256) k_sirt_update_f64(const int64_t *rowptr, int32_t m,
@@ -311,42 +337,59 @@ int sirt_prepare_shadow(const SirtDev &S, cudaStream_t s) {
     return FAIR_OK;
 }
 
-// One reduced-precision pass; `pvals` (padded values) selects the packed
-// index stream when the matrix has one.
+// One reduced-precision pass on the layout `code` selects (0 the CSR; 1, 2
+// the packed stream with that many groups per lane; 3, 4 the fused records),
+// falling back to the layouts that exist: `pvals` (padded values) and
+// `fused` may be null.
 template <typename VT>
 static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
-                    const VT *pvals, double scale, cudaStream_t s) {
+                    const VT *pvals, const uint4 *fused, double scale, int code,
+                    cudaStream_t s) {
     const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
-    const int G = M.sirt_lanes[S.prec], NG = M.sirt_groups[S.prec];
+    const int G = M.sirt_lanes[S.prec];
+    if (code >= 3 && (!fused || sizeof(VT) != 2)) code -= 2;
+    if (code >= 1 && !pvals) code = 0;
     if (pass == 1) {
         EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
-        if (pvals && NG == 2)
-            FAIR_G_DISPATCH(G,
-                            (k_sirt_resid_pk<VT, g_, 2><<<chunk_grid(k_sirt_resid_pk<VT, g_, 2>, M.m), 256, 0, s>>>(
-                                P, M.m, pvals, S.x32, e, S.sched)))
-        else if (pvals)
-            FAIR_G_DISPATCH(G,
-                            (k_sirt_resid_pk<VT, g_, 1><<<chunk_grid(k_sirt_resid_pk<VT, g_, 1>, M.m), 256, 0, s>>>(
-                                P, M.m, pvals, S.x32, e, S.sched)))
-        else
-            FAIR_G_DISPATCH(G,
-                            (k_sirt_resid_lp<VT, g_><<<chunk_grid(k_sirt_resid_lp<VT, g_>, M.m), 256, 0, s>>>(
-                                M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals, S.x32, e, S.sched)))
+        switch (code) {
+            case 4:
+                if constexpr (sizeof(VT) == 2)
+                    FAIR_G_DISPATCH(G, (k_sirt_resid_pkf<VT, g_, 2><<<chunk_grid(k_sirt_resid_pkf<VT, g_, 2>, M.m), 256, 0, s>>>(
+                                           P, M.m, fused, S.x32, e, S.sched)))
+                break;
+            case 3:
+                if constexpr (sizeof(VT) == 2)
+                    FAIR_G_DISPATCH(G, (k_sirt_resid_pkf<VT, g_, 1><<<chunk_grid(k_sirt_resid_pkf<VT, g_, 1>, M.m), 256, 0, s>>>(
+                                           P, M.m, fused, S.x32, e, S.sched)))
+                break;
+            case 2: FAIR_G_DISPATCH(G, (k_sirt_resid_pk<VT, g_, 2><<<chunk_grid(k_sirt_resid_pk<VT, g_, 2>, M.m), 256, 0, s>>>(
+                                           P, M.m, pvals, S.x32, e, S.sched))) break;
+            case 1: FAIR_G_DISPATCH(G, (k_sirt_resid_pk<VT, g_, 1><<<chunk_grid(k_sirt_resid_pk<VT, g_, 1>, M.m), 256, 0, s>>>(
+                                           P, M.m, pvals, S.x32, e, S.sched))) break;
+            default: FAIR_G_DISPATCH(G, (k_sirt_resid_lp<VT, g_><<<chunk_grid(k_sirt_resid_lp<VT, g_>, M.m), 256, 0, s>>>(
+                                            M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals, S.x32, e, S.sched))) break;
+        }
     } else {
         EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale};
-        if (pvals && NG == 2)
-            FAIR_G_DISPATCH(G,
-                            (k_sirt_update_pk<VT, g_, 2><<<chunk_grid(k_sirt_update_pk<VT, g_, 2>, M.m), 256, 0, s>>>(
-                                P, M.m, pvals, (const float *)S.r, e, S.sched)))
-        else if (pvals)
-            FAIR_G_DISPATCH(G,
-                            (k_sirt_update_pk<VT, g_, 1><<<chunk_grid(k_sirt_update_pk<VT, g_, 1>, M.m), 256, 0, s>>>(
-                                P, M.m, pvals, (const float *)S.r, e, S.sched)))
-        else
-            FAIR_G_DISPATCH(G,
-                            (k_sirt_update_lp<VT, g_><<<chunk_grid(k_sirt_update_lp<VT, g_>, M.m), 256, 0, s>>>(
-                                M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals,
-                                (const float *)S.r, e, S.sched)))
+        const float *r = (const float *)S.r;
+        switch (code) {
+            case 4:
+                if constexpr (sizeof(VT) == 2)
+                    FAIR_G_DISPATCH(G, (k_sirt_update_pkf<VT, g_, 2><<<chunk_grid(k_sirt_update_pkf<VT, g_, 2>, M.m), 256, 0, s>>>(
+                                           P, M.m, fused, r, e, S.sched)))
+                break;
+            case 3:
+                if constexpr (sizeof(VT) == 2)
+                    FAIR_G_DISPATCH(G, (k_sirt_update_pkf<VT, g_, 1><<<chunk_grid(k_sirt_update_pkf<VT, g_, 1>, M.m), 256, 0, s>>>(
+                                           P, M.m, fused, r, e, S.sched)))
+                break;
+            case 2: FAIR_G_DISPATCH(G, (k_sirt_update_pk<VT, g_, 2><<<chunk_grid(k_sirt_update_pk<VT, g_, 2>, M.m), 256, 0, s>>>(
+                                           P, M.m, pvals, r, e, S.sched))) break;
+            case 1: FAIR_G_DISPATCH(G, (k_sirt_update_pk<VT, g_, 1><<<chunk_grid(k_sirt_update_pk<VT, g_, 1>, M.m), 256, 0, s>>>(
+                                           P, M.m, pvals, r, e, S.sched))) break;
+            default: FAIR_G_DISPATCH(G, (k_sirt_update_lp<VT, g_><<<chunk_grid(k_sirt_update_lp<VT, g_>, M.m), 256, 0, s>>>(
+                                            M.rowptr.as<int64_t>(), M.m, M.col.as<int32_t>(), vals, r, e, S.sched))) break;
+        }
     }
 }
 
@@ -355,7 +398,30 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
     const DevCSR &M = pass == 1 ? *S.A : *S.AT;
     if (M.m == 0) return;
     if (S.prec == FAIR_PREC_F64) {
-        const int G = M.sirt_lanes[FAIR_PREC_F64];
+        const int G = M.sirt_lanes[FAIR_PREC_F64], NG = M.sirt_groups[FAIR_PREC_F64];
+        if (NG > 0 && M.haspk && M.hasp64 && packed_enabled()) {
+            const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S,
+                           M.pk_L};
+            const double *pv = M.pv64.as<double>();
+            if (pass == 1) {
+                EpiResidF64 e{S.b, S.Minv, (double *)S.r};
+                if (NG == 2)
+                    FAIR_G_DISPATCH(G, (k_sirt_resid_pk64<g_, 2><<<chunk_grid(k_sirt_resid_pk64<g_, 2>, M.m), 256, 0, s>>>(
+                                           P, M.m, pv, S.x, e, S.sched)))
+                else
+                    FAIR_G_DISPATCH(G, (k_sirt_resid_pk64<g_, 1><<<chunk_grid(k_sirt_resid_pk64<g_, 1>, M.m), 256, 0, s>>>(
+                                           P, M.m, pv, S.x, e, S.sched)))
+            } else {
+                EpiUpdateF64 e{S.D, S.x, S.omg, S.lb, S.ub, S.bmode};
+                if (NG == 2)
+                    FAIR_G_DISPATCH(G, (k_sirt_update_pk64<g_, 2><<<chunk_grid(k_sirt_update_pk64<g_, 2>, M.m), 256, 0, s>>>(
+                                           P, M.m, pv, (const double *)S.r, e, S.sched)))
+                else
+                    FAIR_G_DISPATCH(G, (k_sirt_update_pk64<g_, 1><<<chunk_grid(k_sirt_update_pk64<g_, 1>, M.m), 256, 0, s>>>(
+                                           P, M.m, pv, (const double *)S.r, e, S.sched)))
+            }
+            return;
+        }
         const int64_t *rp = M.rowptr.as<int64_t>();
         const int32_t *cl = M.col.as<int32_t>();
         if (pass == 1) {
@@ -370,29 +436,40 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
         return;
     }
     const bool pk = M.haspk && packed_enabled();
+    const int code = M.sirt_groups[S.prec];
+    const uint4 *f16 = pk && M.hasf16 ? M.pf16.as<uint4>() : nullptr;
+    const uint4 *fq = pk && M.hasfq ? M.pfq.as<uint4>() : nullptr;
     if (S.prec == FAIR_PREC_F32) {
-        lp_pass(S, M, pass, M.v32.as<float>(), pk && M.hasp32 ? M.pv32.as<float>() : nullptr, 1.0, s);
+        lp_pass(S, M, pass, M.v32.as<float>(), pk && M.hasp32 ? M.pv32.as<float>() : nullptr,
+                nullptr, 1.0, code, s);
     } else if (S.prec == FAIR_PREC_F16) {
         lp_pass(S, M, pass, M.v16.as<__half>(), pk && M.hasp16 ? M.pv16.as<__half>() : nullptr,
-                1.0, s);
+                f16, 1.0, code, s);
     } else if (M.qsigned) {
         lp_pass(S, M, pass, M.vq.as<int16_t>(), pk && M.haspq ? M.pvq.as<int16_t>() : nullptr,
-                M.qscale, s);
+                fq, M.qscale, code, s);
     } else {
         lp_pass(S, M, pass, M.vq.as<uint16_t>(), pk && M.haspq ? M.pvq.as<uint16_t>() : nullptr,
-                M.qscale, s);
+                fq, M.qscale, code, s);
     }
 }
 
 // The derived value copies (and packed index streams) a reduced-precision
 // SIRT needs on A and A'.
-int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s) {
-    if (prec == FAIR_PREC_F64) return FAIR_OK;
-    FAIR_TRY(csr_make_lowprec(A, prec, s));
-    FAIR_TRY(csr_make_lowprec(AT, prec, s));
-    if (packed_enabled()) {
+int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool pack_f64) {
+    if (prec != FAIR_PREC_F64) {
+        FAIR_TRY(csr_make_lowprec(A, prec, s));
+        FAIR_TRY(csr_make_lowprec(AT, prec, s));
+    }
+    // FP64 reads the CSR unless tuned (or asked) to read the packed stream,
+    // whose padded FP64 values cost 8 bytes per nonzero more
+    const bool f64_pk = pack_f64 || A.sirt_groups[FAIR_PREC_F64] > 0 ||
+                        AT.sirt_groups[FAIR_PREC_F64] > 0;
+    if (packed_enabled() && (prec != FAIR_PREC_F64 || f64_pk)) {
         FAIR_TRY(csr_make_packed(A, prec, s));
         FAIR_TRY(csr_make_packed(AT, prec, s));
+        FAIR_TRY(csr_make_fused(A, prec, s));
+        FAIR_TRY(csr_make_fused(AT, prec, s));
     }
     return FAIR_OK;
 }
@@ -409,7 +486,7 @@ int sirt_iterations(const SirtDev &S, int K, cudaStream_t s) {
 
 int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_t s,
                   float *ms_best) {
-    FAIR_TRY(sirt_make_forms(A, AT, S.prec, s));
+    FAIR_TRY(sirt_make_forms(A, AT, S.prec, s, true));
     FAIR_TRY(sirt_prepare_shadow(S, s));
     static const int lanes[4] = {4, 8, 16, 32};
     cudaEvent_t ev[2];
@@ -417,14 +494,16 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
     int st = FAIR_OK;
     for (int pass = 1; pass <= 2 && st == FAIR_OK; ++pass) {
         DevCSR &M = pass == 1 ? A : AT;
-        // groups per lane and step: 1 or 2 on the packed stream, else 1
-        const bool pk = S.prec != FAIR_PREC_F64 && M.haspk && packed_enabled();
+        // groups per lane and step on the packed stream (1, 2), or 0: the CSR
+        const bool pk = M.haspk && packed_enabled() &&
+                        (S.prec != FAIR_PREC_F64 || M.hasp64);
+        const bool fu = pk && (S.prec == FAIR_PREC_F16 ? M.hasf16 : S.prec == FAIR_PREC_Q16 && M.hasfq);
         int best_g = M.sirt_lanes[S.prec], best_ng = M.sirt_groups[S.prec];
         float best_ms = -1.f;
         // two rounds over the candidates; each keeps its faster round
-        float t[2][4];
+        float t[5][4];
         for (int round = 0; round < 2 && st == FAIR_OK; ++round)
-            for (int ng = 1; ng <= (pk ? 2 : 1) && st == FAIR_OK; ++ng)
+            for (int ng = 0; ng <= (fu ? 4 : pk ? 2 : 0) && st == FAIR_OK; ++ng)
                 for (int c = 0; c < 4 && st == FAIR_OK; ++c) {
                     M.sirt_lanes[S.prec] = lanes[c];
                     M.sirt_groups[S.prec] = ng;
@@ -437,7 +516,7 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
                     float ms = 0.f;
                     cudaEventElapsedTime(&ms, ev[0], ev[1]);
                     ms /= reps;
-                    float &tc = t[ng - 1][c];
+                    float &tc = t[ng][c];
                     tc = round == 0 ? ms : std::min(tc, ms);
                     if (round == 1 && (best_ms < 0.f || tc < best_ms)) {
                         best_ms = tc;

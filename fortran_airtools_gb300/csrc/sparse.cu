@@ -576,7 +576,7 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
     A.has32 = false;
     A.has16 = false;
     A.hasq = false;
-    A.hasp32 = A.hasp16 = A.haspq = false;
+    A.hasp64 = A.hasp32 = A.hasp16 = A.haspq = A.hasf16 = A.hasfq = false;
     return FAIR_OK;
 }
 
