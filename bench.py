@@ -159,6 +159,18 @@ def algorithmic_bytes(nnz, m, n, prec, packed=None):
     return pass1, pass2
 
 
+def kernel_suffix(prec, code, on_pk):
+    """Name suffix of the SIRT pass kernel that layout `code` runs (layout
+    codes of fair_sirt_set_lanes)."""
+    if not on_pk:
+        return "_f64" if prec == "f64" else "_lp"
+    if code >= 5:
+        return "_sl"
+    if prec == "f64":
+        return "_pk64"
+    return "_pkf" if code >= 3 and prec in ("f16", "q16") else "_pk"
+
+
 def traffic_from_profiles(kernel, prec, nnz):
     """Per-launch DRAM bytes of `kernel` in form `prec` from the ncu capture
     summarised in profiles/ (recorded for the N=1024 launch), if any."""
@@ -334,8 +346,9 @@ def run_ours(args):
     dom = 2 if head["pass2_ms"] >= head["pass1_ms"] else 1
     pk = packed.get(hp)
     on_pk = bool(pk and pk[dom - 1])
-    kind = ("_pk64" if on_pk else "_f64") if hp == "f64" else ("_pk" if on_pk else "_lp")
-    kname = {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kind
+    code = (head["pass_config"]["groups_per_lane"][dom - 1] if head.get("pass_config")
+            else 0 if hp == "f64" else 1)  # the library's default layouts
+    kname = {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kernel_suffix(hp, code, on_pk)
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9

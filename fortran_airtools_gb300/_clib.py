@@ -124,6 +124,7 @@ def _declare(L):
         "fair_sirt_adjoint": ([h, C.c_char_p, i32, vp, vp, i32, vp, P(Opts), vp, vp, vp, vp, vp],
                               C.c_int),
         "fair_csr_packed_info": ([h, i32, P(i32), P(i64), P(i64), P(i32), P(i32)], C.c_int),
+        "fair_csr_sliced_info": ([h, i32, P(i32), P(i64)], C.c_int),
         "fair_sirt_autotune": ([h, vp, vp, i32, vp], C.c_int),
         "fair_sirt_prepare": ([h, C.c_char_p, P(Opts)], C.c_int),
         "fair_sirt_run_device": ([h, vp, vp, i32], C.c_int),

@@ -345,6 +345,7 @@ int enqueue_iterations(fair_batch_s *B, int K, cudaStream_t s) {
 
 // Keep of a problem's matrices only what the batch's passes read.
 void compact(DevCSR &M, int prec) {
+    M.drop_sliced();
     M.v32.release(); M.v16.release(); M.vq.release();
     M.has32 = M.has16 = M.hasq = false;
     if (prec == FAIR_PREC_F64) {
@@ -393,7 +394,7 @@ int finish_problem(fair_batch_s *B, BatchProb &q) {
     FAIR_TRY(sirt_weights(q.A, q.AT, true, q.M_sart.as<double>(), q.D.as<double>(), s));
     FAIR_TRY(sirt_weights(q.A, q.AT, false, q.M_cim.as<double>(), nullptr, s));
     if (B->prec != FAIR_PREC_F64) {
-        FAIR_TRY(sirt_make_forms(q.A, q.AT, B->prec, s));
+        FAIR_TRY(sirt_make_forms(q.A, q.AT, B->prec, s, false, false));
         FAIR_CUDA(cudaStreamSynchronize(s));
         if (q.A.nnz > 0 && (!q.A.haspk || !q.AT.haspk)) {
             set_detail("a reduced-precision batch needs matrices with a packed index stream");

@@ -56,7 +56,14 @@ void DevBuf::release() {
     bytes = 0;
 }
 
+void DevCSR::drop_sliced() {
+    soff.release(); sidx.release(); sv64.release(); sv32.release(); sf16.release(); sfq.release();
+    nslots = 0;
+    hassl = hassidx = hassv64 = hassv32 = hassf16 = hassfq = false;
+}
+
 void DevCSR::release() {
+    drop_sliced();
     rowptr.release(); col.release(); v64.release(); v32.release(); v16.release(); vq.release();
     has32 = has16 = hasq = false;
     prow.release(); gidx.release(); gside.release();
@@ -1180,10 +1187,10 @@ int fair_sirt_set_lanes(fair_csr h, const int32_t *config) {
     NEED_MATRIX(h);
     if (!config) return FAIR_ERR_NULL;
     auto lanes_ok = [](int32_t g) { return g == 4 || g == 8 || g == 16 || g == 32; };
-    auto groups_ok = [](int32_t g) { return g >= 0 && g <= 4; };
+    auto groups_ok = [](int32_t g) { return g >= 0 && g <= 6; };
     if (!lanes_ok(config[0]) || !lanes_ok(config[1]) || !groups_ok(config[2]) ||
         !groups_ok(config[3])) {
-        set_detail("lanes per row must be 4, 8, 16 or 32 and the layout code 0-4");
+        set_detail("lanes per row must be 4, 8, 16 or 32 and the layout code 0-6");
         return FAIR_ERR_ARG;
     }
     FAIR_TRY(ensure_transpose(h));
@@ -1233,6 +1240,16 @@ int fair_csr_packed_info(fair_csr h, int32_t which, int32_t *has, int64_t *ngrou
     *nesc = ok ? M.nesc : 0;
     *stride = ok ? M.pk_S : 0;
     *low_bits = ok ? M.pk_L : 0;
+    return FAIR_OK;
+}
+
+int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslots) {
+    if (!h || !has || !nslots) return FAIR_ERR_NULL;
+    if (which != 0 && which != 1) { set_detail("which must be 0 (A) or 1 (A')"); return FAIR_ERR_ARG; }
+    const DevCSR &M = which == 0 ? h->A : h->AT;
+    const bool ok = M.hassl && (which == 0 || h->at_valid);
+    *has = ok ? 1 : 0;
+    *nslots = ok ? M.nslots : 0;
     return FAIR_OK;
 }
 

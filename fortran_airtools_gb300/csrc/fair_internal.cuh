@@ -53,7 +53,8 @@ struct DevCSR {
     int lanes_per_row = 8;      // G of the row engine (4, 8, 16 or 32)
     int sirt_lanes[4] = {8, 8, 8, 8};  // G of the SIRT passes per form (autotuned)
     // layout of the SIRT passes per form: 0 the CSR; 1, 2 the packed stream with
-    // that many groups per lane and step; 3, 4 the fused records (2-byte forms)
+    // that many groups per lane and step; 3, 4 the fused records (2-byte forms);
+    // 5, 6 the sliced copy with 2 or 4 steps in flight
     int sirt_groups[4] = {0, 1, 1, 1};
     // allocate col and v64 for nnz entries plus the pad (pad zeroed)
     int alloc_entries(int64_t nnz_, cudaStream_t s);
@@ -81,6 +82,17 @@ struct DevCSR {
     bool hasp64 = false, hasp32 = false, hasp16 = false, haspq = false;
     DevBuf pf16, pfq;          // fused 16-byte records {index word, 4 values} (2-byte forms)
     bool hasf16 = false, hasfq = false;
+    // Sliced copies (SELL-32, rows.cuh) of the packed stream: group k of row
+    // 32c+l in slot soff[c] + 32k + l, each chunk of 32 rows padded to its
+    // longest row.
+    DevBuf soff;               // int64 [chunks+1] slot offsets
+    int64_t nslots = 0;
+    bool hassl = false;        // soff built
+    DevBuf sidx;               // uint2 [nslots] index words (FP32 and FP64 forms)
+    DevBuf sv64, sv32;         // 4 values per slot
+    DevBuf sf16, sfq;          // fused records per slot (2-byte forms)
+    bool hassidx = false, hassv64 = false, hassv32 = false, hassf16 = false, hassfq = false;
+    void drop_sliced();
     void release();
     bool empty() const { return rowptr.p == nullptr; }
 };
@@ -114,8 +126,14 @@ int csr_make_packed(DevCSR &A, int prec, cudaStream_t s);
 bool packed_enabled();
 // Fused 16-byte records of the packed stream for a 2-byte form (f16, q16).
 int csr_make_fused(DevCSR &A, int prec, cudaStream_t s);
-// Reduced-precision copies (and packed streams) of A and A' for SIRT (solvers.cu).
-int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool pack_f64 = false);
+// Sliced copy (SELL-32) of the packed stream for `prec` (needs the packed
+// stream; does nothing without it or when a chunk would exceed 2^31 slots).
+int csr_make_sliced(DevCSR &A, int prec, cudaStream_t s);
+// Reduced-precision copies, packed streams and sliced copies of A and A' for
+// SIRT (solvers.cu): every layout with `all`, else the ones the passes are
+// set to read; no sliced copies with sliced = false.
+int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool all = false,
+                    bool sliced = true);
 int csr_scale(DevCSR &A, double c, cudaStream_t s);
 int csr_row_norms(const DevCSR &A, int p, double *d_out, cudaStream_t s);
 int csr_row_dot(const DevCSR &A, int32_t row, const double *d_x, double *d_out, cudaStream_t s);

@@ -137,6 +137,54 @@ __global__ void k_pk_fuse(const uint2 *gidx, const uint2 *vals, int64_t ng, uint
     }
 }
 
+// Slots of each chunk of 32 rows in the sliced copy: 32 x its longest row.
+__global__ void k_sl_len(const int64_t *prow, int32_t m, int64_t nch, int32_t *cnt) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nch;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        int64_t mx = 0;
+        for (int l = 0; l < 32; ++l) {
+            const int64_t r = 32 * c + l;
+            if (r >= m) break;
+            const int64_t g = prow[r + 1] - prow[r];
+            mx = g > mx ? g : mx;
+        }
+        cnt[c] = (int32_t)(32 * mx);
+    }
+}
+
+// Group k of row 32c+l to slot soff[c] + 32k + l (one warp per chunk; the
+// slots past a row's end get zeros).
+template <typename T>
+__global__ void k_sl_copy(const int64_t *prow, int32_t m, int64_t nch, const int64_t *soff,
+                          const T *src, T *dst) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nch; c += nw) {
+        const int64_t r = 32 * c + lane;
+        const int64_t g0 = r < m ? prow[r] : 0;
+        const int64_t ng = r < m ? prow[r + 1] - g0 : 0;
+        const int64_t base = soff[c], len = (soff[c + 1] - base) >> 5;
+        for (int64_t k = 0; k < len; ++k) dst[base + 32 * k + lane] = k < ng ? src[g0 + k] : T{};
+    }
+}
+
+// Four FP64 values of one group, copied as one unit.
+struct alignas(16) Dbl4 {
+    double2 a, b;
+};
+
+template <typename T>
+int sl_copy(const DevCSR &A, const void *src, DevBuf &dst, cudaStream_t s) {
+    FAIR_TRY(dst.grow(sizeof(T) * (size_t)std::max<int64_t>(A.nslots, 1)));
+    const int64_t nch = ((int64_t)A.m + 31) / 32;
+    k_sl_copy<T><<<pk_grid(nch * 32), 256, 0, s>>>(A.prow.as<int64_t>(), A.m, nch,
+                                                   A.soff.as<int64_t>(),
+                                                   static_cast<const T *>(src), dst.as<T>());
+    FAIR_CUDA(cudaGetLastError());
+    return FAIR_OK;
+}
+
 int64_t isqrt64(int64_t v) {
     int64_t r = (int64_t)std::sqrt((double)v);
     while (r * r > v) --r;
@@ -249,6 +297,47 @@ int csr_make_packed(DevCSR &A, int prec, cudaStream_t s) {
         FAIR_TRY(pad_values<uint16_t>(A, A.vq, A.pvq, s));
         A.haspq = true;
     }
+    return FAIR_OK;
+}
+
+int csr_make_sliced(DevCSR &A, int prec, cudaStream_t s) {
+    if (!A.haspk || A.m == 0) return FAIR_OK;
+    // chunk slots and group offsets within a chunk stay below 2^31
+    if (32 * (((int64_t)A.max_row + 3) / 4) >= (int64_t(1) << 31)) return FAIR_OK;
+    const int64_t nch = ((int64_t)A.m + 31) / 32;
+    if (!A.hassl) {
+        DevBuf cnt;
+        FAIR_TRY(cnt.grow(sizeof(int32_t) * (size_t)(nch + 1)));
+        FAIR_TRY(A.soff.grow(sizeof(int64_t) * (size_t)(nch + 1)));
+        k_sl_len<<<pk_grid(nch), 256, 0, s>>>(A.prow.as<int64_t>(), A.m, nch, cnt.as<int32_t>());
+        FAIR_CUDA(cudaGetLastError());
+        FAIR_TRY(scan_counts(cnt.as<int32_t>(), nch, A.soff.as<int64_t>(), s));
+        FAIR_CUDA(cudaMemcpyAsync(&A.nslots, A.soff.as<int64_t>() + nch, sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, s));
+        FAIR_CUDA(cudaStreamSynchronize(s));
+        A.hassl = true;
+    }
+    if (prec == FAIR_PREC_F64 || prec == FAIR_PREC_F32) {
+        FAIR_TRY(csr_make_packed(A, prec, s));
+        if (!A.hassidx) {
+            FAIR_TRY(sl_copy<uint2>(A, A.gidx.p, A.sidx, s));
+            A.hassidx = true;
+        }
+        if (prec == FAIR_PREC_F64 && A.hasp64 && !A.hassv64) {
+            FAIR_TRY(sl_copy<Dbl4>(A, A.pv64.p, A.sv64, s));
+            A.hassv64 = true;
+        } else if (prec == FAIR_PREC_F32 && A.hasp32 && !A.hassv32) {
+            FAIR_TRY(sl_copy<float4>(A, A.pv32.p, A.sv32, s));
+            A.hassv32 = true;
+        }
+        return FAIR_OK;
+    }
+    const bool h = prec == FAIR_PREC_F16;
+    if (h ? A.hassf16 : A.hassfq) return FAIR_OK;
+    FAIR_TRY(csr_make_fused(A, prec, s));
+    if (!(h ? A.hasf16 : A.hasfq)) return FAIR_OK;
+    FAIR_TRY(sl_copy<uint4>(A, (h ? A.pf16 : A.pfq).p, h ? A.sf16 : A.sfq, s));
+    (h ? A.hassf16 : A.hassfq) = true;
     return FAIR_OK;
 }
 

@@ -391,6 +391,140 @@ __device__ __forceinline__ void chunk_rows_pk(const int64_t *__restrict__ prow, 
     finish_chunks(sched, nwarps, lane);
 }
 
+// ---- sliced copy of the packed stream (SELL-32) ----------------------------
+// The chunk of 32 rows is also a slice: group k of row base+l is stored at
+// soff[chunk] + 32k + l, the rows' groups interleaved and the slice padded to
+// its longest row (slots past a row's end hold zeros and are never loaded).
+// One lane owns one row: at step k the warp reads group k of its 32 rows as
+// one coalesced 512-byte window (16-byte records) and keeps the next D
+// windows in flight, each lane adds its own row's products, and the row sum
+// is already in the lane that owns the row, so no lane reduction is needed.
+// The 32 rows of a slice are adjacent rays of one angle (or adjacent pixels
+// of one image column for A'), which reach neighbouring x entries at the
+// same step, so the gathers of a step share cache sectors.
+
+// Step codes to column steps for one (S, L), in shared memory: a table
+// lookup instead of the shifts and multiply of pk_step.
+__device__ __forceinline__ void pk_lut_fill(int *lut, int S, int L) {
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) lut[t] = pk_step((uint32_t)t, S, L);
+    __syncthreads();
+}
+__device__ __forceinline__ void pk_decode_lut(uint2 w, const int4 *__restrict__ gside,
+                                              const int *lut, int (&c)[4]) {
+    c[0] = (int)w.x;
+    c[1] = c[0] + lut[w.y & 0xFFu];
+    c[2] = c[1] + lut[(w.y >> 8) & 0xFFu];
+    c[3] = c[2] + lut[(w.y >> 16) & 0xFFu];
+    if (w.y & kPkEsc) {
+        const int4 t = __ldg(gside + (w.y & 0xFFFFFFu));
+        c[1] = t.x; c[2] = t.y; c[3] = t.z;
+    }
+}
+
+// Four padded values of one group as loaded (VBlk::ld) and converted (to).
+template <typename VT> struct VBlk;
+template <> struct VBlk<double> {
+    double2 a, b;
+    __device__ __forceinline__ void ld(const double *p) {
+        a = __ldcs(reinterpret_cast<const double2 *>(p));
+        b = __ldcs(reinterpret_cast<const double2 *>(p) + 1);
+    }
+    __device__ __forceinline__ void clear() { a = b = make_double2(0.0, 0.0); }
+    __device__ __forceinline__ void to(double (&o)[4]) const { o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y; }
+};
+template <> struct VBlk<float> {
+    float4 a;
+    __device__ __forceinline__ void ld(const float *p) { a = __ldcs(reinterpret_cast<const float4 *>(p)); }
+    __device__ __forceinline__ void clear() { a = make_float4(0.f, 0.f, 0.f, 0.f); }
+    __device__ __forceinline__ void to(float (&o)[4]) const { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
+};
+
+// Slot loaders of a sliced copy: Raw is what a lane holds for one group in
+// flight.
+template <typename VT> struct FusedRec {  // fused 16-byte records, 2-byte values
+    const uint4 *rec;
+    using Raw = uint4;
+    __device__ __forceinline__ Raw load(int64_t j) const { return __ldcs(rec + j); }
+    __device__ __forceinline__ static Raw none() { return make_uint4(0u, 0u, 0u, 0u); }
+    __device__ __forceinline__ static void open(const Raw &r, uint2 &w, float (&v)[4]) {
+        w = make_uint2(r.x, r.y);
+        Conv2B<VT>::to(r.z, r.w, v);
+    }
+};
+template <typename VT> struct SplitRec {  // index words + 4 FP32/FP64 values per slot
+    const uint2 *gidx;
+    const VT *val;
+    struct Raw {
+        uint2 w;
+        VBlk<VT> v;
+    };
+    __device__ __forceinline__ Raw load(int64_t j) const {
+        Raw r;
+        r.w = __ldcs(gidx + j);
+        r.v.ld(val + 4 * j);
+        return r;
+    }
+    __device__ __forceinline__ static Raw none() {
+        Raw r;
+        r.w = make_uint2(0u, 0u);
+        r.v.clear();
+        return r;
+    }
+    __device__ __forceinline__ static void open(const Raw &r, uint2 &w, VT (&v)[4]) {
+        w = r.w;
+        r.v.to(v);
+    }
+};
+
+// Every chunk (slice) owned by this warp: lane l sums row base+l over the
+// sliced copy and calls epi(row, sum). `lut` is the block's step-code table.
+template <typename XT, typename ACC, int D, class LD, class Epi>
+__device__ __forceinline__ void chunk_rows_sliced(const int64_t *__restrict__ prow,
+                                                  const int64_t *__restrict__ soff, int32_t m,
+                                                  const LD &ldr, const int4 *__restrict__ gside,
+                                                  const int *lut, const XT *__restrict__ x,
+                                                  Epi &epi, unsigned *sched) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nchunks = ((int64_t)m + 31) >> 5;
+    for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
+         ch = next_chunk(sched, ch, nwarps, lane)) {
+        const int64_t row = (ch << 5) + lane;
+        const int ng = row < m ? (int)(__ldg(prow + row + 1) - __ldg(prow + row)) : 0;
+        const int64_t s0 = __ldg(soff + ch) + lane;
+        const int len = (int)((__ldg(soff + ch + 1) - __ldg(soff + ch)) >> 5);  // slice length
+        typename LD::Raw ring[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) ring[k] = k < ng ? ldr.load(s0 + 32 * k) : LD::none();
+        ACC acc = 0;
+        for (int k0 = 0; k0 < len; k0 += D) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const int kk = k0 + k;
+                if (kk >= len) break;
+                const typename LD::Raw cur = ring[k];
+                const int kn = kk + D;
+                ring[k] = kn < ng ? ldr.load(s0 + 32 * (int64_t)kn) : LD::none();
+                if (kk < ng) {
+                    uint2 w;
+                    ACC v[4];
+                    LD::open(cur, w, v);
+                    int cc[4];
+                    pk_decode_lut(w, gside, lut, cc);
+                    const int cnt = (int)((w.y >> 24) & 3u);  // entries in the group - 1
+                    acc += (ACC)__ldg(x + cc[0]) * v[0];
+#pragma unroll
+                    for (int t = 1; t < 4; ++t)
+                        if (t <= cnt) acc += (ACC)__ldg(x + cc[t]) * v[t];
+                }
+            }
+        }
+        if (row < m) epi(row, acc);
+    }
+    finish_chunks(sched, nwarps, lane);
+}
+
 // Lanes per row used when none has been tuned.
 constexpr int kDefaultLanesPerRow = 8;
 

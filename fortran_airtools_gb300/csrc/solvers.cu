@@ -14,6 +14,7 @@
 // are evaluated on the GPU: a flag set by a one-block kernel gates the later
 // kernels, so the host enqueues all iterations without synchronising.
 #include <algorithm>
+#include <type_traits>
 
 #include "fair_internal.cuh"
 #include "rows.cuh"
@@ -116,6 +117,27 @@ __global__ void __launch_bounds__(256) k_sirt_update_pkf(PkArgs P, int32_t m, co
                                                          const float *r, EpiUpdateLP epi,
                                                          unsigned *sched) {
     chunk_rows_pkf<VT, G, NG>(P.prow, m, rec, P.gside, P.S, P.L, r, epi, sched);
+}
+// The sliced copy of the packed stream (rows.cuh, chunk_rows_sliced): one
+// lane per row, D steps of 32 slots in flight per warp; LD is the slot loader.
+struct SlArgs {
+    const int64_t *prow, *soff;
+    const int4 *gside;
+    int S, L;
+};
+template <class LD, int D, typename XT, typename ACC, class Epi>
+__global__ void __launch_bounds__(256) k_sirt_resid_sl(SlArgs P, int32_t m, LD ldr, const XT *x,
+                                                       Epi epi, unsigned *sched) {
+    __shared__ int lut[256];
+    pk_lut_fill(lut, P.S, P.L);
+    chunk_rows_sliced<XT, ACC, D>(P.prow, P.soff, m, ldr, P.gside, lut, x, epi, sched);
+}
+template <class LD, int D, typename XT, typename ACC, class Epi>
+__global__ void __launch_bounds__(256) k_sirt_update_sl(SlArgs P, int32_t m, LD ldr, const XT *r,
+                                                        Epi epi, unsigned *sched) {
+    __shared__ int lut[256];
+    pk_lut_fill(lut, P.S, P.L);
+    chunk_rows_sliced<XT, ACC, D>(P.prow, P.soff, m, ldr, P.gside, lut, r, epi, sched);
 }
 template <int G, int NG>
 __global__ void __launch_bounds__(256) k_sirt_resid_pk64(PkArgs P, int32_t m, const double *v,
@@ -312,6 +334,29 @@ int chunk_grid(K kernel, int64_t m) {
         default: { constexpr int g_ = 8; CALL; } break;  \
     }
 
+// Sliced passes (layout codes 5 and 6: 2 or 4 steps in flight).
+template <int PASS, class LD, typename XT, typename ACC, class Epi>
+void sliced_pass(int code, const DevCSR &M, const LD &ldr, const XT *x, const Epi &e,
+                 unsigned *sched, cudaStream_t s) {
+    const SlArgs P{M.prow.as<int64_t>(), M.soff.as<int64_t>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
+    const int32_t m = M.m;
+    if constexpr (PASS == 1) {
+        if (code == 6)
+            k_sirt_resid_sl<LD, 4, XT, ACC, Epi><<<chunk_grid(k_sirt_resid_sl<LD, 4, XT, ACC, Epi>, m), 256, 0, s>>>(
+                P, m, ldr, x, e, sched);
+        else
+            k_sirt_resid_sl<LD, 2, XT, ACC, Epi><<<chunk_grid(k_sirt_resid_sl<LD, 2, XT, ACC, Epi>, m), 256, 0, s>>>(
+                P, m, ldr, x, e, sched);
+    } else {
+        if (code == 6)
+            k_sirt_update_sl<LD, 4, XT, ACC, Epi><<<chunk_grid(k_sirt_update_sl<LD, 4, XT, ACC, Epi>, m), 256, 0, s>>>(
+                P, m, ldr, x, e, sched);
+        else
+            k_sirt_update_sl<LD, 2, XT, ACC, Epi><<<chunk_grid(k_sirt_update_sl<LD, 2, XT, ACC, Epi>, m), 256, 0, s>>>(
+                P, m, ldr, x, e, sched);
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ host ----
@@ -347,6 +392,35 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
                     cudaStream_t s) {
     const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
     const int G = M.sirt_lanes[S.prec];
+    if (code >= 5) {
+        // the sliced copy: fused records of the 2-byte forms, split FP32 slots
+        const uint4 *sl = sizeof(VT) != 2 ? nullptr
+                          : S.prec == FAIR_PREC_F16 ? (M.hassf16 ? M.sf16.as<uint4>() : nullptr)
+                                                    : (M.hassfq ? M.sfq.as<uint4>() : nullptr);
+        const bool ok = pvals && M.hassl &&
+                        (sizeof(VT) == 2 ? sl != nullptr
+                                         : std::is_same<VT, float>::value && M.hassidx && M.hassv32);
+        if (ok) {
+            if (pass == 1) {
+                EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
+                if constexpr (sizeof(VT) == 2)
+                    sliced_pass<1, FusedRec<VT>, float, float>(code, M, FusedRec<VT>{sl}, S.x32, e, S.sched, s);
+                else if constexpr (std::is_same<VT, float>::value)
+                    sliced_pass<1, SplitRec<float>, float, float>(
+                        code, M, SplitRec<float>{M.sidx.as<uint2>(), M.sv32.as<float>()}, S.x32, e, S.sched, s);
+            } else {
+                EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale};
+                const float *r = (const float *)S.r;
+                if constexpr (sizeof(VT) == 2)
+                    sliced_pass<2, FusedRec<VT>, float, float>(code, M, FusedRec<VT>{sl}, r, e, S.sched, s);
+                else if constexpr (std::is_same<VT, float>::value)
+                    sliced_pass<2, SplitRec<float>, float, float>(
+                        code, M, SplitRec<float>{M.sidx.as<uint2>(), M.sv32.as<float>()}, r, e, S.sched, s);
+            }
+            return;
+        }
+        code = code == 6 ? 2 : 1;  // the packed stream's lane layout instead
+    }
     if (code >= 3 && (!fused || sizeof(VT) != 2)) code -= 2;
     if (code >= 1 && !pvals) code = 0;
     if (pass == 1) {
@@ -398,11 +472,24 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
     const DevCSR &M = pass == 1 ? *S.A : *S.AT;
     if (M.m == 0) return;
     if (S.prec == FAIR_PREC_F64) {
-        const int G = M.sirt_lanes[FAIR_PREC_F64], NG = M.sirt_groups[FAIR_PREC_F64];
+        const int G = M.sirt_lanes[FAIR_PREC_F64];
+        int NG = M.sirt_groups[FAIR_PREC_F64];
         if (NG > 0 && M.haspk && M.hasp64 && packed_enabled()) {
             const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S,
                            M.pk_L};
             const double *pv = M.pv64.as<double>();
+            if (NG >= 5 && M.hassl && M.hassidx && M.hassv64) {
+                const SplitRec<double> ld{M.sidx.as<uint2>(), M.sv64.as<double>()};
+                if (pass == 1)
+                    sliced_pass<1, SplitRec<double>, double, double>(
+                        NG, M, ld, S.x, EpiResidF64{S.b, S.Minv, (double *)S.r}, S.sched, s);
+                else
+                    sliced_pass<2, SplitRec<double>, double, double>(
+                        NG, M, ld, (const double *)S.r, EpiUpdateF64{S.D, S.x, S.omg, S.lb, S.ub, S.bmode},
+                        S.sched, s);
+                return;
+            }
+            if (NG > 2) NG = 2 - (NG & 1);  // 3, 5 -> 1 group per lane; 4, 6 -> 2
             if (pass == 1) {
                 EpiResidF64 e{S.b, S.Minv, (double *)S.r};
                 if (NG == 2)
@@ -455,21 +542,25 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
 }
 
 // The derived value copies (and packed index streams) a reduced-precision
-// SIRT needs on A and A'.
-int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool pack_f64) {
+// SIRT needs on A and A'. With `all` (the autotuner) every layout of the form
+// is built; otherwise the ones the passes are set to read. `sliced` = false
+// leaves out the sliced copies.
+int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool all, bool sliced) {
     if (prec != FAIR_PREC_F64) {
         FAIR_TRY(csr_make_lowprec(A, prec, s));
         FAIR_TRY(csr_make_lowprec(AT, prec, s));
     }
     // FP64 reads the CSR unless tuned (or asked) to read the packed stream,
     // whose padded FP64 values cost 8 bytes per nonzero more
-    const bool f64_pk = pack_f64 || A.sirt_groups[FAIR_PREC_F64] > 0 ||
+    const bool f64_pk = all || A.sirt_groups[FAIR_PREC_F64] > 0 ||
                         AT.sirt_groups[FAIR_PREC_F64] > 0;
     if (packed_enabled() && (prec != FAIR_PREC_F64 || f64_pk)) {
         FAIR_TRY(csr_make_packed(A, prec, s));
         FAIR_TRY(csr_make_packed(AT, prec, s));
         FAIR_TRY(csr_make_fused(A, prec, s));
         FAIR_TRY(csr_make_fused(AT, prec, s));
+        if (sliced && (all || A.sirt_groups[prec] >= 5)) FAIR_TRY(csr_make_sliced(A, prec, s));
+        if (sliced && (all || AT.sirt_groups[prec] >= 5)) FAIR_TRY(csr_make_sliced(AT, prec, s));
     }
     return FAIR_OK;
 }
@@ -498,14 +589,24 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
         const bool pk = M.haspk && packed_enabled() &&
                         (S.prec != FAIR_PREC_F64 || M.hasp64);
         const bool fu = pk && (S.prec == FAIR_PREC_F16 ? M.hasf16 : S.prec == FAIR_PREC_Q16 && M.hasfq);
+        // the sliced copy of the form
+        const bool sw = pk && M.hassl &&
+                        (S.prec == FAIR_PREC_F64   ? M.hassidx && M.hassv64
+                         : S.prec == FAIR_PREC_F32 ? M.hassidx && M.hassv32
+                         : S.prec == FAIR_PREC_F16 ? M.hassf16
+                                                   : M.hassfq);
         int best_g = M.sirt_lanes[S.prec], best_ng = M.sirt_groups[S.prec];
         float best_ms = -1.f;
         // two rounds over the candidates; each keeps its faster round
-        float t[5][4];
+        float t[7][4];
         for (int round = 0; round < 2 && st == FAIR_OK; ++round)
-            for (int ng = 0; ng <= (fu ? 4 : pk ? 2 : 0) && st == FAIR_OK; ++ng)
-                for (int c = 0; c < 4 && st == FAIR_OK; ++c) {
-                    M.sirt_lanes[S.prec] = lanes[c];
+            for (int ng = 0; ng <= 6 && st == FAIR_OK; ++ng) {
+                if (ng >= 1 && ng <= 2 && !pk) continue;
+                if (ng >= 3 && ng <= 4 && !fu) continue;
+                if (ng >= 5 && !sw) continue;
+                // lanes per row do not matter to the sliced copy: one candidate
+                for (int c = 0; c < (ng >= 5 ? 1 : 4) && st == FAIR_OK; ++c) {
+                    M.sirt_lanes[S.prec] = ng >= 5 ? best_g : lanes[c];
                     M.sirt_groups[S.prec] = ng;
                     sirt_pass(S, pass, s);  // warm-up
                     cudaEventRecord(ev[0], s);
@@ -520,10 +621,11 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
                     tc = round == 0 ? ms : std::min(tc, ms);
                     if (round == 1 && (best_ms < 0.f || tc < best_ms)) {
                         best_ms = tc;
-                        best_g = lanes[c];
+                        best_g = M.sirt_lanes[S.prec];
                         best_ng = ng;
                     }
                 }
+            }
         M.sirt_lanes[S.prec] = best_g;
         M.sirt_groups[S.prec] = best_ng;
         if (ms_best) ms_best[pass - 1] = best_ms;

@@ -577,6 +577,7 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
     A.has16 = false;
     A.hasq = false;
     A.hasp64 = A.hasp32 = A.hasp16 = A.haspq = A.hasf16 = A.hasfq = false;
+    A.hassv64 = A.hassv32 = A.hassf16 = A.hassfq = false;
     return FAIR_OK;
 }
 

@@ -62,13 +62,17 @@ class CSRMatrix:
 
     def packed_info(self, transposed: bool = False) -> dict:
         """Packed index stream of A (or A'), built by the first reduced-precision
-        SIRT: {'has', 'ngroups', 'nesc', 'stride', 'low_bits'}."""
-        has, S, L = C.c_int32(), C.c_int32(), C.c_int32()
-        ng, ne = C.c_int64(), C.c_int64()
-        check(lib().fair_csr_packed_info(self._h, 1 if transposed else 0, C.byref(has),
+        SIRT: {'has', 'ngroups', 'nesc', 'stride', 'low_bits', 'sliced',
+        'nslots'} ('sliced': its SELL-32 copy is built, with 'nslots' slots)."""
+        has, S, L, sl = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        ng, ne, ns = C.c_int64(), C.c_int64(), C.c_int64()
+        which = 1 if transposed else 0
+        check(lib().fair_csr_packed_info(self._h, which, C.byref(has),
                                          C.byref(ng), C.byref(ne), C.byref(S), C.byref(L)))
+        check(lib().fair_csr_sliced_info(self._h, which, C.byref(sl), C.byref(ns)))
         return {"has": bool(has.value), "ngroups": ng.value, "nesc": ne.value,
-                "stride": S.value, "low_bits": L.value}
+                "stride": S.value, "low_bits": L.value, "sliced": bool(sl.value),
+                "nslots": ns.value}
 
     def set_stream(self, cuda_stream_ptr: int | None):
         check(lib().fair_csr_set_stream(self._h, cuda_stream_ptr))

@@ -51,18 +51,26 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
                       const double *gx, double *xK, double *gb, double *gx0, double *glam);
 
 /* Autotuner of the SIRT passes (no reference counterpart): after
- * fair_sirt_prepare, times each pass over A and A' with 4, 8, 16 and 32 lanes
- * per row and, on a packed index stream, 1 or 2 groups of 4 entries per lane
- * and step (reps launches each, CUDA events on the handle's stream), and
+ * fair_sirt_prepare, times each pass over A and A' on every layout the
+ * matrix has (reps launches each, CUDA events on the handle's stream), and
  * keeps the fastest for the handle's current precision. config (may be NULL)
- * receives {lanes A, lanes A', groups A, groups A'}. d_b as in
- * fair_sirt_run_device; d_x is scratch (overwritten). */
+ * receives {lanes A, lanes A', layout A, layout A'}. Layout codes:
+ *   0     the CSR (int32 columns + values), lanes per row 4, 8, 16 or 32;
+ *   1, 2  the packed index stream with padded values, that many groups of 4
+ *         entries per lane and step;
+ *   3, 4  the fused 16-byte records {index word, 4 values} of the 2-byte
+ *         forms (f16, q16), 1 or 2 records per lane and step;
+ *   5, 6  the packed stream (fused records for the 2-byte forms) walked
+ *         linearly, one group per lane, 2 or 4 windows of 32 groups in flight
+ *         per warp (lanes per row unused).
+ * A code whose layout the matrix lacks falls back to the nearest one it has.
+ * d_b as in fair_sirt_run_device; d_x is scratch (overwritten). */
 int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
                        int32_t *config);
 
-/* Sets {lanes A, lanes A', groups A, groups A'} of the SIRT passes for the
- * handle's current precision: lanes per row 4, 8, 16 or 32; groups per lane
- * 1 or 2 (used on the packed index stream). No reference counterpart. */
+/* Sets {lanes A, lanes A', layout A, layout A'} of the SIRT passes for the
+ * handle's current precision: lanes per row 4, 8, 16 or 32; layout codes 0-6
+ * as listed at fair_sirt_autotune. No reference counterpart. */
 int fair_sirt_set_lanes(fair_csr h, const int32_t *config);
 
 /* Packed index stream of A (which = 0) or A' (which = 1), built by the first
@@ -72,6 +80,12 @@ int fair_sirt_set_lanes(fair_csr h, const int32_t *config);
  * stream is used unless the environment sets FAIR_PACKED=0. */
 int fair_csr_packed_info(fair_csr h, int32_t which, int32_t *has, int64_t *ngroups,
                          int64_t *nesc, int32_t *stride, int32_t *low_bits);
+
+/* Sliced copy (SELL-32) of the packed stream of A (which = 0) or A' (1),
+ * built when a SIRT pass is set to layout 5 or 6 or by the autotuner (no
+ * reference counterpart): has = 1 when built, nslots = its slots (groups plus
+ * the padding of each chunk of 32 rows to its longest row). */
+int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslots);
 
 /* Capacity, in doubles, of the fixed device array behind
  * fair_matvecmul_noalloc (32 MiB): n + m of the matrix must fit in it. */
