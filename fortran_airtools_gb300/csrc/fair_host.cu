@@ -59,6 +59,7 @@ void DevBuf::release() {
 void DevCSR::drop_sliced() {
     soff.release(); sidx.release(); sv64.release(); sv32.release(); sf16.release(); sfq.release();
     nslots = 0;
+    sl_G = 0;
     hassl = hassidx = hassv64 = hassv32 = hassf16 = hassfq = false;
 }
 
@@ -1186,11 +1187,16 @@ int fair_sirt_set_lanes(fair_csr h, const int32_t *config) {
     ENTER(h);
     NEED_MATRIX(h);
     if (!config) return FAIR_ERR_NULL;
-    auto lanes_ok = [](int32_t g) { return g == 4 || g == 8 || g == 16 || g == 32; };
-    auto groups_ok = [](int32_t g) { return g >= 0 && g <= 6; };
-    if (!lanes_ok(config[0]) || !lanes_ok(config[1]) || !groups_ok(config[2]) ||
-        !groups_ok(config[3])) {
-        set_detail("lanes per row must be 4, 8, 16 or 32 and the layout code 0-6");
+    // lanes per row: 4-32 on the row layouts (codes 0-4); 1-8, or 0 (chosen
+    // per chunk), on the sliced copy (5-8)
+    auto ok = [](int32_t g, int32_t code) {
+        if (code >= 0 && code <= 4) return g == 4 || g == 8 || g == 16 || g == 32;
+        if (code >= 5 && code <= 8) return g == 0 || g == 1 || g == 2 || g == 4 || g == 8;
+        return false;
+    };
+    if (!ok(config[0], config[2]) || !ok(config[1], config[3])) {
+        set_detail("layout code must be 0-8, with 4, 8, 16 or 32 lanes per row for codes 0-4 "
+                   "and 0, 1, 2, 4 or 8 for codes 5-8");
         return FAIR_ERR_ARG;
     }
     FAIR_TRY(ensure_transpose(h));

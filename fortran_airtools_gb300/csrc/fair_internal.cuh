@@ -42,6 +42,14 @@ struct DevBuf {
     template <typename T> T *as() const { return static_cast<T *>(p); }
 };
 
+// A scratch allocation released when it goes out of scope.
+struct TmpBuf : DevBuf {
+    TmpBuf() = default;
+    TmpBuf(const TmpBuf &) = delete;
+    TmpBuf &operator=(const TmpBuf &) = delete;
+    ~TmpBuf() { release(); }
+};
+
 // Spare entries after every column/value array: the 16-byte-aligned load
 // window of the row engine (rows.cuh) may read up to 3 entries past the end.
 constexpr int64_t kEntryPad = 4;
@@ -54,7 +62,8 @@ struct DevCSR {
     int sirt_lanes[4] = {8, 8, 8, 8};  // G of the SIRT passes per form (autotuned)
     // layout of the SIRT passes per form: 0 the CSR; 1, 2 the packed stream with
     // that many groups per lane and step; 3, 4 the fused records (2-byte forms);
-    // 5, 6 the sliced copy with 2 or 4 steps in flight
+    // 5, 6 the sliced copy with 2 or 4 steps in flight; 7, 8 the same with
+    // the gathers one step ahead
     int sirt_groups[4] = {0, 1, 1, 1};
     // allocate col and v64 for nnz entries plus the pad (pad zeroed)
     int alloc_entries(int64_t nnz_, cudaStream_t s);
@@ -82,11 +91,11 @@ struct DevCSR {
     bool hasp64 = false, hasp32 = false, hasp16 = false, haspq = false;
     DevBuf pf16, pfq;          // fused 16-byte records {index word, 4 values} (2-byte forms)
     bool hasf16 = false, hasfq = false;
-    // Sliced copies (SELL-32, rows.cuh) of the packed stream: group k of row
-    // 32c+l in slot soff[c] + 32k + l, each chunk of 32 rows padded to its
-    // longest row.
+    // Sliced copies of the packed stream (rows.cuh): slices of 32/sl_G rows
+    // with sl_G lanes per row, each chunk of 32 rows one run of slots.
     DevBuf soff;               // int64 [chunks+1] slot offsets
     int64_t nslots = 0;
+    int sl_G = 0;              // lanes per row of the built copy
     bool hassl = false;        // soff built
     DevBuf sidx;               // uint2 [nslots] index words (FP32 and FP64 forms)
     DevBuf sv64, sv32;         // 4 values per slot
@@ -126,9 +135,10 @@ int csr_make_packed(DevCSR &A, int prec, cudaStream_t s);
 bool packed_enabled();
 // Fused 16-byte records of the packed stream for a 2-byte form (f16, q16).
 int csr_make_fused(DevCSR &A, int prec, cudaStream_t s);
-// Sliced copy (SELL-32) of the packed stream for `prec` (needs the packed
-// stream; does nothing without it or when a chunk would exceed 2^31 slots).
-int csr_make_sliced(DevCSR &A, int prec, cudaStream_t s);
+// Sliced copy of the packed stream with G lanes per row (1, 2, 4 or 8;
+// rows.cuh) for `prec`, rebuilt when G changes (needs the packed stream; does
+// nothing without it or when a chunk would exceed 2^31 slots).
+int csr_make_sliced(DevCSR &A, int prec, int G, cudaStream_t s);
 // Reduced-precision copies, packed streams and sliced copies of A and A' for
 // SIRT (solvers.cu): every layout with `all`, else the ones the passes are
 // set to read; no sliced copies with sliced = false.
@@ -167,6 +177,9 @@ int sirt_iterations(const SirtDev &S, int K, cudaStream_t s);
 // One SIRT pass (1: residual over A, 2: update over A') with the forms
 // already made; enqueues one kernel.
 void sirt_pass(const SirtDev &S, int pass, cudaStream_t s);
+// One SIRT pass over the sliced copy (layout codes 5-8, sirt_sliced.cu);
+// false when the matrix has no sliced copy of the form.
+bool sirt_pass_sliced(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s);
 // Same with CUDA events around each pass; summed pass durations in ms.
 int sirt_iterations_timed(const SirtDev &S, int K, cudaStream_t s, float *ms1, float *ms2);
 // Times each SIRT pass for every lanes-per-row choice and keeps the fastest
@@ -230,6 +243,21 @@ int dev_dot(const double *a, const double *b, int64_t n, double *d_partials, dou
 // ---- launch helpers -----------------------------------------------------------
 int sm_count();
 constexpr int kReduceBlocks = 4096;  // partial-sum slots used by reductions (>= any grid)
+
+// Grid of a chunk kernel (rows.cuh, 256 threads = 8 warps per block): the
+// blocks that stay resident on every SM, no more than the chunks of 32 rows
+// need, and never more than the partial-sum slots.
+template <class K>
+int chunk_grid(K kernel, int64_t m) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0);
+    if (occ < 1) occ = 1;
+    const int64_t need = (((int64_t)m + 31) / 32 + 7) / 8;
+    int64_t g = (int64_t)sm_count() * occ;
+    if (g > need) g = need;
+    if (g < 1) g = 1;
+    return (int)(g < kReduceBlocks ? g : kReduceBlocks);
+}
 
 // ---- project random stream ---------------------------------------------------------
 // Reserve `count` draws of the library stream (fair_host.cu): seed and first counter.

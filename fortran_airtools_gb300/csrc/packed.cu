@@ -137,35 +137,81 @@ __global__ void k_pk_fuse(const uint2 *gidx, const uint2 *vals, int64_t ng, uint
     }
 }
 
-// Slots of each chunk of 32 rows in the sliced copy: 32 x its longest row.
-__global__ void k_sl_len(const int64_t *prow, int32_t m, int64_t nch, int32_t *cnt) {
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nch;
-         c += (int64_t)gridDim.x * blockDim.x) {
-        int64_t mx = 0;
-        for (int l = 0; l < 32; ++l) {
-            const int64_t r = 32 * c + l;
-            if (r >= m) break;
-            const int64_t g = prow[r + 1] - prow[r];
-            mx = g > mx ? g : mx;
-        }
-        cnt[c] = (int32_t)(32 * mx);
-    }
-}
-
-// Group k of row 32c+l to slot soff[c] + 32k + l (one warp per chunk; the
-// slots past a row's end get zeros).
-template <typename T>
-__global__ void k_sl_copy(const int64_t *prow, int32_t m, int64_t nch, const int64_t *soff,
-                          const T *src, T *dst) {
+// Slots of each chunk in the sliced copy (rows.cuh), one warp per chunk: 32
+// per step, the chunk's steps being the sum over its slices of R = 32/G rows
+// of the slice's longest row in steps of G groups. G is the given one, or
+// with G = 0 chosen per chunk from its rows' column steps: 8 lanes along
+// each row when most steps are +-1 (neighbouring entries of a row are
+// neighbours in x, so a row's lanes share cache sectors), else 1 lane per row
+// (the rows' entries at one step are neighbours in x). lg[c] = log2 of the
+// chunk's G.
+__global__ void k_sl_len(const int64_t *prow, int32_t m, int64_t nch, int G, const uint2 *gidx,
+                         int S, int L, int32_t *cnt, int8_t *lg) {
+    constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t c = warp; c < nch; c += nw) {
         const int64_t r = 32 * c + lane;
-        const int64_t g0 = r < m ? prow[r] : 0;
-        const int64_t ng = r < m ? prow[r + 1] - g0 : 0;
-        const int64_t base = soff[c], len = (soff[c + 1] - base) >> 5;
-        for (int64_t k = 0; k < len; ++k) dst[base + 32 * k + lane] = k < ng ? src[g0 + k] : T{};
+        const int64_t ng = r < m ? prow[r + 1] - prow[r] : 0;
+        int g = G;
+        if (g == 0) {
+            const int64_t s0 = prow[32 * c], s1 = prow[32 * c + 32 < m ? 32 * c + 32 : m];
+            unsigned unit = 0, other = 0;
+            for (int64_t j = s0 + lane; j < s1; j += 32) {
+                const uint2 w = gidx[j];
+                if (w.y & kPkEsc) { other += 3; continue; }
+                const int cnt = (int)((w.y >> 24) & 3u);
+                for (int t = 0; t < cnt; ++t) {
+                    const int d = pk_step((w.y >> (8 * t)) & 0xFFu, S, L);
+                    (d == 1 || d == -1 ? unit : other) += 1;
+                }
+            }
+            unit = __reduce_add_sync(FULL, unit);
+            other = __reduce_add_sync(FULL, other);
+            g = unit > other ? 8 : 1;
+        }
+        const int R = 32 / g;
+        const unsigned st = (unsigned)((ng + g - 1) / g);
+        int64_t total = 0;
+        for (int i = 0; i < g; ++i) total += __reduce_max_sync(FULL, lane / R == i ? st : 0u);
+        if (lane == 0) {
+            cnt[c] = (int32_t)(32 * total);
+            lg[c] = (int8_t)(g == 8 ? 3 : g == 4 ? 2 : g == 2 ? 1 : 0);
+        }
+    }
+}
+
+// Tag every chunk's slot offset with its log2 G (offsets are multiples of 32).
+__global__ void k_sl_tag(int64_t *soff, int64_t nch, const int8_t *lg) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nch;
+         c += (int64_t)gridDim.x * blockDim.x)
+        soff[c] |= lg[c];
+}
+
+// The slots of one chunk per warp: at step k of slice i, lane g*G + l gets
+// group k*G + l of row 32c + i*R + g, or `hole` past the row's end.
+template <typename T>
+__global__ void k_sl_copy(const int64_t *prow, int32_t m, int64_t nch, const int64_t *soff,
+                          const T *src, T *dst, T hole) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nch; c += nw) {
+        const int G = 1 << (int)(soff[c] & 7), R = 32 / G, g = lane / G, gl = lane % G;
+        int64_t pos = soff[c] & ~(int64_t)31;
+        for (int i = 0; i < G; ++i) {
+            const int64_t r = 32 * c + i * R + g;
+            const int64_t g0 = r < m ? prow[r] : 0;
+            const int64_t ng = r < m ? prow[r + 1] - g0 : 0;
+            const unsigned st = (unsigned)((ng + G - 1) / G);
+            const int64_t Ls = (int64_t)__reduce_max_sync(0xffffffffu, st);
+            for (int64_t k = 0; k < Ls; ++k) {
+                const int64_t j = k * G + gl;
+                dst[pos + 32 * k + lane] = j < ng ? src[g0 + j] : hole;
+            }
+            pos += 32 * Ls;
+        }
     }
 }
 
@@ -175,12 +221,12 @@ struct alignas(16) Dbl4 {
 };
 
 template <typename T>
-int sl_copy(const DevCSR &A, const void *src, DevBuf &dst, cudaStream_t s) {
+int sl_copy(const DevCSR &A, const void *src, DevBuf &dst, T hole, cudaStream_t s) {
     FAIR_TRY(dst.grow(sizeof(T) * (size_t)std::max<int64_t>(A.nslots, 1)));
     const int64_t nch = ((int64_t)A.m + 31) / 32;
     k_sl_copy<T><<<pk_grid(nch * 32), 256, 0, s>>>(A.prow.as<int64_t>(), A.m, nch,
                                                    A.soff.as<int64_t>(),
-                                                   static_cast<const T *>(src), dst.as<T>());
+                                                   static_cast<const T *>(src), dst.as<T>(), hole);
     FAIR_CUDA(cudaGetLastError());
     return FAIR_OK;
 }
@@ -215,7 +261,7 @@ int build_index(DevCSR &A, cudaStream_t s) {
         for (int L = 4; L <= 5; ++L) add((int)sq, L);
     add(0, 7);
 
-    DevBuf gcnt, esc;
+    TmpBuf gcnt, esc;
     FAIR_TRY(gcnt.grow(sizeof(int32_t) * ((size_t)A.m + 1)));
     FAIR_TRY(A.prow.grow(sizeof(int64_t) * ((size_t)A.m + 1)));
     FAIR_TRY(esc.grow(sizeof(unsigned long long) * (kPkCand + 1)));
@@ -300,34 +346,45 @@ int csr_make_packed(DevCSR &A, int prec, cudaStream_t s) {
     return FAIR_OK;
 }
 
-int csr_make_sliced(DevCSR &A, int prec, cudaStream_t s) {
+int csr_make_sliced(DevCSR &A, int prec, int G, cudaStream_t s) {
     if (!A.haspk || A.m == 0) return FAIR_OK;
+    if (G != 0 && G != 1 && G != 2 && G != 4 && G != 8) {
+        set_detail("sliced copy: lanes per row must be 0 (per chunk), 1, 2, 4 or 8");
+        return FAIR_ERR_ARG;
+    }
     // chunk slots and group offsets within a chunk stay below 2^31
-    if (32 * (((int64_t)A.max_row + 3) / 4) >= (int64_t(1) << 31)) return FAIR_OK;
+    if (32 * (((int64_t)A.max_row + 3) / 4 + 8) >= (int64_t(1) << 31)) return FAIR_OK;
+    if (A.hassl && A.sl_G != G) A.drop_sliced();
     const int64_t nch = ((int64_t)A.m + 31) / 32;
     if (!A.hassl) {
-        DevBuf cnt;
+        TmpBuf cnt, lg;  // released after the synchronisation below
         FAIR_TRY(cnt.grow(sizeof(int32_t) * (size_t)(nch + 1)));
+        FAIR_TRY(lg.grow((size_t)nch));
         FAIR_TRY(A.soff.grow(sizeof(int64_t) * (size_t)(nch + 1)));
-        k_sl_len<<<pk_grid(nch), 256, 0, s>>>(A.prow.as<int64_t>(), A.m, nch, cnt.as<int32_t>());
+        k_sl_len<<<pk_grid(nch * 32), 256, 0, s>>>(A.prow.as<int64_t>(), A.m, nch, G,
+                                                   A.gidx.as<uint2>(), A.pk_S, A.pk_L,
+                                                   cnt.as<int32_t>(), lg.as<int8_t>());
         FAIR_CUDA(cudaGetLastError());
         FAIR_TRY(scan_counts(cnt.as<int32_t>(), nch, A.soff.as<int64_t>(), s));
+        k_sl_tag<<<pk_grid(nch), 256, 0, s>>>(A.soff.as<int64_t>(), nch, lg.as<int8_t>());
+        FAIR_CUDA(cudaGetLastError());
         FAIR_CUDA(cudaMemcpyAsync(&A.nslots, A.soff.as<int64_t>() + nch, sizeof(int64_t),
                                   cudaMemcpyDeviceToHost, s));
         FAIR_CUDA(cudaStreamSynchronize(s));
+        A.sl_G = G;
         A.hassl = true;
     }
     if (prec == FAIR_PREC_F64 || prec == FAIR_PREC_F32) {
         FAIR_TRY(csr_make_packed(A, prec, s));
         if (!A.hassidx) {
-            FAIR_TRY(sl_copy<uint2>(A, A.gidx.p, A.sidx, s));
+            FAIR_TRY(sl_copy<uint2>(A, A.gidx.p, A.sidx, make_uint2(0u, kPkHole), s));
             A.hassidx = true;
         }
         if (prec == FAIR_PREC_F64 && A.hasp64 && !A.hassv64) {
-            FAIR_TRY(sl_copy<Dbl4>(A, A.pv64.p, A.sv64, s));
+            FAIR_TRY(sl_copy<Dbl4>(A, A.pv64.p, A.sv64, Dbl4{}, s));
             A.hassv64 = true;
         } else if (prec == FAIR_PREC_F32 && A.hasp32 && !A.hassv32) {
-            FAIR_TRY(sl_copy<float4>(A, A.pv32.p, A.sv32, s));
+            FAIR_TRY(sl_copy<float4>(A, A.pv32.p, A.sv32, make_float4(0.f, 0.f, 0.f, 0.f), s));
             A.hassv32 = true;
         }
         return FAIR_OK;
@@ -336,7 +393,8 @@ int csr_make_sliced(DevCSR &A, int prec, cudaStream_t s) {
     if (h ? A.hassf16 : A.hassfq) return FAIR_OK;
     FAIR_TRY(csr_make_fused(A, prec, s));
     if (!(h ? A.hasf16 : A.hasfq)) return FAIR_OK;
-    FAIR_TRY(sl_copy<uint4>(A, (h ? A.pf16 : A.pfq).p, h ? A.sf16 : A.sfq, s));
+    FAIR_TRY(sl_copy<uint4>(A, (h ? A.pf16 : A.pfq).p, h ? A.sf16 : A.sfq,
+                            make_uint4(0u, kPkHole, 0u, 0u), s));
     (h ? A.hassf16 : A.hassfq) = true;
     return FAIR_OK;
 }

@@ -23,23 +23,60 @@
 
 namespace fair {
 
+// Loads of the matrix streams (indices, values, records): read once per pass,
+// so they bypass L1 (no allocation), which stays with the gathered vector,
+// and ask L2 to fetch 256-byte blocks around each access.
+#define FAIR_STREAM_L1_BYPASS 1
+#if FAIR_STREAM_L1_BYPASS
+__device__ __forceinline__ uint4 ld_stream(const uint4 *p) {
+    uint4 r;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ int4 ld_stream(const int4 *p) {
+    int4 r;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.v4.s32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ uint2 ld_stream(const uint2 *p) {
+    uint2 r;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ float4 ld_stream(const float4 *p) {
+    float4 r;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ double2 ld_stream(const double2 *p) {
+    double2 r;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.v2.f64 {%0, %1}, [%2];" : "=d"(r.x), "=d"(r.y) : "l"(p));
+    return r;
+}
+#else
+template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+#endif
+
 template <typename VT, typename AT> struct VLoad;
 template <> struct VLoad<double, double> {
     static __device__ __forceinline__ void ld(const double *p, double (&o)[4]) {
-        double2 a = __ldcs(reinterpret_cast<const double2 *>(p));
-        double2 b = __ldcs(reinterpret_cast<const double2 *>(p) + 1);
+        double2 a = ld_stream(reinterpret_cast<const double2 *>(p));
+        double2 b = ld_stream(reinterpret_cast<const double2 *>(p) + 1);
         o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
     }
 };
 template <> struct VLoad<float, float> {
     static __device__ __forceinline__ void ld(const float *p, float (&o)[4]) {
-        float4 t = __ldcs(reinterpret_cast<const float4 *>(p));
+        float4 t = ld_stream(reinterpret_cast<const float4 *>(p));
         o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
     }
 };
 template <> struct VLoad<__half, float> {
     static __device__ __forceinline__ void ld(const __half *p, float (&o)[4]) {
-        uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
+        uint2 t = ld_stream(reinterpret_cast<const uint2 *>(p));
         __half2 a = *reinterpret_cast<__half2 *>(&t.x), b = *reinterpret_cast<__half2 *>(&t.y);
         float2 fa = __half22float2(a), fb = __half22float2(b);
         o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
@@ -108,13 +145,13 @@ template <> struct Conv2B<__half> {
 };
 template <> struct VLoad<uint16_t, float> {
     static __device__ __forceinline__ void ld(const uint16_t *p, float (&o)[4]) {
-        uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
+        uint2 t = ld_stream(reinterpret_cast<const uint2 *>(p));
         Conv2B<uint16_t>::to(t.x, t.y, o);
     }
 };
 template <> struct VLoad<int16_t, float> {
     static __device__ __forceinline__ void ld(const int16_t *p, float (&o)[4]) {
-        uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
+        uint2 t = ld_stream(reinterpret_cast<const uint2 *>(p));
         Conv2B<int16_t>::to(t.x, t.y, o);
     }
 };
@@ -143,7 +180,7 @@ __device__ __forceinline__ ACC csr_chunk_sums(const int64_t *__restrict__ rowptr
         int4 cc = make_int4(0, 0, 0, 0);
         ACC vv[4] = {0, 0, 0, 0};
         if (k < e) {
-            cc = __ldcs(reinterpret_cast<const int4 *>(col + k));
+            cc = ld_stream(reinterpret_cast<const int4 *>(col + k));
             VLoad<VT, ACC>::ld(val + k, vv);
         }
         while (k < e) {
@@ -151,7 +188,7 @@ __device__ __forceinline__ ACC csr_chunk_sums(const int64_t *__restrict__ rowptr
             int4 cn = make_int4(0, 0, 0, 0);
             ACC vn[4] = {0, 0, 0, 0};
             if (kn < e) {
-                cn = __ldcs(reinterpret_cast<const int4 *>(col + kn));
+                cn = ld_stream(reinterpret_cast<const int4 *>(col + kn));
                 VLoad<VT, ACC>::ld(val + kn, vn);
             }
             if (k >= s && k + 3 < e) {
@@ -253,14 +290,14 @@ template <typename VT, typename ACC> struct SplitLoad {
     const uint2 *gidx;
     const VT *val;
     __device__ __forceinline__ void ld(int64_t j, uint2 &w, ACC (&v)[4]) const {
-        w = __ldcs(gidx + j);
+        w = ld_stream(gidx + j);
         VLoad<VT, ACC>::ld(val + 4 * j, v);
     }
 };
 template <typename VT> struct FusedLoad {
     const uint4 *rec;
     __device__ __forceinline__ void ld(int64_t j, uint2 &w, float (&v)[4]) const {
-        const uint4 r = __ldcs(rec + j);
+        const uint4 r = ld_stream(rec + j);
         w = make_uint2(r.x, r.y);
         Conv2B<VT>::to(r.z, r.w, v);
     }
@@ -391,17 +428,22 @@ __device__ __forceinline__ void chunk_rows_pk(const int64_t *__restrict__ prow, 
     finish_chunks(sched, nwarps, lane);
 }
 
-// ---- sliced copy of the packed stream (SELL-32) ----------------------------
-// The chunk of 32 rows is also a slice: group k of row base+l is stored at
-// soff[chunk] + 32k + l, the rows' groups interleaved and the slice padded to
-// its longest row (slots past a row's end hold zeros and are never loaded).
-// One lane owns one row: at step k the warp reads group k of its 32 rows as
-// one coalesced 512-byte window (16-byte records) and keeps the next D
-// windows in flight, each lane adds its own row's products, and the row sum
-// is already in the lane that owns the row, so no lane reduction is needed.
-// The 32 rows of a slice are adjacent rays of one angle (or adjacent pixels
-// of one image column for A'), which reach neighbouring x entries at the
-// same step, so the gathers of a step share cache sectors.
+// ---- sliced copy of the packed stream --------------------------------------
+// A chunk of 32 rows is cut into slices of R = 32/G rows with G lanes per row.
+// Within a slice the rows' groups are interleaved by step: at step k lane
+// g*G + l of the slice holds group k*G + l of its row g, all 32 slots of a
+// step stored together, and every row is padded with hole records to the
+// slice's longest row (in steps). The slices of a chunk follow one another,
+// so the chunk is one contiguous run of slots, soff[chunk] .. soff[chunk+1],
+// that the warp reads 32 slots (512 bytes of 16-byte records) per step with
+// the loads of the next D steps in flight across slice boundaries. Every
+// lane adds its own groups' products; at the end of a slice (a step count
+// the whole warp knows) the G lanes of each row are summed and the row sum
+// moves to the lane that owns the row. G = 1 is SELL-32: one lane per row,
+// no lane sums. The rows of a slice are adjacent rays of one angle (or
+// adjacent pixels of one image column for A'), so the gathers of one step
+// reach neighbouring x entries.
+constexpr uint32_t kPkHole = 1u << 27;  // padding slot of a sliced copy (no entries)
 
 // Step codes to column steps for one (S, L), in shared memory: a table
 // lookup instead of the shifts and multiply of pk_step.
@@ -426,15 +468,15 @@ template <typename VT> struct VBlk;
 template <> struct VBlk<double> {
     double2 a, b;
     __device__ __forceinline__ void ld(const double *p) {
-        a = __ldcs(reinterpret_cast<const double2 *>(p));
-        b = __ldcs(reinterpret_cast<const double2 *>(p) + 1);
+        a = ld_stream(reinterpret_cast<const double2 *>(p));
+        b = ld_stream(reinterpret_cast<const double2 *>(p) + 1);
     }
     __device__ __forceinline__ void clear() { a = b = make_double2(0.0, 0.0); }
     __device__ __forceinline__ void to(double (&o)[4]) const { o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y; }
 };
 template <> struct VBlk<float> {
     float4 a;
-    __device__ __forceinline__ void ld(const float *p) { a = __ldcs(reinterpret_cast<const float4 *>(p)); }
+    __device__ __forceinline__ void ld(const float *p) { a = ld_stream(reinterpret_cast<const float4 *>(p)); }
     __device__ __forceinline__ void clear() { a = make_float4(0.f, 0.f, 0.f, 0.f); }
     __device__ __forceinline__ void to(float (&o)[4]) const { o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; }
 };
@@ -444,7 +486,7 @@ template <> struct VBlk<float> {
 template <typename VT> struct FusedRec {  // fused 16-byte records, 2-byte values
     const uint4 *rec;
     using Raw = uint4;
-    __device__ __forceinline__ Raw load(int64_t j) const { return __ldcs(rec + j); }
+    __device__ __forceinline__ Raw load(int64_t j) const { return ld_stream(rec + j); }
     __device__ __forceinline__ static Raw none() { return make_uint4(0u, 0u, 0u, 0u); }
     __device__ __forceinline__ static void open(const Raw &r, uint2 &w, float (&v)[4]) {
         w = make_uint2(r.x, r.y);
@@ -460,7 +502,7 @@ template <typename VT> struct SplitRec {  // index words + 4 FP32/FP64 values pe
     };
     __device__ __forceinline__ Raw load(int64_t j) const {
         Raw r;
-        r.w = __ldcs(gidx + j);
+        r.w = ld_stream(gidx + j);
         r.v.ld(val + 4 * j);
         return r;
     }
@@ -476,51 +518,120 @@ template <typename VT> struct SplitRec {  // index words + 4 FP32/FP64 values pe
     }
 };
 
-// Every chunk (slice) owned by this warp: lane l sums row base+l over the
-// sliced copy and calls epi(row, sum). `lut` is the block's step-code table.
-template <typename XT, typename ACC, int D, class LD, class Epi>
+// Every chunk owned by this warp: lane l sums row base+l over the sliced
+// copy and calls epi(row, sum). A chunk's slot offset carries log2 of its
+// lanes per row G in its low bits (offsets are multiples of 32), so G may
+// differ from chunk to chunk; GF = 1 compiles the copy whose chunks all have
+// G = 1 (no slices to track, no lane sums), GF = 0 reads G per chunk. With
+// PF the gathers of step t+1 are issued before the products of step t, so a
+// warp has two steps of gathers in flight (for vectors that miss L1). `lut`
+// is the block's step-code table.
+template <typename XT, typename ACC, int D, int GF, int PF, class LD, class Epi>
 __device__ __forceinline__ void chunk_rows_sliced(const int64_t *__restrict__ prow,
                                                   const int64_t *__restrict__ soff, int32_t m,
                                                   const LD &ldr, const int4 *__restrict__ gside,
                                                   const int *lut, const XT *__restrict__ x,
                                                   Epi &epi, unsigned *sched) {
+    constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t nchunks = ((int64_t)m + 31) >> 5;
+    // products of one slot: the group's values and its gathered x (zeros
+    // past the group's entries and for holes)
+    auto gather = [&](const typename LD::Raw &r, ACC (&v)[4], ACC (&xv)[4]) {
+        uint2 w;
+        LD::open(r, w, v);
+        xv[0] = xv[1] = xv[2] = xv[3] = (ACC)0;
+        if (!(w.y & kPkHole)) {
+            int cc[4];
+            pk_decode_lut(w, gside, lut, cc);
+            const int cnt = (int)((w.y >> 24) & 3u);  // entries in the group - 1
+            xv[0] = (ACC)__ldg(x + cc[0]);
+#pragma unroll
+            for (int q = 1; q < 4; ++q)
+                if (q <= cnt) xv[q] = (ACC)__ldg(x + cc[q]);
+        }
+    };
     for (int64_t ch = sched ? next_chunk(sched, 0, nwarps, lane) : warp; ch < nchunks;
          ch = next_chunk(sched, ch, nwarps, lane)) {
+        const int64_t o0 = __ldg(soff + ch), o1 = __ldg(soff + ch + 1);
+        const int lg = GF == 1 ? 0 : (int)(o0 & 7);
+        const int G = 1 << lg, R = 32 >> lg;  // lanes per row, rows per slice
         const int64_t row = (ch << 5) + lane;
         const int ng = row < m ? (int)(__ldg(prow + row + 1) - __ldg(prow + row)) : 0;
-        const int64_t s0 = __ldg(soff + ch) + lane;
-        const int len = (int)((__ldg(soff + ch + 1) - __ldg(soff + ch)) >> 5);  // slice length
+        const int steps = (ng + G - 1) >> lg;  // steps of row base+lane
+        const int64_t s0 = (o0 & ~(int64_t)31) + lane;
+        const int T = (int)(((o1 & ~(int64_t)31) - (o0 & ~(int64_t)31)) >> 5);  // chunk steps
+        // steps of slice i: the longest of its R rows
+        auto slice_steps = [&](int i) -> int {
+            return (int)__reduce_max_sync(FULL, (unsigned)__shfl_sync(FULL, steps, i * R + (lane & (R - 1))));
+        };
         typename LD::Raw ring[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) ring[k] = k < ng ? ldr.load(s0 + 32 * k) : LD::none();
-        ACC acc = 0;
-        for (int k0 = 0; k0 < len; k0 += D) {
+        for (int k = 0; k < D; ++k) ring[k] = k < T ? ldr.load(s0 + 32 * k) : LD::none();
+        ACC acc = 0, mine = 0;
+        int i = 0, end = 0;  // current slice and the step that ends it
+        if constexpr (GF != 1) {
+            end = slice_steps(0);
+            while (end == 0 && i < G - 1) end = slice_steps(++i);  // slices of empty rows
+        }
+        ACC v[4] = {0, 0, 0, 0}, xv[4] = {0, 0, 0, 0};  // step t's values and gathers (PF)
+        if constexpr (PF) {
+            if (T > 0) {
+                gather(ring[0], v, xv);
+                ring[0] = D < T ? ldr.load(s0 + 32 * D) : LD::none();
+            }
+        }
+        for (int t0 = 0; t0 < T; t0 += D) {
 #pragma unroll
             for (int k = 0; k < D; ++k) {
-                const int kk = k0 + k;
-                if (kk >= len) break;
-                const typename LD::Raw cur = ring[k];
-                const int kn = kk + D;
-                ring[k] = kn < ng ? ldr.load(s0 + 32 * (int64_t)kn) : LD::none();
-                if (kk < ng) {
-                    uint2 w;
-                    ACC v[4];
-                    LD::open(cur, w, v);
-                    int cc[4];
-                    pk_decode_lut(w, gside, lut, cc);
-                    const int cnt = (int)((w.y >> 24) & 3u);  // entries in the group - 1
-                    acc += (ACC)__ldg(x + cc[0]) * v[0];
+                const int t = t0 + k;
+                if (t >= T) break;
+                if constexpr (PF) {
+                    ACC vn[4] = {0, 0, 0, 0}, xn[4] = {0, 0, 0, 0};
+                    const int kn = (k + 1) % D;  // ring slot of step t+1 (fixed once unrolled)
+                    if (t + 1 < T) {
+                        gather(ring[kn], vn, xn);
+                        ring[kn] = t + 1 + D < T ? ldr.load(s0 + 32 * (int64_t)(t + 1 + D)) : LD::none();
+                    }
 #pragma unroll
-                    for (int t = 1; t < 4; ++t)
-                        if (t <= cnt) acc += (ACC)__ldg(x + cc[t]) * v[t];
+                    for (int q = 0; q < 4; ++q) acc += xv[q] * v[q];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        v[q] = vn[q];
+                        xv[q] = xn[q];
+                    }
+                } else {
+                    const typename LD::Raw cur = ring[k];
+                    ring[k] = t + D < T ? ldr.load(s0 + 32 * (int64_t)(t + D)) : LD::none();
+                    uint2 w;
+                    LD::open(cur, w, v);
+                    if (!(w.y & kPkHole)) {
+                        int cc[4];
+                        pk_decode_lut(w, gside, lut, cc);
+                        const int cnt = (int)((w.y >> 24) & 3u);  // entries in the group - 1
+                        acc += (ACC)__ldg(x + cc[0]) * v[0];
+#pragma unroll
+                        for (int q = 1; q < 4; ++q)
+                            if (q <= cnt) acc += (ACC)__ldg(x + cc[q]) * v[q];
+                    }
+                }
+                if constexpr (GF != 1) {
+                    if (t + 1 == end) {  // slice i done: sum each row's G lanes
+                        for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+                        const ACC r = __shfl_sync(FULL, acc, ((lane - i * R) & (R - 1)) << lg);
+                        if (lane >= i * R && lane < i * R + R) mine = r;
+                        acc = 0;
+                        int add = 0;
+                        while (add == 0 && i < G - 1) add = slice_steps(++i);
+                        end += add;
+                    }
                 }
             }
         }
-        if (row < m) epi(row, acc);
+        if constexpr (GF == 1) mine = acc;
+        if (row < m) epi(row, mine);
     }
     finish_chunks(sched, nwarps, lane);
 }

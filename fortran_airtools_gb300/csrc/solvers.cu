@@ -118,27 +118,6 @@ __global__ void __launch_bounds__(256) k_sirt_update_pkf(PkArgs P, int32_t m, co
                                                          unsigned *sched) {
     chunk_rows_pkf<VT, G, NG>(P.prow, m, rec, P.gside, P.S, P.L, r, epi, sched);
 }
-// The sliced copy of the packed stream (rows.cuh, chunk_rows_sliced): one
-// lane per row, D steps of 32 slots in flight per warp; LD is the slot loader.
-struct SlArgs {
-    const int64_t *prow, *soff;
-    const int4 *gside;
-    int S, L;
-};
-template <class LD, int D, typename XT, typename ACC, class Epi>
-__global__ void __launch_bounds__(256) k_sirt_resid_sl(SlArgs P, int32_t m, LD ldr, const XT *x,
-                                                       Epi epi, unsigned *sched) {
-    __shared__ int lut[256];
-    pk_lut_fill(lut, P.S, P.L);
-    chunk_rows_sliced<XT, ACC, D>(P.prow, P.soff, m, ldr, P.gside, lut, x, epi, sched);
-}
-template <class LD, int D, typename XT, typename ACC, class Epi>
-__global__ void __launch_bounds__(256) k_sirt_update_sl(SlArgs P, int32_t m, LD ldr, const XT *r,
-                                                        Epi epi, unsigned *sched) {
-    __shared__ int lut[256];
-    pk_lut_fill(lut, P.S, P.L);
-    chunk_rows_sliced<XT, ACC, D>(P.prow, P.soff, m, ldr, P.gside, lut, r, epi, sched);
-}
 template <int G, int NG>
 __global__ void __launch_bounds__(256) k_sirt_resid_pk64(PkArgs P, int32_t m, const double *v,
                                                          const double *x, EpiResidF64 epi,
@@ -314,18 +293,6 @@ int elem_grid(int64_t n) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, cap));
 }
 
-// Grid for a chunk kernel: resident blocks on every SM, no more than the
-// chunks need, and never more than the partial-sum slots.
-template <class K>
-int chunk_grid(K kernel, int64_t m) {
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0);
-    if (occ < 1) occ = 1;
-    int64_t need = (((int64_t)m + 31) / 32 + 7) / 8;
-    int64_t g = std::min<int64_t>((int64_t)sm_count() * occ, std::max<int64_t>(need, 1));
-    return (int)std::min<int64_t>(g, kReduceBlocks);
-}
-
 #define FAIR_G_DISPATCH(G, CALL)                 \
     switch (G) {                                 \
         case 4: { constexpr int g_ = 4; CALL; } break;   \
@@ -333,29 +300,6 @@ int chunk_grid(K kernel, int64_t m) {
         case 32: { constexpr int g_ = 32; CALL; } break; \
         default: { constexpr int g_ = 8; CALL; } break;  \
     }
-
-// Sliced passes (layout codes 5 and 6: 2 or 4 steps in flight).
-template <int PASS, class LD, typename XT, typename ACC, class Epi>
-void sliced_pass(int code, const DevCSR &M, const LD &ldr, const XT *x, const Epi &e,
-                 unsigned *sched, cudaStream_t s) {
-    const SlArgs P{M.prow.as<int64_t>(), M.soff.as<int64_t>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
-    const int32_t m = M.m;
-    if constexpr (PASS == 1) {
-        if (code == 6)
-            k_sirt_resid_sl<LD, 4, XT, ACC, Epi><<<chunk_grid(k_sirt_resid_sl<LD, 4, XT, ACC, Epi>, m), 256, 0, s>>>(
-                P, m, ldr, x, e, sched);
-        else
-            k_sirt_resid_sl<LD, 2, XT, ACC, Epi><<<chunk_grid(k_sirt_resid_sl<LD, 2, XT, ACC, Epi>, m), 256, 0, s>>>(
-                P, m, ldr, x, e, sched);
-    } else {
-        if (code == 6)
-            k_sirt_update_sl<LD, 4, XT, ACC, Epi><<<chunk_grid(k_sirt_update_sl<LD, 4, XT, ACC, Epi>, m), 256, 0, s>>>(
-                P, m, ldr, x, e, sched);
-        else
-            k_sirt_update_sl<LD, 2, XT, ACC, Epi><<<chunk_grid(k_sirt_update_sl<LD, 2, XT, ACC, Epi>, m), 256, 0, s>>>(
-                P, m, ldr, x, e, sched);
-    }
-}
 
 }  // namespace
 
@@ -393,33 +337,8 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
     const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
     const int G = M.sirt_lanes[S.prec];
     if (code >= 5) {
-        // the sliced copy: fused records of the 2-byte forms, split FP32 slots
-        const uint4 *sl = sizeof(VT) != 2 ? nullptr
-                          : S.prec == FAIR_PREC_F16 ? (M.hassf16 ? M.sf16.as<uint4>() : nullptr)
-                                                    : (M.hassfq ? M.sfq.as<uint4>() : nullptr);
-        const bool ok = pvals && M.hassl &&
-                        (sizeof(VT) == 2 ? sl != nullptr
-                                         : std::is_same<VT, float>::value && M.hassidx && M.hassv32);
-        if (ok) {
-            if (pass == 1) {
-                EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
-                if constexpr (sizeof(VT) == 2)
-                    sliced_pass<1, FusedRec<VT>, float, float>(code, M, FusedRec<VT>{sl}, S.x32, e, S.sched, s);
-                else if constexpr (std::is_same<VT, float>::value)
-                    sliced_pass<1, SplitRec<float>, float, float>(
-                        code, M, SplitRec<float>{M.sidx.as<uint2>(), M.sv32.as<float>()}, S.x32, e, S.sched, s);
-            } else {
-                EpiUpdateLP e{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale};
-                const float *r = (const float *)S.r;
-                if constexpr (sizeof(VT) == 2)
-                    sliced_pass<2, FusedRec<VT>, float, float>(code, M, FusedRec<VT>{sl}, r, e, S.sched, s);
-                else if constexpr (std::is_same<VT, float>::value)
-                    sliced_pass<2, SplitRec<float>, float, float>(
-                        code, M, SplitRec<float>{M.sidx.as<uint2>(), M.sv32.as<float>()}, r, e, S.sched, s);
-            }
-            return;
-        }
-        code = code == 6 ? 2 : 1;  // the packed stream's lane layout instead
+        if (sirt_pass_sliced(S, M, pass, code, s)) return;
+        code = (code & 1) ? 1 : 2;  // no sliced copy: the packed stream's lane layout
     }
     if (code >= 3 && (!fused || sizeof(VT) != 2)) code -= 2;
     if (code >= 1 && !pvals) code = 0;
@@ -478,17 +397,7 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
             const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S,
                            M.pk_L};
             const double *pv = M.pv64.as<double>();
-            if (NG >= 5 && M.hassl && M.hassidx && M.hassv64) {
-                const SplitRec<double> ld{M.sidx.as<uint2>(), M.sv64.as<double>()};
-                if (pass == 1)
-                    sliced_pass<1, SplitRec<double>, double, double>(
-                        NG, M, ld, S.x, EpiResidF64{S.b, S.Minv, (double *)S.r}, S.sched, s);
-                else
-                    sliced_pass<2, SplitRec<double>, double, double>(
-                        NG, M, ld, (const double *)S.r, EpiUpdateF64{S.D, S.x, S.omg, S.lb, S.ub, S.bmode},
-                        S.sched, s);
-                return;
-            }
+            if (NG >= 5 && sirt_pass_sliced(S, M, pass, NG, s)) return;
             if (NG > 2) NG = 2 - (NG & 1);  // 3, 5 -> 1 group per lane; 4, 6 -> 2
             if (pass == 1) {
                 EpiResidF64 e{S.b, S.Minv, (double *)S.r};
@@ -542,9 +451,10 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
 }
 
 // The derived value copies (and packed index streams) a reduced-precision
-// SIRT needs on A and A'. With `all` (the autotuner) every layout of the form
-// is built; otherwise the ones the passes are set to read. `sliced` = false
-// leaves out the sliced copies.
+// SIRT needs on A and A'. With `all` (the autotuner) the packed layouts of
+// the form are built; otherwise the ones the passes are set to read. Sliced
+// copies are built only for a pass set to read one (the autotuner builds its
+// own candidates); `sliced` = false leaves them out.
 int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool all, bool sliced) {
     if (prec != FAIR_PREC_F64) {
         FAIR_TRY(csr_make_lowprec(A, prec, s));
@@ -559,8 +469,10 @@ int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool all, b
         FAIR_TRY(csr_make_packed(AT, prec, s));
         FAIR_TRY(csr_make_fused(A, prec, s));
         FAIR_TRY(csr_make_fused(AT, prec, s));
-        if (sliced && (all || A.sirt_groups[prec] >= 5)) FAIR_TRY(csr_make_sliced(A, prec, s));
-        if (sliced && (all || AT.sirt_groups[prec] >= 5)) FAIR_TRY(csr_make_sliced(AT, prec, s));
+        if (sliced && A.sirt_groups[prec] >= 5)
+            FAIR_TRY(csr_make_sliced(A, prec, A.sirt_lanes[prec], s));
+        if (sliced && AT.sirt_groups[prec] >= 5)
+            FAIR_TRY(csr_make_sliced(AT, prec, AT.sirt_lanes[prec], s));
     }
     return FAIR_OK;
 }
@@ -575,59 +487,72 @@ int sirt_iterations(const SirtDev &S, int K, cudaStream_t s) {
     return FAIR_OK;
 }
 
+// True when some form of M is set to read its sliced copy.
+static bool uses_sliced(const DevCSR &M) {
+    for (int g : M.sirt_groups)
+        if (g >= 5) return true;
+    return false;
+}
+
 int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_t s,
                   float *ms_best) {
     FAIR_TRY(sirt_make_forms(A, AT, S.prec, s, true));
     FAIR_TRY(sirt_prepare_shadow(S, s));
-    static const int lanes[4] = {4, 8, 16, 32};
     cudaEvent_t ev[2];
     for (auto &e : ev) FAIR_CUDA(cudaEventCreate(&e));
     int st = FAIR_OK;
     for (int pass = 1; pass <= 2 && st == FAIR_OK; ++pass) {
         DevCSR &M = pass == 1 ? A : AT;
-        // groups per lane and step on the packed stream (1, 2), or 0: the CSR
         const bool pk = M.haspk && packed_enabled() &&
                         (S.prec != FAIR_PREC_F64 || M.hasp64);
         const bool fu = pk && (S.prec == FAIR_PREC_F16 ? M.hasf16 : S.prec == FAIR_PREC_Q16 && M.hasfq);
-        // the sliced copy of the form
-        const bool sw = pk && M.hassl &&
-                        (S.prec == FAIR_PREC_F64   ? M.hassidx && M.hassv64
-                         : S.prec == FAIR_PREC_F32 ? M.hassidx && M.hassv32
-                         : S.prec == FAIR_PREC_F16 ? M.hassf16
-                                                   : M.hassfq);
-        int best_g = M.sirt_lanes[S.prec], best_ng = M.sirt_groups[S.prec];
+        // candidates {layout code, lanes per row}: the CSR (0), the packed
+        // stream (1, 2), the fused records (3, 4) with 4-32 lanes per row;
+        // the sliced copy (5-8) with 1-8, or 0 (per chunk)
+        struct Cand { int code, lanes; };
+        Cand cand[48];
+        int nc = 0;
+        for (int code = 0; code <= 4; ++code) {
+            if ((code >= 1 && !pk) || (code >= 3 && !fu)) continue;
+            for (int g : {4, 8, 16, 32}) cand[nc++] = {code, g};
+        }
+        if (pk && (S.prec == FAIR_PREC_F64 || S.prec == FAIR_PREC_F32 || fu))
+            for (int g : {0, 1, 2, 4, 8})
+                for (int code : {5, 6, 7, 8}) cand[nc++] = {code, g};
+        int best_g = M.sirt_lanes[S.prec], best_code = M.sirt_groups[S.prec];
         float best_ms = -1.f;
+        float t[48];
         // two rounds over the candidates; each keeps its faster round
-        float t[7][4];
         for (int round = 0; round < 2 && st == FAIR_OK; ++round)
-            for (int ng = 0; ng <= 6 && st == FAIR_OK; ++ng) {
-                if (ng >= 1 && ng <= 2 && !pk) continue;
-                if (ng >= 3 && ng <= 4 && !fu) continue;
-                if (ng >= 5 && !sw) continue;
-                // lanes per row do not matter to the sliced copy: one candidate
-                for (int c = 0; c < (ng >= 5 ? 1 : 4) && st == FAIR_OK; ++c) {
-                    M.sirt_lanes[S.prec] = ng >= 5 ? best_g : lanes[c];
-                    M.sirt_groups[S.prec] = ng;
-                    sirt_pass(S, pass, s);  // warm-up
-                    cudaEventRecord(ev[0], s);
-                    for (int r = 0; r < reps; ++r) sirt_pass(S, pass, s);
-                    cudaEventRecord(ev[1], s);
-                    cudaError_t e = cudaEventSynchronize(ev[1]);
-                    if (e != cudaSuccess) { st = cuda_fail(e, "autotune", __FILE__, __LINE__); break; }
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, ev[0], ev[1]);
-                    ms /= reps;
-                    float &tc = t[ng][c];
-                    tc = round == 0 ? ms : std::min(tc, ms);
-                    if (round == 1 && (best_ms < 0.f || tc < best_ms)) {
-                        best_ms = tc;
-                        best_g = M.sirt_lanes[S.prec];
-                        best_ng = ng;
-                    }
+            for (int i = 0; i < nc && st == FAIR_OK; ++i) {
+                const Cand c = cand[i];
+                if (c.code >= 5) {
+                    st = csr_make_sliced(M, S.prec, c.lanes, s);
+                    if (st != FAIR_OK) break;
+                    if (!M.hassl) { t[i] = -1.f; continue; }  // no sliced copy for this matrix
+                }
+                M.sirt_lanes[S.prec] = c.lanes;
+                M.sirt_groups[S.prec] = c.code;
+                sirt_pass(S, pass, s);  // warm-up
+                cudaEventRecord(ev[0], s);
+                for (int r = 0; r < reps; ++r) sirt_pass(S, pass, s);
+                cudaEventRecord(ev[1], s);
+                cudaError_t e = cudaEventSynchronize(ev[1]);
+                if (e != cudaSuccess) { st = cuda_fail(e, "autotune", __FILE__, __LINE__); break; }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[0], ev[1]);
+                ms /= reps;
+                t[i] = round == 0 ? ms : std::min(t[i], ms);
+                if (round == 1 && (best_ms < 0.f || t[i] < best_ms)) {
+                    best_ms = t[i];
+                    best_g = c.lanes;
+                    best_code = c.code;
                 }
             }
         M.sirt_lanes[S.prec] = best_g;
-        M.sirt_groups[S.prec] = best_ng;
+        M.sirt_groups[S.prec] = best_code;
+        if (st == FAIR_OK && best_code >= 5) st = csr_make_sliced(M, S.prec, best_g, s);
+        if (!uses_sliced(M)) M.drop_sliced();  // free the copies no pass reads
         if (ms_best) ms_best[pass - 1] = best_ms;
     }
     for (auto &e : ev) cudaEventDestroy(e);

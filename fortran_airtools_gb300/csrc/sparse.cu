@@ -390,15 +390,6 @@ __global__ void __launch_bounds__(256) k_spmv_lp(const int64_t *rowptr, int32_t 
     chunk_rows<VT, float, float, G>(rowptr, m, col, v, x, epi, sched);
 }
 
-template <class K>
-int chunk_grid(K kernel, int64_t m) {
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0);
-    if (occ < 1) occ = 1;
-    int64_t need = (((int64_t)m + 31) / 32 + 7) / 8;
-    return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, need));
-}
-
 int grid_for(int threads, int64_t work_items, int per_sm = 8) {
     int64_t b = (work_items + threads - 1) / threads;
     int64_t cap = (int64_t)sm_count() * per_sm;

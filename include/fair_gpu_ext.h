@@ -52,25 +52,31 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
 
 /* Autotuner of the SIRT passes (no reference counterpart): after
  * fair_sirt_prepare, times each pass over A and A' on every layout the
- * matrix has (reps launches each, CUDA events on the handle's stream), and
- * keeps the fastest for the handle's current precision. config (may be NULL)
- * receives {lanes A, lanes A', layout A, layout A'}. Layout codes:
- *   0     the CSR (int32 columns + values), lanes per row 4, 8, 16 or 32;
+ * matrix has and every lanes-per-row choice (reps launches each, CUDA events
+ * on the handle's stream), and keeps the fastest for the handle's current
+ * precision. config (may be NULL) receives {lanes A, lanes A', layout A,
+ * layout A'}. Layout codes:
+ *   0     the CSR (int32 columns + values), 4, 8, 16 or 32 lanes per row;
  *   1, 2  the packed index stream with padded values, that many groups of 4
  *         entries per lane and step;
  *   3, 4  the fused 16-byte records {index word, 4 values} of the 2-byte
  *         forms (f16, q16), 1 or 2 records per lane and step;
- *   5, 6  the packed stream (fused records for the 2-byte forms) walked
- *         linearly, one group per lane, 2 or 4 windows of 32 groups in flight
- *         per warp (lanes per row unused).
+ *   5, 6  the sliced copy of the packed stream (fused records for the 2-byte
+ *         forms): slices of 32/G rows with G = 1, 2, 4 or 8 lanes per row,
+ *         the groups of a slice interleaved by step, 2 or 4 steps of 32 slots
+ *         in flight per warp; lanes per row 0 chooses G per chunk of 32 rows
+ *         from the rows' column steps (8 when most steps are +-1, else 1);
+ *   7, 8  as 5, 6 with the gathers of x issued one step ahead.
  * A code whose layout the matrix lacks falls back to the nearest one it has.
  * d_b as in fair_sirt_run_device; d_x is scratch (overwritten). */
 int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
                        int32_t *config);
 
 /* Sets {lanes A, lanes A', layout A, layout A'} of the SIRT passes for the
- * handle's current precision: lanes per row 4, 8, 16 or 32; layout codes 0-6
- * as listed at fair_sirt_autotune. No reference counterpart. */
+ * handle's current precision: layout codes 0-8 as listed at
+ * fair_sirt_autotune, with 4, 8, 16 or 32 lanes per row for codes 0-4 and 0,
+ * 1, 2, 4 or 8 for codes 5-8 (else FAIR_ERR_ARG). No reference
+ * counterpart. */
 int fair_sirt_set_lanes(fair_csr h, const int32_t *config);
 
 /* Packed index stream of A (which = 0) or A' (which = 1), built by the first

@@ -1,10 +1,13 @@
-"""The sliced copy (SELL-32) of the packed stream (layout codes 5 and 6): one
-lane per row, group k of the 32 rows of a chunk read together, 2 or 4 steps in
-flight. It holds the same values as the CSR layout, so the two iterates differ
-only by summation order: FP64 within 1e-12 of each other (and 1e-10 of the
-oracle), the FP32-accumulating forms within 2e-6 of each other. The ragged
-matrix mixes, inside one chunk, empty rows, rows of 1-5 entries and rows
-spanning hundreds of groups, and has chunks whose rows are all empty."""
+"""The sliced copy of the packed stream (layout codes 5-8): slices of
+32/G rows with G = 1, 2, 4 or 8 lanes per row (G = 0: chosen per chunk of 32
+rows), the groups of a slice interleaved by step, 2 or 4 steps of 32 slots in
+flight per warp (codes 7, 8: with the gathers of x one step ahead). It holds
+the same values as the CSR layout, so the two iterates differ only by
+summation order: FP64 within 1e-12 of each other (and 1e-10 of the oracle),
+the FP32-accumulating forms within 2e-6 of each other. The ragged matrix
+mixes, inside one slice, empty rows, rows of 1-5 entries and rows spanning
+hundreds of groups, and has chunks whose rows are all empty; padding slots
+(holes) must add nothing."""
 import ctypes as C
 
 import numpy as np
@@ -58,11 +61,12 @@ def ragged(fair, oracle):
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32", "f16", "q16"])
-@pytest.mark.parametrize("code", [5, 6])
-def test_sliced_ragged_rows(ragged, fair, oracle, prec, code):
+@pytest.mark.parametrize("code", [5, 6, 7, 8])
+@pytest.mark.parametrize("G", [0, 1, 2, 4, 8])
+def test_sliced_ragged_rows(ragged, fair, oracle, prec, code, G):
     A, R, b = ragged
     o = fair.airms.options(lbound=0.0)
-    xs = run(fair, A, b, prec, (8, 8, code, code), "cimmino", 15, o)
+    xs = run(fair, A, b, prec, (G, G, code, code), "cimmino", 15, o)
     assert A.packed_info()["has"] and A.packed_info()["sliced"]
     xc = run(fair, A, b, prec, (8, 8, 0, 0), "cimmino", 15, o)
     assert np.all(np.isfinite(xs))
@@ -92,7 +96,8 @@ def fan64(fair, oracle):
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32", "f16", "q16"])
-@pytest.mark.parametrize("cfg", [(8, 8, 5, 6), (8, 8, 6, 5)])
+@pytest.mark.parametrize("cfg", [(1, 8, 5, 6), (8, 1, 6, 5), (2, 4, 6, 6), (4, 2, 5, 5), (0, 0, 6, 6),
+                                 (8, 1, 7, 8), (1, 0, 8, 7)])
 @pytest.mark.parametrize("case", ["par96", "fan64"])
 def test_sliced_geometry(request, fair, oracle, case, prec, cfg):
     A, R, b = request.getfixturevalue(case)
@@ -102,3 +107,15 @@ def test_sliced_geometry(request, fair, oracle, case, prec, cfg):
     assert rel_err(xs, xc) < TOL_SAME[prec]
     xr = oracle.sirt("sart", R, b, 20, opts=oracle.options(lbound=0.0, ubound=1.0))
     assert rel_err(xs, xr) < TOL_ORACLE[prec]
+
+
+def test_sliced_lanes_checked(par96, fair):
+    """Codes 5-8 take 0 (per chunk), 1, 2, 4 or 8 lanes per row; codes 0-4
+    take 4-32."""
+    from fortran_airtools_gb300._clib import check, lib
+    A = par96[0]
+    for bad in [(16, 8, 5, 1), (8, 2, 1, 0), (8, 8, 9, 1), (3, 8, 6, 1)]:
+        with pytest.raises(fair.FairError):
+            check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(*bad)))
+    check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(1, 32, 5, 0)))
+    check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, 0, 0)))
