@@ -348,7 +348,8 @@ def run_ours(args):
     on_pk = bool(pk and pk[dom - 1])
     code = (head["pass_config"]["groups_per_lane"][dom - 1] if head.get("pass_config")
             else 0 if hp == "f64" else 1)  # the library's default layouts
-    kname = {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kernel_suffix(hp, code, on_pk)
+    kname = ("k_tl_partials" if dom == 1 and code >= 9 and on_pk else
+             {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kernel_suffix(hp, code, on_pk))
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9

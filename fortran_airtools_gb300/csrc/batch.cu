@@ -346,6 +346,7 @@ int enqueue_iterations(fair_batch_s *B, int K, cudaStream_t s) {
 // Keep of a problem's matrices only what the batch's passes read.
 void compact(DevCSR &M, int prec) {
     M.drop_sliced();
+    M.tl.release();
     M.v32.release(); M.v16.release(); M.vq.release();
     M.has32 = M.has16 = M.hasq = false;
     if (prec == FAIR_PREC_F64) {

@@ -63,8 +63,19 @@ void DevCSR::drop_sliced() {
     hassl = hassidx = hassv64 = hassv32 = hassf16 = hassfq = false;
 }
 
+void DevCSR::Tiled::release() {
+    segbase.release(); soff.release(); pslot.release(); units.release(); idx.release();
+    v64.release(); v32.release(); r16.release(); rq.release(); part.release();
+    sstart.release(); send.release();
+    T = N = ntr = 0;
+    nseg = nchunks = nslots = 0;
+    nunits = 0;
+    has_idx = has_v64 = has_v32 = has_r16 = has_rq = false;
+}
+
 void DevCSR::release() {
     drop_sliced();
+    tl.release();
     rowptr.release(); col.release(); v64.release(); v32.release(); v16.release(); vq.release();
     has32 = has16 = hasq = false;
     prow.release(); gidx.release(); gside.release();
@@ -1192,11 +1203,12 @@ int fair_sirt_set_lanes(fair_csr h, const int32_t *config) {
     auto ok = [](int32_t g, int32_t code) {
         if (code >= 0 && code <= 4) return g == 4 || g == 8 || g == 16 || g == 32;
         if (code >= 5 && code <= 8) return g == 0 || g == 1 || g == 2 || g == 4 || g == 8;
+        if (code == 9 || code == 10) return g == 4 || g == 8 || g == 16 || g == 32;
         return false;
     };
     if (!ok(config[0], config[2]) || !ok(config[1], config[3])) {
-        set_detail("layout code must be 0-8, with 4, 8, 16 or 32 lanes per row for codes 0-4 "
-                   "and 0, 1, 2, 4 or 8 for codes 5-8");
+        set_detail("layout code must be 0-10, with 4, 8, 16 or 32 lanes per row for codes 0-4, "
+                   "9 and 10 and 0, 1, 2, 4 or 8 for codes 5-8");
         return FAIR_ERR_ARG;
     }
     FAIR_TRY(ensure_transpose(h));
@@ -1230,8 +1242,10 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
 
 int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches) {
     if (!h || !launches) return FAIR_ERR_NULL;
-    // one FP32 shadow conversion per call in reduced precision, two passes per iteration
-    *launches = (h->prec != FAIR_PREC_F64 ? 1 : 0) + 2 * (int64_t)K;
+    // one FP32 shadow conversion per call in reduced precision, one kernel per
+    // pass and iteration (two for a residual pass on the tiled copy)
+    const int p1 = h->A.sirt_groups[h->prec] >= 9 && h->A.tl.built() ? 2 : 1;
+    *launches = (h->prec != FAIR_PREC_F64 ? 1 : 0) + (int64_t)(p1 + 1) * K;
     return FAIR_OK;
 }
 

@@ -101,6 +101,26 @@ struct DevCSR {
     DevBuf sv64, sv32;         // 4 values per slot
     DevBuf sf16, sfq;          // fused records per slot (2-byte forms)
     bool hassidx = false, hassv64 = false, hassv32 = false, hassf16 = false, hassfq = false;
+    // Tiled copy for A x (tiled.cu): rows cut into segments by T x T tiles of
+    // the N x N image, segments stored per tile (one lane per segment, sliced
+    // by chunks of 32 segments), column indices local to the tile.
+    struct Tiled {
+        int T = 0, N = 0, ntr = 0;      // tile side, image side, tiles per image column
+        int64_t nseg = 0, nchunks = 0, nslots = 0;
+        int32_t nunits = 0;
+        DevBuf segbase;   // int64 [m+1] first segment (partial slot) of each row
+        DevBuf soff;      // int64 [nchunks+1] slot offsets of the chunks
+        DevBuf pslot;     // int32 [nchunks*32] segment of each chunk lane (-1: none)
+        DevBuf units;     // int4 [nunits] {tile, first chunk, end chunk, 0}
+        DevBuf idx;       // uint2 [nslots] four local indices (FP32, FP64 forms)
+        DevBuf v64, v32;  // values per slot
+        DevBuf r16, rq;   // fused records {local indices, 2-byte values} (f16, q16)
+        DevBuf sstart, send;  // int64 [nseg] entry range of each segment (value fills)
+        bool has_idx = false, has_v64 = false, has_v32 = false, has_r16 = false, has_rq = false;
+        DevBuf part;      // partial sums [nseg] (8 bytes each)
+        bool built() const { return T > 0; }
+        void release();
+    } tl;
     void drop_sliced();
     void release();
     bool empty() const { return rowptr.p == nullptr; }
@@ -177,6 +197,12 @@ int sirt_iterations(const SirtDev &S, int K, cudaStream_t s);
 // One SIRT pass (1: residual over A, 2: update over A') with the forms
 // already made; enqueues one kernel.
 void sirt_pass(const SirtDev &S, int pass, cudaStream_t s);
+// Tiled copy of a ray matrix for A x (tiled.cu; needs n = N^2 and the
+// reduced-precision copy of `prec`); does nothing when n is not a square.
+int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s);
+// Pass 1 of SIRT on the tiled copy (layout code 9; two kernels); false when
+// the matrix has no tiled copy of the form.
+bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int code, cudaStream_t s);
 // One SIRT pass over the sliced copy (layout codes 5-8, sirt_sliced.cu);
 // false when the matrix has no sliced copy of the form.
 bool sirt_pass_sliced(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s);

@@ -569,6 +569,7 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
     A.hasq = false;
     A.hasp64 = A.hasp32 = A.hasp16 = A.haspq = A.hasf16 = A.hasfq = false;
     A.hassv64 = A.hassv32 = A.hassf16 = A.hassfq = false;
+    A.tl.has_v64 = A.tl.has_v32 = A.tl.has_r16 = A.tl.has_rq = false;
     return FAIR_OK;
 }
 

@@ -1,0 +1,571 @@
+// tiled.cu -- A x on a copy of a ray matrix cut by image tiles (layout code 9
+// of the residual pass of SIRT, AIRMs.f90:1089-1110).
+//
+// The columns of a ray matrix are the pixels of an N x N image (column j =
+// c*N + r). On the row layouts the x entries a warp gathers are scattered
+// along whole rays, so half of them miss L1 and each costs a 32-byte sector
+// from L2: more L2-to-SM bytes than the matrix itself. Here every row is cut
+// into segments, one per T x T tile of the image that the ray crosses (a
+// convex tile is crossed once, so a segment is a run of the row's entries).
+// The segments of a tile are sorted by length (longest first) and stored in
+// chunks of 32, one lane per segment, slot k of lane l at soff[chunk] + 32k +
+// l (the sliced layout of rows.cuh with G = 1); a slot holds 4 entries as
+// 16-bit indices into the tile's shared-memory copy (column stride T + 1, so
+// that steps along rows and columns fall in different banks) plus their
+// values. Padding entries and slots point at a zero cell with value 0.
+// A work unit is a run of chunks of one tile: a CTA copies the tile of x into
+// shared memory once and its warps take the unit's chunks, every lane summing
+// its segment into one partial (FP32, or FP64 for the FP64 form) stored at
+// the segment's slot in row order; a second kernel adds each row's partials
+// in that fixed order and applies the residual epilogue, so the result does
+// not depend on scheduling.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fair_internal.cuh"
+#include "rows.cuh"
+#include "sirt_epi.cuh"
+
+namespace fair {
+
+namespace {
+
+constexpr int kTile = 128;          // tile side T (local indices < T*(T+1) + 1 < 2^16)
+constexpr int kUnitChunks = 128;    // chunks per work unit (the tile copy is reloaded per unit)
+constexpr int kTlThreads = 512;     // threads of a tile CTA
+
+// N with N*N = n, or 0.
+int64_t isqrt_exact(int64_t n) {
+    int64_t r = (int64_t)std::sqrt((double)n);
+    while (r * r > n) --r;
+    while ((r + 1) * (r + 1) <= n) ++r;
+    return r > 0 && r * r == n ? r : 0;
+}
+
+int tl_grid(int64_t work_items) {
+    int64_t b = (work_items + 255) / 256;
+    int64_t cap = (int64_t)sm_count() * 8;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, cap));
+}
+
+__device__ __forceinline__ int tile_of(int32_t col, int N, int T, int ntr) {
+    const int c = col / N, r = col - c * N;
+    return (c / T) * ntr + r / T;
+}
+
+// Segments per row (one warp per row): runs of entries in one tile.
+__global__ void k_tl_count(const int64_t *rowptr, int32_t m, const int32_t *col, int N, int T,
+                           int ntr, int32_t *nseg) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < m; row += nw) {
+        const int64_t s = rowptr[row], e = rowptr[row + 1];
+        int carry = -1, count = 0;
+        for (int64_t k0 = s; k0 < e; k0 += 32) {
+            const int64_t k = k0 + lane;
+            const int t = k < e ? tile_of(col[k], N, T, ntr) : -2;
+            int tp = __shfl_up_sync(FULL, t, 1);
+            if (lane == 0) tp = carry;
+            count += __popc(__ballot_sync(FULL, k < e && t != tp));
+            carry = __shfl_sync(FULL, t, 31);
+        }
+        if (lane == 0) nseg[row] = count;
+    }
+}
+
+// Segment s of row `row`: tile, first entry, row (segments in row order).
+__global__ void k_tl_segs(const int64_t *rowptr, int32_t m, const int32_t *col, int N, int T,
+                          int ntr, const int64_t *segbase, int32_t *stile, int64_t *sstart,
+                          int32_t *srow) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < m; row += nw) {
+        const int64_t s = rowptr[row], e = rowptr[row + 1];
+        int64_t next = segbase[row];
+        int carry = -1;
+        for (int64_t k0 = s; k0 < e; k0 += 32) {
+            const int64_t k = k0 + lane;
+            const int t = k < e ? tile_of(col[k], N, T, ntr) : -2;
+            int tp = __shfl_up_sync(FULL, t, 1);
+            if (lane == 0) tp = carry;
+            const bool head = k < e && t != tp;
+            const unsigned hm = __ballot_sync(FULL, head);
+            if (head) {
+                const int64_t sg = next + __popc(hm & ((1u << lane) - 1u));
+                stile[sg] = t;
+                sstart[sg] = k;
+                srow[sg] = (int32_t)row;
+            }
+            next += __popc(hm);
+            carry = __shfl_sync(FULL, t, 31);
+        }
+    }
+}
+
+// Groups of 4 entries of each segment; sort key = tile, then longest first.
+__global__ void k_tl_keys(int64_t nseg, const int64_t *rowptr, const int64_t *segbase,
+                          const int32_t *stile, const int64_t *sstart, const int32_t *srow,
+                          int LB, int32_t *sglen, int32_t *key, unsigned *kcnt) {
+    for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg;
+         sg += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t row = srow[sg];
+        const int64_t end = sg + 1 < segbase[row + 1] ? sstart[sg + 1] : rowptr[row + 1];
+        const int64_t g = (end - sstart[sg] + 3) / 4;
+        sglen[sg] = (int32_t)g;
+        const int k = stile[sg] * LB + (LB - 1 - (int)(g < LB - 1 ? g : LB - 1));
+        key[sg] = k;
+        atomicAdd(kcnt + k, 1u);
+    }
+}
+
+__global__ void k_tl_scatter(int64_t nseg, const int32_t *key, unsigned long long *kpos,
+                             int32_t *perm) {
+    for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg;
+         sg += (int64_t)gridDim.x * blockDim.x)
+        perm[atomicAdd(kpos + key[sg], 1ull)] = (int32_t)sg;
+}
+
+// Slots of each chunk: 32 x its longest segment (groups).
+__global__ void k_tl_chunklen(int64_t nchunks, const int2 *chunks, const int32_t *perm,
+                              const int32_t *sglen, int32_t *cnt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nchunks; c += nw) {
+        const int2 ch = chunks[c];
+        const unsigned g = lane < ch.y ? (unsigned)sglen[perm[ch.x + lane]] : 0u;
+        const unsigned mx = __reduce_max_sync(0xffffffffu, g);
+        if (lane == 0) cnt[c] = (int32_t)(32 * mx);
+    }
+}
+
+// Segment of every chunk lane (-1 past the chunk's segments).
+__global__ void k_tl_pslot(int64_t nchunks, const int2 *chunks, const int32_t *perm,
+                           int32_t *pslot) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nchunks; c += nw) {
+        const int2 ch = chunks[c];
+        pslot[c * 32 + lane] = lane < ch.y ? perm[ch.x + lane] : -1;
+    }
+}
+
+// End entry of every segment (the next segment's start, or the row's end).
+__global__ void k_tl_ends(int64_t nseg, const int64_t *rowptr, const int64_t *segbase,
+                          const int64_t *sstart, const int32_t *srow, int64_t *send) {
+    for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg;
+         sg += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t row = srow[sg];
+        send[sg] = sg + 1 < segbase[row + 1] ? sstart[sg + 1] : rowptr[row + 1];
+    }
+}
+
+// Local index of column `col` in the shared copy of its tile.
+__device__ __forceinline__ uint32_t tl_local(int32_t col, int N, int T) {
+    const int c = col / N, r = col - c * N;
+    return (uint32_t)((c % T) * (T + 1) + r % T);
+}
+
+// The slots of every chunk (one warp per chunk, lane l = segment pslot[32c+l]):
+// slot k of a lane holds entries 4k..4k+3 of its segment. Writes the four
+// local indices of each slot (idx, may be null) and the values through `put`
+// (entries past the segment: the zero cell, source -1).
+template <class Put>
+__global__ void k_tl_fill(int64_t nchunks, const int64_t *soff, const int32_t *pslot,
+                          const int64_t *sstart, const int64_t *send, const int32_t *col, int N,
+                          int T, uint2 *idx, Put put) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t zero = (uint32_t)(T * (T + 1));
+    for (int64_t c = warp; c < nchunks; c += nw) {
+        const int64_t base = soff[c], len = (soff[c + 1] - base) >> 5;
+        const int32_t sg = pslot[c * 32 + lane];
+        const int64_t st = sg >= 0 ? sstart[sg] : 0, en = sg >= 0 ? send[sg] : 0;
+        for (int64_t k = 0; k < len; ++k) {
+            uint32_t li[4];
+            int64_t src[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t e = st + 4 * k + q;
+                const bool in = e < en;
+                li[q] = in ? tl_local(col[e], N, T) : zero;
+                src[q] = in ? e : -1;
+            }
+            const int64_t slot = base + 32 * k + lane;
+            if (idx) idx[slot] = make_uint2(li[0] | (li[1] << 16), li[2] | (li[3] << 16));
+            put(slot, li, src);
+        }
+    }
+}
+
+struct PutNone {
+    __device__ void operator()(int64_t, const uint32_t (&)[4], const int64_t (&)[4]) const {}
+};
+struct Put2B {  // fused record {indices, four 2-byte codes}
+    const uint16_t *v;
+    uint4 *rec;
+    __device__ void operator()(int64_t slot, const uint32_t (&li)[4], const int64_t (&src)[4]) const {
+        uint32_t h[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) h[q] = src[q] >= 0 ? v[src[q]] : 0u;
+        rec[slot] = make_uint4(li[0] | (li[1] << 16), li[2] | (li[3] << 16), h[0] | (h[1] << 16),
+                               h[2] | (h[3] << 16));
+    }
+};
+struct PutF32 {
+    const float *v;
+    float4 *out;
+    __device__ void operator()(int64_t slot, const uint32_t (&)[4], const int64_t (&src)[4]) const {
+        out[slot] = make_float4(src[0] >= 0 ? v[src[0]] : 0.f, src[1] >= 0 ? v[src[1]] : 0.f,
+                                src[2] >= 0 ? v[src[2]] : 0.f, src[3] >= 0 ? v[src[3]] : 0.f);
+    }
+};
+struct PutF64 {
+    const double *v;
+    double2 *out;  // two double2 per slot
+    __device__ void operator()(int64_t slot, const uint32_t (&)[4], const int64_t (&src)[4]) const {
+        out[2 * slot] = make_double2(src[0] >= 0 ? v[src[0]] : 0.0, src[1] >= 0 ? v[src[1]] : 0.0);
+        out[2 * slot + 1] = make_double2(src[2] >= 0 ? v[src[2]] : 0.0, src[3] >= 0 ? v[src[3]] : 0.0);
+    }
+};
+
+// ---- the pass ---------------------------------------------------------------
+// Slot loaders: four local indices and four values.
+template <typename VT> struct TlFused {
+    const uint4 *rec;
+    using Raw = uint4;
+    __device__ __forceinline__ Raw load(int64_t j) const { return ld_stream(rec + j); }
+    __device__ __forceinline__ static Raw none() { return make_uint4(0u, 0u, 0u, 0u); }
+    __device__ __forceinline__ static void open(const Raw &r, uint32_t (&li)[4], float (&v)[4]) {
+        li[0] = r.x & 0xFFFFu; li[1] = r.x >> 16; li[2] = r.y & 0xFFFFu; li[3] = r.y >> 16;
+        Conv2B<VT>::to(r.z, r.w, v);
+    }
+};
+template <typename VT> struct TlSplit {
+    const uint2 *idx;
+    const VT *val;
+    struct Raw {
+        uint2 w;
+        VBlk<VT> v;
+    };
+    __device__ __forceinline__ Raw load(int64_t j) const {
+        Raw r;
+        r.w = ld_stream(idx + j);
+        r.v.ld(val + 4 * j);
+        return r;
+    }
+    __device__ __forceinline__ static Raw none() {
+        Raw r;
+        r.w = make_uint2(0u, 0u);
+        r.v.clear();
+        return r;
+    }
+    __device__ __forceinline__ static void open(const Raw &r, uint32_t (&li)[4], VT (&v)[4]) {
+        li[0] = r.w.x & 0xFFFFu; li[1] = r.w.x >> 16; li[2] = r.w.y & 0xFFFFu; li[3] = r.w.y >> 16;
+        r.v.to(v);
+    }
+};
+
+struct TlArgs {
+    const int64_t *soff;
+    const int32_t *pslot;
+    const int4 *units;
+    int32_t nunits;
+    int N, T, ntr;
+};
+
+// Partial sums of all segments. Persistent CTAs take work units through
+// ctr[0] (reset by the last CTA through ctr[1] for the next launch).
+template <class LD, typename XT, typename ACC, int D>
+__global__ void __launch_bounds__(kTlThreads) k_tl_partials(TlArgs P, LD ldr,
+                                                            const XT *__restrict__ x,
+                                                            ACC *__restrict__ part, unsigned *ctr) {
+    extern __shared__ __align__(16) unsigned char tl_smem[];
+    XT *xs = reinterpret_cast<XT *>(tl_smem);
+    __shared__ int s_unit, s_chunk;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int T = P.T, N = P.N;
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = (int)atomicAdd(ctr, 1u);
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= P.nunits) break;
+        const int4 U = P.units[u];
+        const int tc = U.x / P.ntr, tr = U.x - tc * P.ntr;
+        for (int e = threadIdx.x; e < T * T; e += blockDim.x) {
+            const int lc = e / T, lr = e - lc * T;
+            const int gr = tr * T + lr, gc = tc * T + lc;
+            xs[lc * (T + 1) + lr] = (gr < N && gc < N) ? x[(int64_t)gc * N + gr] : (XT)0;
+        }
+        if (threadIdx.x == 0) {
+            xs[T * (T + 1)] = (XT)0;  // the zero cell of padding entries
+            s_chunk = U.y;
+        }
+        __syncthreads();
+        for (;;) {
+            int c = 0;
+            if (lane == 0) c = atomicAdd(&s_chunk, 1);
+            c = __shfl_sync(FULL, c, 0);
+            if (c >= U.z) break;
+            const int64_t o0 = __ldg(P.soff + c);
+            const int len = (int)((__ldg(P.soff + c + 1) - o0) >> 5);
+            const int64_t s0 = o0 + lane;
+            typename LD::Raw ring[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) ring[k] = k < len ? ldr.load(s0 + 32 * k) : LD::none();
+            ACC acc = 0;
+            for (int t0 = 0; t0 < len; t0 += D) {
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const int t = t0 + k;
+                    if (t >= len) break;
+                    const typename LD::Raw cur = ring[k];
+                    ring[k] = t + D < len ? ldr.load(s0 + 32 * (int64_t)(t + D)) : LD::none();
+                    uint32_t li[4];
+                    ACC v[4];
+                    LD::open(cur, li, v);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc += (ACC)xs[li[q]] * v[q];
+                }
+            }
+            const int ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
+            if (ps >= 0) part[ps] = acc;
+        }
+        __syncthreads();  // the tile is rewritten by the next unit
+    }
+    if (threadIdx.x == 0) {
+        const unsigned done = atomicAdd(ctr + 1, 1u);
+        if (done == gridDim.x - 1) {  // every CTA has stopped taking units
+            ctr[0] = 0u;
+            ctr[1] = 0u;
+        }
+    }
+}
+
+// Row sums of the partials (in row order) and the residual epilogue.
+template <typename ACC, class Epi>
+__global__ void k_tl_rows(int32_t m, const int64_t *__restrict__ segbase,
+                          const ACC *__restrict__ part, Epi epi) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        ACC acc = 0;
+        for (int64_t k = segbase[i]; k < segbase[i + 1]; ++k) acc += part[k];
+        epi(i, acc);
+    }
+}
+
+template <class LD, typename XT, typename ACC, class Epi>
+int launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &e,
+              unsigned *ctr, cudaStream_t s) {
+    const DevCSR::Tiled &tl = M.tl;
+    const TlArgs P{tl.soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.units.as<int4>(), tl.nunits,
+                   tl.N, tl.T, tl.ntr};
+    const size_t smem = sizeof(XT) * ((size_t)tl.T * (tl.T + 1) + 1);
+    ACC *part = tl.part.as<ACC>();
+    auto run = [&](auto kernel) -> int {
+        static thread_local bool attr_set = false;  // per instantiation
+        if (!attr_set) {
+            FAIR_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr_set = true;
+        }
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kTlThreads, smem);
+        const int grid = std::max(1, std::min(sm_count() * std::max(occ, 1), (int)tl.nunits));
+        kernel<<<grid, kTlThreads, smem, s>>>(P, ldr, x, part, ctr);
+        return FAIR_OK;
+    };
+    if (code == 10) FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 4>));
+    else FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 2>));
+    k_tl_rows<ACC, Epi><<<tl_grid(M.m), 256, 0, s>>>(M.m, tl.segbase.as<int64_t>(), part, e);
+    FAIR_CUDA(cudaGetLastError());
+    return FAIR_OK;
+}
+
+}  // namespace
+
+int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
+    if (A.m == 0 || A.nnz == 0) return FAIR_OK;
+    DevCSR::Tiled &tl = A.tl;
+    if (!tl.built()) {
+        const int64_t N = isqrt_exact(A.n);
+        if (N <= 0) return FAIR_OK;  // not an image of N x N pixels
+        const int T = kTile, ntr = (int)((N + T - 1) / T);
+        const int64_t ntiles = (int64_t)ntr * ntr;
+        const int LB = T / 2 + 2;  // length classes of the sort (segments of up to 2T entries)
+        if (ntiles * LB >= (int64_t(1) << 31)) return FAIR_OK;
+        // segments
+        TmpBuf nseg;
+        FAIR_TRY(nseg.grow(sizeof(int32_t) * ((size_t)A.m + 1)));
+        FAIR_TRY(tl.segbase.grow(sizeof(int64_t) * ((size_t)A.m + 1)));
+        k_tl_count<<<tl_grid((int64_t)A.m * 32), 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m,
+                                                              A.col.as<int32_t>(), (int)N, T, ntr,
+                                                              nseg.as<int32_t>());
+        FAIR_CUDA(cudaGetLastError());
+        FAIR_TRY(scan_counts(nseg.as<int32_t>(), A.m, tl.segbase.as<int64_t>(), s));
+        int64_t S = 0;
+        FAIR_CUDA(cudaMemcpyAsync(&S, tl.segbase.as<int64_t>() + A.m, sizeof(S),
+                                  cudaMemcpyDeviceToHost, s));
+        FAIR_CUDA(cudaStreamSynchronize(s));
+        if (S <= 0 || S >= (int64_t(1) << 31)) { tl.release(); return FAIR_OK; }
+        TmpBuf stile, sstart, srow, sglen, key, kcnt, kpos, perm;
+        FAIR_TRY(stile.grow(sizeof(int32_t) * S));
+        FAIR_TRY(sstart.grow(sizeof(int64_t) * S));
+        FAIR_TRY(srow.grow(sizeof(int32_t) * S));
+        FAIR_TRY(sglen.grow(sizeof(int32_t) * S));
+        FAIR_TRY(key.grow(sizeof(int32_t) * S));
+        FAIR_TRY(perm.grow(sizeof(int32_t) * S));
+        const int64_t nkeys = ntiles * LB;
+        FAIR_TRY(kcnt.grow(sizeof(unsigned) * (nkeys + 1)));
+        FAIR_TRY(kpos.grow(sizeof(unsigned long long) * (nkeys + 1)));
+        FAIR_CUDA(cudaMemsetAsync(kcnt.p, 0, sizeof(unsigned) * (nkeys + 1), s));
+        k_tl_segs<<<tl_grid((int64_t)A.m * 32), 256, 0, s>>>(
+            A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(), (int)N, T, ntr,
+            tl.segbase.as<int64_t>(), stile.as<int32_t>(), sstart.as<int64_t>(), srow.as<int32_t>());
+        k_tl_keys<<<tl_grid(S), 256, 0, s>>>(S, A.rowptr.as<int64_t>(), tl.segbase.as<int64_t>(),
+                                              stile.as<int32_t>(), sstart.as<int64_t>(),
+                                              srow.as<int32_t>(), LB, sglen.as<int32_t>(),
+                                              key.as<int32_t>(), kcnt.as<unsigned>());
+        FAIR_CUDA(cudaGetLastError());
+        // bucket offsets on the host (ntiles * LB counters)
+        std::vector<unsigned> hc((size_t)nkeys);
+        FAIR_CUDA(cudaMemcpyAsync(hc.data(), kcnt.p, sizeof(unsigned) * nkeys,
+                                  cudaMemcpyDeviceToHost, s));
+        FAIR_CUDA(cudaStreamSynchronize(s));
+        std::vector<unsigned long long> ho((size_t)nkeys + 1, 0ull);
+        for (int64_t k = 0; k < nkeys; ++k) ho[k + 1] = ho[k] + hc[k];
+        FAIR_CUDA(cudaMemcpyAsync(kpos.p, ho.data(), sizeof(unsigned long long) * nkeys,
+                                  cudaMemcpyHostToDevice, s));
+        k_tl_scatter<<<tl_grid(S), 256, 0, s>>>(S, key.as<int32_t>(), kpos.as<unsigned long long>(),
+                                                 perm.as<int32_t>());
+        FAIR_CUDA(cudaGetLastError());
+        // chunks of 32 segments per tile, units of kUnitChunks chunks
+        std::vector<int2> chunks;
+        std::vector<int4> units;
+        for (int64_t t = 0; t < ntiles; ++t) {
+            const int64_t a = (int64_t)ho[t * LB], b = (int64_t)ho[(t + 1) * LB];
+            const int64_t c0 = (int64_t)chunks.size();
+            for (int64_t p = a; p < b; p += 32)
+                chunks.push_back(make_int2((int)p, (int)std::min<int64_t>(32, b - p)));
+            const int64_t c1 = (int64_t)chunks.size();
+            for (int64_t c = c0; c < c1; c += kUnitChunks)
+                units.push_back(make_int4((int)t, (int)c, (int)std::min<int64_t>(c + kUnitChunks, c1), 0));
+        }
+        // most work first: units of longer segments lead within a tile already
+        const int64_t nch = (int64_t)chunks.size();
+        TmpBuf dch, ccnt;
+        FAIR_TRY(dch.grow(sizeof(int2) * std::max<int64_t>(nch, 1)));
+        FAIR_TRY(ccnt.grow(sizeof(int32_t) * (nch + 1)));
+        FAIR_TRY(tl.soff.grow(sizeof(int64_t) * (nch + 1)));
+        FAIR_TRY(tl.pslot.grow(sizeof(int32_t) * 32 * std::max<int64_t>(nch, 1)));
+        FAIR_TRY(tl.units.grow(sizeof(int4) * std::max<size_t>(units.size(), 1)));
+        FAIR_CUDA(cudaMemcpyAsync(dch.p, chunks.data(), sizeof(int2) * nch, cudaMemcpyHostToDevice, s));
+        FAIR_CUDA(cudaMemcpyAsync(tl.units.p, units.data(), sizeof(int4) * units.size(),
+                                  cudaMemcpyHostToDevice, s));
+        k_tl_chunklen<<<tl_grid(nch * 32), 256, 0, s>>>(nch, dch.as<int2>(), perm.as<int32_t>(),
+                                                         sglen.as<int32_t>(), ccnt.as<int32_t>());
+        FAIR_CUDA(cudaGetLastError());
+        FAIR_TRY(scan_counts(ccnt.as<int32_t>(), nch, tl.soff.as<int64_t>(), s));
+        int64_t nslots = 0;
+        FAIR_CUDA(cudaMemcpyAsync(&nslots, tl.soff.as<int64_t>() + nch, sizeof(nslots),
+                                  cudaMemcpyDeviceToHost, s));
+        FAIR_CUDA(cudaStreamSynchronize(s));
+        FAIR_TRY(tl.sstart.grow(sizeof(int64_t) * S));
+        FAIR_TRY(tl.send.grow(sizeof(int64_t) * S));
+        FAIR_CUDA(cudaMemcpyAsync(tl.sstart.p, sstart.p, sizeof(int64_t) * S,
+                                  cudaMemcpyDeviceToDevice, s));
+        k_tl_ends<<<tl_grid(S), 256, 0, s>>>(S, A.rowptr.as<int64_t>(), tl.segbase.as<int64_t>(),
+                                              sstart.as<int64_t>(), srow.as<int32_t>(),
+                                              tl.send.as<int64_t>());
+        k_tl_pslot<<<tl_grid(nch * 32), 256, 0, s>>>(nch, dch.as<int2>(), perm.as<int32_t>(),
+                                                      tl.pslot.as<int32_t>());
+        FAIR_CUDA(cudaGetLastError());
+        // index words (read by the FP32 and FP64 forms)
+        FAIR_TRY(tl.idx.grow(sizeof(uint2) * std::max<int64_t>(nslots, 1)));
+        k_tl_fill<PutNone><<<tl_grid(nch * 32), 256, 0, s>>>(
+            nch, tl.soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.sstart.as<int64_t>(),
+            tl.send.as<int64_t>(), A.col.as<int32_t>(), (int)N, T, tl.idx.as<uint2>(), PutNone{});
+        FAIR_CUDA(cudaGetLastError());
+        FAIR_TRY(tl.part.grow(sizeof(double) * S));
+        tl.T = T;
+        tl.N = (int)N;
+        tl.ntr = ntr;
+        tl.nseg = S;
+        tl.nchunks = nch;
+        tl.nslots = nslots;
+        tl.nunits = (int32_t)units.size();
+        tl.has_idx = true;
+        FAIR_CUDA(cudaStreamSynchronize(s));  // before the scratch buffers go
+    }
+    // the values of the form, slot by slot
+    const int64_t nch = tl.nchunks;
+    const int grid = tl_grid(nch * 32);
+    const int64_t *soff = tl.soff.as<int64_t>(), *st = tl.sstart.as<int64_t>(), *en = tl.send.as<int64_t>();
+    const int32_t *ps = tl.pslot.as<int32_t>(), *col = A.col.as<int32_t>();
+    const size_t ns = (size_t)std::max<int64_t>(tl.nslots, 1);
+    if (prec == FAIR_PREC_F64 && !tl.has_v64) {
+        FAIR_TRY(tl.v64.grow(sizeof(double) * 4 * ns));
+        k_tl_fill<PutF64><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, col, tl.N, tl.T, nullptr,
+                                                PutF64{A.v64.as<double>(), tl.v64.as<double2>()});
+        tl.has_v64 = true;
+    } else if (prec == FAIR_PREC_F32 && !tl.has_v32) {
+        FAIR_TRY(csr_make_lowprec(A, prec, s));
+        FAIR_TRY(tl.v32.grow(sizeof(float) * 4 * ns));
+        k_tl_fill<PutF32><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, col, tl.N, tl.T, nullptr,
+                                                PutF32{A.v32.as<float>(), tl.v32.as<float4>()});
+        tl.has_v32 = true;
+    } else if ((prec == FAIR_PREC_F16 && !tl.has_r16) || (prec == FAIR_PREC_Q16 && !tl.has_rq)) {
+        FAIR_TRY(csr_make_lowprec(A, prec, s));
+        const bool h = prec == FAIR_PREC_F16;
+        DevBuf &dst = h ? tl.r16 : tl.rq;
+        FAIR_TRY(dst.grow(sizeof(uint4) * ns));
+        const uint16_t *v = h ? A.v16.as<uint16_t>() : A.vq.as<uint16_t>();
+        k_tl_fill<Put2B><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, col, tl.N, tl.T, nullptr,
+                                               Put2B{v, dst.as<uint4>()});
+        (h ? tl.has_r16 : tl.has_rq) = true;
+    }
+    FAIR_CUDA(cudaGetLastError());
+    return FAIR_OK;
+}
+
+bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int code, cudaStream_t s) {
+    const DevCSR::Tiled &tl = M.tl;
+    if (!tl.built() || !S.sched) return false;  // the work-unit counters are S.sched
+    int st = FAIR_OK;
+    if (S.prec == FAIR_PREC_F64) {
+        if (!tl.has_v64) return false;
+        st = launch_tl<TlSplit<double>, double, double>(
+            M, code, TlSplit<double>{tl.idx.as<uint2>(), tl.v64.as<double>()}, S.x,
+            EpiResidF64{S.b, S.Minv, (double *)S.r}, S.sched, s);
+    } else {
+        const double scale = S.prec == FAIR_PREC_Q16 ? M.qscale : 1.0;
+        const EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
+        if (S.prec == FAIR_PREC_F32) {
+            if (!tl.has_v32) return false;
+            st = launch_tl<TlSplit<float>, float, float>(
+                M, code, TlSplit<float>{tl.idx.as<uint2>(), tl.v32.as<float>()}, S.x32, e, S.sched, s);
+        } else if (S.prec == FAIR_PREC_F16) {
+            if (!tl.has_r16) return false;
+            st = launch_tl<TlFused<__half>, float, float>(M, code, TlFused<__half>{tl.r16.as<uint4>()},
+                                                          S.x32, e, S.sched, s);
+        } else {
+            if (!tl.has_rq) return false;
+            if (M.qsigned)
+                st = launch_tl<TlFused<int16_t>, float, float>(
+                    M, code, TlFused<int16_t>{tl.rq.as<uint4>()}, S.x32, e, S.sched, s);
+            else
+                st = launch_tl<TlFused<uint16_t>, float, float>(
+                    M, code, TlFused<uint16_t>{tl.rq.as<uint4>()}, S.x32, e, S.sched, s);
+        }
+    }
+    return st == FAIR_OK;
+}
+
+}  // namespace fair

@@ -66,17 +66,22 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
  *         the groups of a slice interleaved by step, 2 or 4 steps of 32 slots
  *         in flight per warp; lanes per row 0 chooses G per chunk of 32 rows
  *         from the rows' column steps (8 when most steps are +-1, else 1);
- *   7, 8  as 5, 6 with the gathers of x issued one step ahead.
+ *   7, 8  as 5, 6 with the gathers of x issued one step ahead;
+ *   9, 10 (the residual pass over A only, for A with n = N^2 columns) the
+ *         tiled copy: rows cut into segments by 128 x 128 tiles of the image,
+ *         each tile of x staged in shared memory by the CTA that works on it,
+ *         16-bit tile-local indices, one partial sum per segment added up per
+ *         row in a second kernel; 2 or 4 steps in flight.
  * A code whose layout the matrix lacks falls back to the nearest one it has.
  * d_b as in fair_sirt_run_device; d_x is scratch (overwritten). */
 int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
                        int32_t *config);
 
 /* Sets {lanes A, lanes A', layout A, layout A'} of the SIRT passes for the
- * handle's current precision: layout codes 0-8 as listed at
- * fair_sirt_autotune, with 4, 8, 16 or 32 lanes per row for codes 0-4 and 0,
- * 1, 2, 4 or 8 for codes 5-8 (else FAIR_ERR_ARG). No reference
- * counterpart. */
+ * handle's current precision: layout codes 0-10 as listed at
+ * fair_sirt_autotune, with 4, 8, 16 or 32 lanes per row for codes 0-4, 9 and
+ * 10 (unused by 9 and 10) and 0, 1, 2, 4 or 8 for codes 5-8 (else
+ * FAIR_ERR_ARG). No reference counterpart. */
 int fair_sirt_set_lanes(fair_csr h, const int32_t *config);
 
 /* Packed index stream of A (which = 0) or A' (which = 1), built by the first

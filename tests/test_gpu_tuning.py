@@ -27,7 +27,8 @@ def prob(fair, oracle):
 @pytest.mark.parametrize("prec,tol", [("f64", 1e-10), ("f32", 1e-5), ("f16", 5e-3), ("q16", 1e-4)])
 @pytest.mark.parametrize("cfg", [(4, 32, 1, 2), (16, 4, 2, 1), (32, 16, 2, 2), (8, 8, 1, 1),
                                  (8, 4, 0, 2), (8, 8, 0, 0), (8, 4, 3, 4), (16, 32, 4, 3),
-                                 (8, 8, 5, 6), (4, 2, 6, 5), (1, 1, 5, 5), (8, 1, 7, 8)])
+                                 (8, 8, 5, 6), (4, 2, 6, 5), (1, 1, 5, 5), (8, 1, 7, 8),
+                                 (8, 1, 9, 5), (16, 8, 10, 3)])
 def test_lanes_choice(prob, fair, oracle, prec, tol, cfg):
     from fortran_airtools_gb300._clib import check, lib
     A, R, b = prob
@@ -56,8 +57,8 @@ def test_autotune(prob, fair, oracle):
         cfg = (C.c_int32 * 4)()
         check(L.fair_sirt_autotune(A.handle, d_b.data_ptr(), d_x.data_ptr(), 2, cfg))
         for lanes, code in ((cfg[0], cfg[2]), (cfg[1], cfg[3])):
-            assert code in range(9)
-            assert lanes in ((0, 1, 2, 4, 8) if code >= 5 else (4, 8, 16, 32))
+            assert code in range(11)
+            assert lanes in ((0, 1, 2, 4, 8) if 5 <= code <= 8 else (4, 8, 16, 32))
         x = fair.airms.sirt("cimmino", A, b, 15)
     finally:
         A.set_precision("f64")
