@@ -310,7 +310,24 @@ __global__ void k_check_rowptr(const int64_t *rowptr, int32_t m, int *err) {
 
 // ------------------------------------------------------------ row norms ----
 // p-norm of every row (compute_row_norms, sparse_matrices.f90:740-780): a warp
-// per row, four independent loads in flight per lane.
+// per row, four independent loads in flight per lane. P = 1 and 2 are
+// compiled with one FP64 operation per entry (|a| added; a*a fused into the
+// sum: on this part every FP64 warp instruction holds its pipe for 64
+// cycles, so the entry count of FP64 operations bounds the kernel); P = 0
+// takes p at run time.
+template <int P>
+__device__ __forceinline__ double norm_term(double acc, double a, int p) {
+    if constexpr (P == 1) return acc + fabs(a);
+    else if constexpr (P == 2) return fma(a, a, acc);
+    else {
+        a = fabs(a);
+        double t = a;
+        for (int q = 1; q < p; ++q) t *= a;
+        return acc + t;
+    }
+}
+
+template <int P>
 __global__ void k_row_norms(const int64_t *rowptr, int32_t m, const double *v, int p,
                             double *out) {
     int lane = threadIdx.x & 31;
@@ -321,20 +338,12 @@ __global__ void k_row_norms(const int64_t *rowptr, int32_t m, const double *v, i
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
         int64_t j = s + lane;
         for (; j + 96 < e; j += 128) {
-            double a[4] = {fabs(__ldcs(v + j)), fabs(__ldcs(v + j + 32)), fabs(__ldcs(v + j + 64)),
-                           fabs(__ldcs(v + j + 96))};
+            const double a[4] = {__ldcs(v + j), __ldcs(v + j + 32), __ldcs(v + j + 64),
+                                 __ldcs(v + j + 96)};
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                double t = a[u];
-                for (int q = 1; q < p; ++q) t *= a[u];
-                acc[u] += t;
-            }
+            for (int u = 0; u < 4; ++u) acc[u] = norm_term<P>(acc[u], a[u], p);
         }
-        for (; j < e; j += 32) {
-            double a = fabs(__ldcs(v + j)), t = a;
-            for (int q = 1; q < p; ++q) t *= a;
-            acc[0] += t;
-        }
+        for (; j < e; j += 32) acc[0] = norm_term<P>(acc[0], __ldcs(v + j), p);
         double sum = warp_sum((acc[0] + acc[1]) + (acc[2] + acc[3]));
         if (lane == 0) out[r] = p == 1 ? sum : (p == 2 ? sqrt(sum) : pow(sum, 1.0 / p));
     }
@@ -574,9 +583,14 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
 }
 
 int csr_row_norms(const DevCSR &A, int p, double *d_out, cudaStream_t s) {
-    if (A.m > 0)
-        k_row_norms<<<grid_for(256, (int64_t)A.m * 32), 256, 0, s>>>(
-            A.rowptr.as<int64_t>(), A.m, A.v64.as<double>(), p, d_out);
+    if (A.m > 0) {
+        const int g = grid_for(256, (int64_t)A.m * 32);
+        const int64_t *rp = A.rowptr.as<int64_t>();
+        const double *v = A.v64.as<double>();
+        if (p == 1) k_row_norms<1><<<g, 256, 0, s>>>(rp, A.m, v, p, d_out);
+        else if (p == 2) k_row_norms<2><<<g, 256, 0, s>>>(rp, A.m, v, p, d_out);
+        else k_row_norms<0><<<g, 256, 0, s>>>(rp, A.m, v, p, d_out);
+    }
     FAIR_CUDA(cudaGetLastError());
     return FAIR_OK;
 }

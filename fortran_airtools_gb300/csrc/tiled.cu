@@ -32,7 +32,7 @@ namespace fair {
 namespace {
 
 constexpr int kTile = 128;          // tile side T (local indices < T*(T+1) + 1 < 2^16)
-constexpr int kUnitChunks = 128;    // chunks per work unit (the tile copy is reloaded per unit)
+constexpr int kUnitChunks = 128;    // most chunks per work unit (the tile copy is reloaded per unit)
 constexpr int kTlThreads = 512;     // threads of a tile CTA
 
 // N with N*N = n, or 0.
@@ -446,17 +446,22 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
         k_tl_scatter<<<tl_grid(S), 256, 0, s>>>(S, key.as<int32_t>(), kpos.as<unsigned long long>(),
                                                  perm.as<int32_t>());
         FAIR_CUDA(cudaGetLastError());
-        // chunks of 32 segments per tile, units of kUnitChunks chunks
+        // chunks of 32 segments per tile; units of up to kUnitChunks chunks,
+        // fewer when that leaves under a dozen units per SM to balance
         std::vector<int2> chunks;
         std::vector<int4> units;
         for (int64_t t = 0; t < ntiles; ++t) {
             const int64_t a = (int64_t)ho[t * LB], b = (int64_t)ho[(t + 1) * LB];
-            const int64_t c0 = (int64_t)chunks.size();
             for (int64_t p = a; p < b; p += 32)
                 chunks.push_back(make_int2((int)p, (int)std::min<int64_t>(32, b - p)));
-            const int64_t c1 = (int64_t)chunks.size();
-            for (int64_t c = c0; c < c1; c += kUnitChunks)
-                units.push_back(make_int4((int)t, (int)c, (int)std::min<int64_t>(c + kUnitChunks, c1), 0));
+        }
+        const int64_t per_unit = std::max<int64_t>(
+            8, std::min<int64_t>(kUnitChunks, (int64_t)chunks.size() / ((int64_t)sm_count() * 12)));
+        for (int64_t t = 0, c0 = 0; t < ntiles; ++t) {
+            const int64_t c1 = c0 + ((int64_t)ho[(t + 1) * LB] - (int64_t)ho[t * LB] + 31) / 32;
+            for (int64_t c = c0; c < c1; c += per_unit)
+                units.push_back(make_int4((int)t, (int)c, (int)std::min<int64_t>(c + per_unit, c1), 0));
+            c0 = c1;
         }
         // most work first: units of longer segments lead within a tile already
         const int64_t nch = (int64_t)chunks.size();
