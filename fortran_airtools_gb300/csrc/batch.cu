@@ -347,6 +347,8 @@ int enqueue_iterations(fair_batch_s *B, int K, cudaStream_t s) {
 void compact(DevCSR &M, int prec) {
     M.drop_sliced();
     M.tl.release();
+    M.dl[0].release();
+    M.dl[1].release();
     M.v32.release(); M.v16.release(); M.vq.release();
     M.has32 = M.has16 = M.hasq = false;
     if (prec == FAIR_PREC_F64) {

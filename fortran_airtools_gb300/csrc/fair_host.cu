@@ -73,9 +73,21 @@ void DevCSR::Tiled::release() {
     has_idx = has_v64 = has_v32 = has_r16 = has_rq = false;
 }
 
+void DevCSR::Delta::release() {
+    soff.release(); anchor.release(); code.release(); side.release();
+    v64.release(); v32.release(); r16.release(); rq.release();
+    S = 0;
+    L = 7;
+    nslots = nesc = 0;
+    tried = built = false;
+    has_v64 = has_v32 = has_r16 = has_rq = false;
+}
+
 void DevCSR::release() {
     drop_sliced();
     tl.release();
+    dl[0].release();
+    dl[1].release();
     rowptr.release(); col.release(); v64.release(); v32.release(); v16.release(); vq.release();
     has32 = has16 = hasq = false;
     prow.release(); gidx.release(); gside.release();
@@ -1203,12 +1215,12 @@ int fair_sirt_set_lanes(fair_csr h, const int32_t *config) {
     auto ok = [](int32_t g, int32_t code) {
         if (code >= 0 && code <= 4) return g == 4 || g == 8 || g == 16 || g == 32;
         if (code >= 5 && code <= 8) return g == 0 || g == 1 || g == 2 || g == 4 || g == 8;
-        if (code == 9 || code == 10) return g == 4 || g == 8 || g == 16 || g == 32;
+        if (code >= 9 && code <= 13) return g == 4 || g == 8 || g == 16 || g == 32;
         return false;
     };
     if (!ok(config[0], config[2]) || !ok(config[1], config[3])) {
-        set_detail("layout code must be 0-10, with 4, 8, 16 or 32 lanes per row for codes 0-4, "
-                   "9 and 10 and 0, 1, 2, 4 or 8 for codes 5-8");
+        set_detail("layout code must be 0-13, with 4, 8, 16 or 32 lanes per row for codes 0-4 "
+                   "and 9-13 and 0, 1, 2, 4 or 8 for codes 5-8");
         return FAIR_ERR_ARG;
     }
     FAIR_TRY(ensure_transpose(h));

@@ -121,6 +121,26 @@ struct DevCSR {
         bool built() const { return T > 0; }
         void release();
     } tl;
+    // Delta copies (sirt_delta.cu): the sliced layout with one lane per row
+    // whose slots carry column steps from the row's previous entry instead of
+    // columns (the row's first column is its anchor). dl[0]: 4 entries per
+    // slot, a word of four 7-bit steps beside the values (FP32, FP64 forms);
+    // dl[1]: 6 entries per slot in one 16-byte record {six 5-bit steps, six
+    // 2-byte values} (f16, q16).
+    struct Delta {
+        int E = 4, bits = 7;      // entries per slot, bits per step code
+        int S = 0, L = 7;         // step code: delta = lo + hi * S, lo the low L bits
+        int64_t nslots = 0, nesc = 0;
+        bool tried = false, built = false;
+        DevBuf soff;              // int64 [chunks+1]
+        DevBuf anchor;            // int32 [m] first column of each row (0 if empty)
+        DevBuf code;              // uint32 [nslots] step words
+        DevBuf side;              // int4 [nesc*(E+3)/4] the columns of a slot without codes
+        DevBuf v64, v32;          // 4 values per slot (E = 4)
+        DevBuf r16, rq;           // records {word, six 2-byte values} (E = 6)
+        bool has_v64 = false, has_v32 = false, has_r16 = false, has_rq = false;
+        void release();
+    } dl[2];
     void drop_sliced();
     void release();
     bool empty() const { return rowptr.p == nullptr; }
@@ -203,6 +223,11 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s);
 // Pass 1 of SIRT on the tiled copy (layout code 9; two kernels); false when
 // the matrix has no tiled copy of the form.
 bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int code, cudaStream_t s);
+// Delta copy of the form (sirt_delta.cu): does nothing when too many groups
+// would need the side table.
+int csr_make_delta(DevCSR &A, int prec, cudaStream_t s);
+// A SIRT pass over the delta copy (layout codes 11, 12); false without one.
+bool sirt_pass_delta(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s);
 // One SIRT pass over the sliced copy (layout codes 5-8, sirt_sliced.cu);
 // false when the matrix has no sliced copy of the form.
 bool sirt_pass_sliced(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s);

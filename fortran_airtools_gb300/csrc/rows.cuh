@@ -40,6 +40,11 @@ __device__ __forceinline__ int4 ld_stream(const int4 *p) {
         : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
     return r;
 }
+__device__ __forceinline__ unsigned ld_stream(const unsigned *p) {
+    unsigned r;
+    asm("ld.global.nc.L1::no_allocate.L2::256B.u32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+}
 __device__ __forceinline__ uint2 ld_stream(const uint2 *p) {
     uint2 r;
     asm("ld.global.nc.L1::no_allocate.L2::256B.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
@@ -121,26 +126,34 @@ __device__ __forceinline__ float u16_hi(uint32_t w, float bias) {
 // Four 2-byte values held in two 32-bit words, to floats.
 template <typename VT> struct Conv2B;
 template <> struct Conv2B<uint16_t> {
-    static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
+    static __device__ __forceinline__ void two(uint32_t a, float &lo, float &hi) {
         constexpr float b = 8388608.0f;  // 2^23
-        o[0] = u16_lo(a, b); o[1] = u16_hi(a, b);
-        o[2] = u16_lo(b2, b); o[3] = u16_hi(b2, b);
+        lo = u16_lo(a, b); hi = u16_hi(a, b);
+    }
+    static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
+        two(a, o[0], o[1]);
+        two(b2, o[2], o[3]);
     }
 };
 template <> struct Conv2B<int16_t> {
-    static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
+    static __device__ __forceinline__ void two(uint32_t a, float &lo, float &hi) {
         constexpr float b = 8421376.0f;  // 2^23 + 2^15
         a ^= 0x80008000u;
-        b2 ^= 0x80008000u;
-        o[0] = u16_lo(a, b); o[1] = u16_hi(a, b);
-        o[2] = u16_lo(b2, b); o[3] = u16_hi(b2, b);
+        lo = u16_lo(a, b); hi = u16_hi(a, b);
+    }
+    static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
+        two(a, o[0], o[1]);
+        two(b2, o[2], o[3]);
     }
 };
 template <> struct Conv2B<__half> {
+    static __device__ __forceinline__ void two(uint32_t a, float &lo, float &hi) {
+        const float2 f = __half22float2(*reinterpret_cast<__half2 *>(&a));
+        lo = f.x; hi = f.y;
+    }
     static __device__ __forceinline__ void to(uint32_t a, uint32_t b2, float (&o)[4]) {
-        __half2 ha = *reinterpret_cast<__half2 *>(&a), hb = *reinterpret_cast<__half2 *>(&b2);
-        float2 fa = __half22float2(ha), fb = __half22float2(hb);
-        o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
+        two(a, o[0], o[1]);
+        two(b2, o[2], o[3]);
     }
 };
 template <> struct VLoad<uint16_t, float> {

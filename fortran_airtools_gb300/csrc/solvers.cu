@@ -336,6 +336,10 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
                     cudaStream_t s) {
     const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
     const int G = M.sirt_lanes[S.prec];
+    if (code >= 11) {
+        if (sirt_pass_delta(S, M, pass, code, s)) return;
+        code = code == 11 ? 5 : 8;  // no delta copy: the sliced copy
+    }
     if (code >= 9) {
         if (pass == 1 && sirt_pass_tiled(S, M, code, s)) return;
         code = 3;  // no tiled copy: the fused records (else the packed stream)
@@ -401,7 +405,8 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
             const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S,
                            M.pk_L};
             const double *pv = M.pv64.as<double>();
-            if (NG >= 9 && pass == 1 && sirt_pass_tiled(S, M, NG, s)) return;
+            if (NG >= 11 && sirt_pass_delta(S, M, pass, NG, s)) return;
+            if (NG >= 9 && NG <= 10 && pass == 1 && sirt_pass_tiled(S, M, NG, s)) return;
             if (NG >= 5 && NG <= 8 && sirt_pass_sliced(S, M, pass, NG, s)) return;
             if (NG >= 9) NG = 1;
             if (NG > 2) NG = 2 - (NG & 1);  // 3, 5 -> 1 group per lane; 4, 6 -> 2
@@ -479,7 +484,10 @@ int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool all, b
             FAIR_TRY(csr_make_sliced(A, prec, A.sirt_lanes[prec], s));
         if (sliced && AT.sirt_groups[prec] >= 5 && AT.sirt_groups[prec] <= 8)
             FAIR_TRY(csr_make_sliced(AT, prec, AT.sirt_lanes[prec], s));
-        if (sliced && A.sirt_groups[prec] >= 9) FAIR_TRY(csr_make_tiled(A, prec, s));
+        if (sliced && A.sirt_groups[prec] >= 9 && A.sirt_groups[prec] <= 10)
+            FAIR_TRY(csr_make_tiled(A, prec, s));
+        if (sliced && A.sirt_groups[prec] >= 11) FAIR_TRY(csr_make_delta(A, prec, s));
+        if (sliced && AT.sirt_groups[prec] >= 11) FAIR_TRY(csr_make_delta(AT, prec, s));
     }
     return FAIR_OK;
 }
@@ -502,7 +510,12 @@ static bool uses_sliced(const DevCSR &M) {
 }
 static bool uses_tiled(const DevCSR &M) {
     for (int g : M.sirt_groups)
-        if (g >= 9) return true;
+        if (g >= 9 && g <= 10) return true;
+    return false;
+}
+static bool uses_delta(const DevCSR &M) {
+    for (int g : M.sirt_groups)
+        if (g >= 11) return true;
     return false;
 }
 
@@ -520,9 +533,10 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
         const bool fu = pk && (S.prec == FAIR_PREC_F16 ? M.hasf16 : S.prec == FAIR_PREC_Q16 && M.hasfq);
         // candidates {layout code, lanes per row}: the CSR (0), the packed
         // stream (1, 2), the fused records (3, 4) with 4-32 lanes per row;
-        // the sliced copy (5-8) with 1-8, or 0 (per chunk); the tiled copy (9, 10)
+        // the sliced copy (5-8) with 1-8, or 0 (per chunk); the tiled copy (9, 10);
+        // the delta copy (11-13)
         struct Cand { int code, lanes; };
-        Cand cand[52];
+        Cand cand[56];
         int nc = 0;
         for (int code = 0; code <= 4; ++code) {
             if ((code >= 1 && !pk) || (code >= 3 && !fu)) continue;
@@ -531,6 +545,11 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
         if (pk && (S.prec == FAIR_PREC_F64 || S.prec == FAIR_PREC_F32 || fu))
             for (int g : {0, 1, 2, 4, 8})
                 for (int code : {5, 6, 7, 8}) cand[nc++] = {code, g};
+        // the delta copy (11-13)
+        st = csr_make_delta(M, S.prec, s);
+        if (st != FAIR_OK) break;
+        if (M.dl[S.prec == FAIR_PREC_F16 || S.prec == FAIR_PREC_Q16].built)
+            for (int code : {11, 12, 13}) cand[nc++] = {code, 8};
         // the tiled copy (9, 10), residual pass only
         if (pass == 1) {
             st = csr_make_tiled(M, S.prec, s);
@@ -540,7 +559,7 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
         }
         int best_g = M.sirt_lanes[S.prec], best_code = M.sirt_groups[S.prec];
         float best_ms = -1.f;
-        float t[52];
+        float t[56];
         // two rounds over the candidates; each keeps its faster round
         for (int round = 0; round < 2 && st == FAIR_OK; ++round)
             for (int i = 0; i < nc && st == FAIR_OK; ++i) {
@@ -573,6 +592,10 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
         if (st == FAIR_OK && best_code >= 5 && best_code <= 8) st = csr_make_sliced(M, S.prec, best_g, s);
         if (!uses_sliced(M)) M.drop_sliced();  // free the copies no pass reads
         if (!uses_tiled(M)) M.tl.release();
+        if (!uses_delta(M)) {
+            M.dl[0].release();
+            M.dl[1].release();
+        }
         if (ms_best) ms_best[pass - 1] = best_ms;
     }
     for (auto &e : ev) cudaEventDestroy(e);

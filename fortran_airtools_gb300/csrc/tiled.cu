@@ -31,7 +31,7 @@ namespace fair {
 
 namespace {
 
-constexpr int kTile = 128;          // tile side T (local indices < T*(T+1) + 1 < 2^16)
+constexpr int kTile = 96;           // tile side T (local indices < T*(T+1) + 1 < 2^16)
 constexpr int kUnitChunks = 128;    // most chunks per work unit (the tile copy is reloaded per unit)
 constexpr int kTlThreads = 512;     // threads of a tile CTA
 

@@ -71,16 +71,22 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
  *         tiled copy: rows cut into segments by 128 x 128 tiles of the image,
  *         each tile of x staged in shared memory by the CTA that works on it,
  *         16-bit tile-local indices, one partial sum per segment added up per
- *         row in a second kernel; 2 or 4 steps in flight.
+ *         row in a second kernel; 2 or 4 steps in flight;
+ *   11-13 the delta copy: the sliced layout with one lane per row whose
+ *         slots hold column steps from the row's previous entry instead of
+ *         columns: four 7-bit steps beside 4 FP32/FP64 values, or one 16-byte
+ *         record of six 5-bit steps and six 2-byte values (f16, q16); 11 with
+ *         2 slots in flight, 12 with 4 and the gathers one slot ahead, 13
+ *         with 2 and the gathers one slot ahead.
  * A code whose layout the matrix lacks falls back to the nearest one it has.
  * d_b as in fair_sirt_run_device; d_x is scratch (overwritten). */
 int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
                        int32_t *config);
 
 /* Sets {lanes A, lanes A', layout A, layout A'} of the SIRT passes for the
- * handle's current precision: layout codes 0-10 as listed at
- * fair_sirt_autotune, with 4, 8, 16 or 32 lanes per row for codes 0-4, 9 and
- * 10 (unused by 9 and 10) and 0, 1, 2, 4 or 8 for codes 5-8 (else
+ * handle's current precision: layout codes 0-13 as listed at
+ * fair_sirt_autotune, with 4, 8, 16 or 32 lanes per row for codes 0-4 and
+ * 9-13 (unused by 9-13) and 0, 1, 2, 4 or 8 for codes 5-8 (else
  * FAIR_ERR_ARG). No reference counterpart. */
 int fair_sirt_set_lanes(fair_csr h, const int32_t *config);
 

@@ -97,7 +97,7 @@ def fan64(fair, oracle):
 
 @pytest.mark.parametrize("prec", ["f64", "f32", "f16", "q16"])
 @pytest.mark.parametrize("cfg", [(1, 8, 5, 6), (8, 1, 6, 5), (2, 4, 6, 6), (4, 2, 5, 5), (0, 0, 6, 6),
-                                 (8, 1, 7, 8), (1, 0, 8, 7)])
+                                 (8, 1, 7, 8), (1, 0, 8, 7), (8, 8, 11, 12), (8, 8, 12, 11)])
 @pytest.mark.parametrize("case", ["par96", "fan64"])
 def test_sliced_geometry(request, fair, oracle, case, prec, cfg):
     A, R, b = request.getfixturevalue(case)
@@ -110,12 +110,50 @@ def test_sliced_geometry(request, fair, oracle, case, prec, cfg):
 
 
 def test_sliced_lanes_checked(par96, fair):
-    """Codes 5-8 take 0 (per chunk), 1, 2, 4 or 8 lanes per row; codes 0-4,
-    9 and 10 take 4-32; codes past 10 are refused."""
+    """Codes 5-8 take 0 (per chunk), 1, 2, 4 or 8 lanes per row; codes 0-4
+    and 9-13 take 4-32; codes past 13 are refused."""
     from fortran_airtools_gb300._clib import check, lib
     A = par96[0]
-    for bad in [(16, 8, 5, 1), (8, 2, 1, 0), (8, 8, 11, 1), (3, 8, 6, 1), (1, 8, 9, 1)]:
+    for bad in [(16, 8, 5, 1), (8, 2, 1, 0), (8, 8, 14, 1), (3, 8, 6, 1), (1, 8, 9, 1), (8, 2, 11, 0)]:
         with pytest.raises(fair.FairError):
             check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(*bad)))
     check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(1, 32, 5, 0)))
     check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, 0, 0)))
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32", "f16", "q16"])
+@pytest.mark.parametrize("code", [11, 12, 13])
+def test_delta_ragged_rows(ragged, fair, oracle, prec, code):
+    """The delta copy (codes 11, 12: one lane per row, 7-bit column steps from
+    the row's previous entry) on rows of every length, empty rows included."""
+    A, R, b = ragged
+    o = fair.airms.options(lbound=0.0)
+    xs = run(fair, A, b, prec, (8, 8, code, code), "cimmino", 15, o)
+    xc = run(fair, A, b, prec, (8, 8, 0, 0), "cimmino", 15, o)
+    assert np.all(np.isfinite(xs))
+    assert rel_err(xs, xc) < TOL_SAME[prec]
+    xr = oracle.sirt("cimmino", R, b, 15, opts=oracle.options(lbound=0.0))
+    assert rel_err(xs, xr) < TOL_ORACLE[prec]
+
+
+@pytest.mark.parametrize("prec", ["f64", "q16"])
+def test_delta_side_table(par96, fair, oracle, prec):
+    """Rows whose entries are shuffled have steps outside the 7-bit codes:
+    their groups go to the side table; the iterate does not change."""
+    A0, R, b = par96
+    vA, IA, JA = A0.arrays()
+    vA, JA = vA.copy(), JA.copy()
+    rng = np.random.default_rng(12)
+    for r in rng.choice(R.m, size=R.m // 40, replace=False):
+        s, e = IA[r], IA[r + 1]
+        perm = rng.permutation(e - s)
+        vA[s:e], JA[s:e] = vA[s:e][perm], JA[s:e][perm]
+    A = fair.CSRMatrix.construct(R.m, R.n, vA, IA, JA)
+    Rs = oracle.OracleCSR(R.m, R.n, IA.astype(np.int64), JA.astype(np.int32), vA)
+    o = fair.airms.options(lbound=0.0)
+    xs = run(fair, A, b, prec, (8, 8, 12, 11), "cimmino", 12, o)
+    xc = run(fair, A, b, prec, (8, 8, 0, 0), "cimmino", 12, o)
+    assert rel_err(xs, xc) < TOL_SAME[prec]
+    xr = oracle.sirt("cimmino", Rs, b, 12, opts=oracle.options(lbound=0.0))
+    assert rel_err(xs, xr) < TOL_ORACLE[prec]
+    A.close()

@@ -1,13 +1,14 @@
 """The tiled copy of a ray matrix for the residual pass (layout codes 9, 10):
-rows cut into segments by 128 x 128 tiles of the N x N image, each tile of x
+rows cut into segments by 96 x 96 tiles of the N x N image, each tile of x
 staged in shared memory, one partial sum per segment, the partials of a row
 added in row order by a second kernel. The copy holds the same values as the
 CSR layout, so the iterates differ only by summation order: FP64 within
 1e-12 of the CSR iterate (and 1e-10 of the oracle), the FP32-accumulating
 forms within 2e-6. Images of 3 x 3 tiles with partial edge tiles, a single
-partial tile, a square matrix whose rows jump between tiles, and a matrix
-whose columns are not a square image (no tiled copy: the pass falls back to
-the row layouts)."""
+partial tile, a square matrix whose rows jump between tiles (its transpose
+also asks for the delta copy, which it refuses: too many steps outside the
+codes), and a matrix whose columns are not a square image (no tiled copy:
+the pass falls back to the row layouts)."""
 import ctypes as C
 
 import numpy as np
@@ -89,7 +90,7 @@ def test_tiled_geometry(request, fair, oracle, case, prec, code):
 def test_tiled_jumpy_rows(jumpy, fair, oracle, prec):
     A, R, b = jumpy
     o = fair.airms.options(lbound=0.0)
-    xt = run(fair, A, b, prec, (8, 8, 10, 1), "cimmino", 10, o)
+    xt = run(fair, A, b, prec, (8, 8, 10, 12), "cimmino", 10, o)
     xc = run(fair, A, b, prec, (8, 8, 0, 0), "cimmino", 10, o)
     assert np.all(np.isfinite(xt))
     assert rel_err(xt, xc) < TOL_SAME[prec]
