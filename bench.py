@@ -164,7 +164,7 @@ def kernel_suffix(prec, code, on_pk):
     codes of fair_sirt_set_lanes)."""
     if not on_pk:
         return "_f64" if prec == "f64" else "_lp"
-    if code >= 11:
+    if 11 <= code <= 13:
         return "_dl"
     if code >= 5:
         return "_sl"
@@ -350,7 +350,7 @@ def run_ours(args):
     on_pk = bool(pk and pk[dom - 1])
     code = (head["pass_config"]["groups_per_lane"][dom - 1] if head.get("pass_config")
             else 0 if hp == "f64" else 1)  # the library's default layouts
-    kname = ("k_tl_partials" if dom == 1 and code in (9, 10) and on_pk else
+    kname = ("k_tl_partials" if dom == 1 and code in (9, 10, 14) and on_pk else
              {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kernel_suffix(hp, code, on_pk))
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]

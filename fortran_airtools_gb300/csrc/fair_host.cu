@@ -67,6 +67,11 @@ void DevCSR::Tiled::release() {
     segbase.release(); soff.release(); pslot.release(); units.release(); idx.release();
     v64.release(); v32.release(); r16.release(); rq.release(); part.release();
     sstart.release(); send.release();
+    soff6.release(); anc6.release(); code6.release(); side6.release(); r6_16.release(); r6_q.release();
+    S6 = 0;
+    L6 = 5;
+    nslots6 = nesc6 = 0;
+    tried6 = built6 = has6_16 = has6_q = false;
     T = N = ntr = 0;
     nseg = nchunks = nslots = 0;
     nunits = 0;
@@ -1215,12 +1220,12 @@ int fair_sirt_set_lanes(fair_csr h, const int32_t *config) {
     auto ok = [](int32_t g, int32_t code) {
         if (code >= 0 && code <= 4) return g == 4 || g == 8 || g == 16 || g == 32;
         if (code >= 5 && code <= 8) return g == 0 || g == 1 || g == 2 || g == 4 || g == 8;
-        if (code >= 9 && code <= 13) return g == 4 || g == 8 || g == 16 || g == 32;
+        if (code >= 9 && code <= 14) return g == 4 || g == 8 || g == 16 || g == 32;
         return false;
     };
     if (!ok(config[0], config[2]) || !ok(config[1], config[3])) {
-        set_detail("layout code must be 0-13, with 4, 8, 16 or 32 lanes per row for codes 0-4 "
-                   "and 9-13 and 0, 1, 2, 4 or 8 for codes 5-8");
+        set_detail("layout code must be 0-14, with 4, 8, 16 or 32 lanes per row for codes 0-4 "
+                   "and 9-14 and 0, 1, 2, 4 or 8 for codes 5-8");
         return FAIR_ERR_ARG;
     }
     FAIR_TRY(ensure_transpose(h));
@@ -1256,7 +1261,8 @@ int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches) {
     if (!h || !launches) return FAIR_ERR_NULL;
     // one FP32 shadow conversion per call in reduced precision, one kernel per
     // pass and iteration (two for a residual pass on the tiled copy)
-    const int p1 = h->A.sirt_groups[h->prec] >= 9 && h->A.tl.built() ? 2 : 1;
+    const int g1 = h->A.sirt_groups[h->prec];
+    const int p1 = (g1 == 9 || g1 == 10 || g1 == 14) && h->A.tl.built() ? 2 : 1;
     *launches = (h->prec != FAIR_PREC_F64 ? 1 : 0) + (int64_t)(p1 + 1) * K;
     return FAIR_OK;
 }

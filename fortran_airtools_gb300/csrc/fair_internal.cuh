@@ -116,6 +116,14 @@ struct DevCSR {
         DevBuf v64, v32;  // values per slot
         DevBuf r16, rq;   // fused records {local indices, 2-byte values} (f16, q16)
         DevBuf sstart, send;  // int64 [nseg] entry range of each segment (value fills)
+        // the 6-entry step records of the 2-byte forms (layout code 14): per slot
+        // {six 5-bit steps of the tile-local index, six 2-byte values}, the
+        // segment's first local index in anc6 [nchunks*32]
+        int S6 = 0, L6 = 5;
+        int64_t nslots6 = 0, nesc6 = 0;
+        bool tried6 = false, built6 = false;
+        DevBuf soff6, anc6, code6, side6, r6_16, r6_q;
+        bool has6_16 = false, has6_q = false;
         bool has_idx = false, has_v64 = false, has_v32 = false, has_r16 = false, has_rq = false;
         DevBuf part;      // partial sums [nseg] (8 bytes each)
         bool built() const { return T > 0; }

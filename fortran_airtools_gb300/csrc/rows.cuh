@@ -649,6 +649,49 @@ __device__ __forceinline__ void chunk_rows_sliced(const int64_t *__restrict__ pr
     finish_chunks(sched, nwarps, lane);
 }
 
+// ---- column steps (delta copies) -------------------------------------------
+// A B-bit step code: a signed low part of L bits and a signed high part of
+// B - L bits, delta = lo + hi*S (L = B: the plain signed delta). A word holds
+// E codes, code q in bits B*q .. B*q + B - 1.
+template <int B>
+__host__ __device__ inline bool step_encode(int64_t d, int S, int L, uint32_t &code) {
+    constexpr uint32_t mask = (1u << B) - 1u;
+    if (L >= B) {
+        if (d < -(int64_t(1) << (B - 1)) || d >= (int64_t(1) << (B - 1))) return false;
+        code = (uint32_t)d & mask;
+        return true;
+    }
+    int64_t hi = 0;
+    if (S > 0) hi = d >= 0 ? (d + S / 2) / S : -((-d + S / 2) / S);
+    const int64_t lo = d - hi * S;
+    const int64_t lmin = -(int64_t(1) << (L - 1)), lmax = (int64_t(1) << (L - 1)) - 1;
+    const int64_t hmin = -(int64_t(1) << (B - 1 - L)), hmax = (int64_t(1) << (B - 1 - L)) - 1;
+    if (lo < lmin || lo > lmax || hi < hmin || hi > hmax) return false;
+    code = (uint32_t)((hi << L) | (lo & ((int64_t(1) << L) - 1))) & mask;
+    return true;
+}
+template <int B>
+__device__ __forceinline__ int step_decode(uint32_t b, int S, int L) {
+    const int lo = (int)(b << (32 - L)) >> (32 - L);
+    const int hi = L >= B ? 0 : (int)(b << (32 - B)) >> (32 - B + L);
+    return lo + hi * S;
+}
+// The word of E steps from `prev` through c[0..E-1]; false when a step has no code.
+template <int E, int B>
+__device__ __forceinline__ bool step_word(const int (&c)[E], int prev, int S, int L, uint32_t &w) {
+    uint32_t cd;
+    bool ok = step_encode<B>((int64_t)c[0] - prev, S, L, cd);
+    w = ok ? cd : 0u;
+#pragma unroll
+    for (int q = 1; q < E; ++q) {
+        ok = ok && step_encode<B>((int64_t)c[q] - c[q - 1], S, L, cd);
+        if (ok) w |= cd << (B * q);
+    }
+    return ok;
+}
+constexpr uint32_t kStepEsc = 1u << 31;         // the word's columns are in a side table
+constexpr uint32_t kStepSlot = 0x3FFFFFFFu;     // its slot there
+
 // Lanes per row used when none has been tuned.
 constexpr int kDefaultLanesPerRow = 8;
 

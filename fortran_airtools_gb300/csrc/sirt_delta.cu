@@ -33,8 +33,8 @@ namespace fair {
 
 namespace {
 
-constexpr uint32_t kDlEsc = 1u << 31;
-constexpr uint32_t kDlSlot = 0x3FFFFFFFu;  // side-table slot of an escaped word
+constexpr uint32_t kDlEsc = kStepEsc;
+constexpr uint32_t kDlSlot = kStepSlot;
 constexpr int kDlCand = 8;
 struct DlCands {
     int n = 0;
@@ -48,50 +48,12 @@ int dl_grid(int64_t work_items) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, cap));
 }
 
-// B-bit step code of delta d.
-template <int B>
-__host__ __device__ inline bool dl_encode(int64_t d, int S, int L, uint32_t &code) {
-    constexpr uint32_t mask = (1u << B) - 1u;
-    if (L >= B) {
-        if (d < -(int64_t(1) << (B - 1)) || d >= (int64_t(1) << (B - 1))) return false;
-        code = (uint32_t)d & mask;
-        return true;
-    }
-    int64_t hi = 0;
-    if (S > 0) hi = d >= 0 ? (d + S / 2) / S : -((-d + S / 2) / S);
-    const int64_t lo = d - hi * S;
-    const int64_t lmin = -(int64_t(1) << (L - 1)), lmax = (int64_t(1) << (L - 1)) - 1;
-    const int64_t hmin = -(int64_t(1) << (B - 1 - L)), hmax = (int64_t(1) << (B - 1 - L)) - 1;
-    if (lo < lmin || lo > lmax || hi < hmin || hi > hmax) return false;
-    code = (uint32_t)((hi << L) | (lo & ((int64_t(1) << L) - 1))) & mask;
-    return true;
-}
-template <int B>
-__device__ __forceinline__ int dl_step(uint32_t b, int S, int L) {
-    const int lo = (int)(b << (32 - L)) >> (32 - L);
-    const int hi = L >= B ? 0 : (int)(b << (32 - B)) >> (32 - B + L);
-    return lo + hi * S;
-}
-
 // The E columns of the slot starting at entry e0 of a row ending at e;
 // entries past the row repeat the last column.
 template <int E>
 __device__ __forceinline__ void dl_cols(const int32_t *col, int64_t e0, int64_t e, int (&c)[E]) {
 #pragma unroll
     for (int q = 0; q < E; ++q) c[q] = e0 + q < e ? col[e0 + q] : (q ? c[q - 1] : 0);
-}
-
-template <int E, int B>
-__device__ __forceinline__ bool dl_word(const int (&cs)[E], int prev, int S, int L, uint32_t &w) {
-    uint32_t cd;
-    bool ok = dl_encode<B>((int64_t)cs[0] - prev, S, L, cd);
-    w = ok ? cd : 0u;
-#pragma unroll
-    for (int q = 1; q < E; ++q) {
-        ok = ok && dl_encode<B>((int64_t)cs[q] - cs[q - 1], S, L, cd);
-        if (ok) w |= cd << (B * q);
-    }
-    return ok;
 }
 
 // Slots whose steps have no code, per candidate (one warp per row).
@@ -114,7 +76,7 @@ __global__ void k_dl_count(const int64_t *rowptr, int32_t m, const int32_t *col,
             for (int c = 0; c < kDlCand; ++c) {
                 if (c >= C.n) break;
                 uint32_t w;
-                if (!dl_word<E, B>(cs, prev, C.S[c], C.L[c], w)) ++cnt[c];
+                if (!step_word<E, B>(cs, prev, C.S[c], C.L[c], w)) ++cnt[c];
             }
         }
     }
@@ -161,7 +123,7 @@ __global__ void k_dl_fill(const int64_t *rowptr, int32_t m, const int32_t *col, 
             if (e0 < e) {
                 int cs[E];
                 dl_cols<E>(col, e0, e, cs);
-                if (!dl_word<E, B>(cs, prev, S, L, w)) {
+                if (!step_word<E, B>(cs, prev, S, L, w)) {
                     const unsigned long long slot = atomicAdd(nesc, 1ull);
                     if (slot < cap) {
                         int t[4 * E4];
@@ -366,7 +328,7 @@ template <class LD, typename XT, int D, int PF, class Epi>
 __global__ void __launch_bounds__(256) k_sirt_resid_dl(DlArgs P, LD ldr, int32_t m, const XT *x,
                                                        Epi epi, unsigned *sched) {
     __shared__ int lut[128];
-    for (int t = threadIdx.x; t < (1 << LD::B); t += blockDim.x) lut[t] = dl_step<LD::B>((uint32_t)t, P.S, P.L);
+    for (int t = threadIdx.x; t < (1 << LD::B); t += blockDim.x) lut[t] = step_decode<LD::B>((uint32_t)t, P.S, P.L);
     __syncthreads();
     dl_rows<LD, XT, D, PF>(P, ldr, m, lut, x, epi, sched);
 }
@@ -374,7 +336,7 @@ template <class LD, typename XT, int D, int PF, class Epi>
 __global__ void __launch_bounds__(256) k_sirt_update_dl(DlArgs P, LD ldr, int32_t m, const XT *r,
                                                         Epi epi, unsigned *sched) {
     __shared__ int lut[128];
-    for (int t = threadIdx.x; t < (1 << LD::B); t += blockDim.x) lut[t] = dl_step<LD::B>((uint32_t)t, P.S, P.L);
+    for (int t = threadIdx.x; t < (1 << LD::B); t += blockDim.x) lut[t] = step_decode<LD::B>((uint32_t)t, P.S, P.L);
     __syncthreads();
     dl_rows<LD, XT, D, PF>(P, ldr, m, lut, r, epi, sched);
 }

@@ -336,6 +336,10 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
                     cudaStream_t s) {
     const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
     const int G = M.sirt_lanes[S.prec];
+    if (code == 14) {  // the tiled copy's step records (else its 4-entry slots)
+        if (pass == 1 && sirt_pass_tiled(S, M, code, s)) return;
+        code = 9;
+    }
     if (code >= 11) {
         if (sirt_pass_delta(S, M, pass, code, s)) return;
         code = code == 11 ? 5 : 8;  // no delta copy: the sliced copy
@@ -405,6 +409,7 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
             const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S,
                            M.pk_L};
             const double *pv = M.pv64.as<double>();
+            if (NG == 14) NG = 9;  // step records: 2-byte forms only
             if (NG >= 11 && sirt_pass_delta(S, M, pass, NG, s)) return;
             if (NG >= 9 && NG <= 10 && pass == 1 && sirt_pass_tiled(S, M, NG, s)) return;
             if (NG >= 5 && NG <= 8 && sirt_pass_sliced(S, M, pass, NG, s)) return;
@@ -484,10 +489,11 @@ int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool all, b
             FAIR_TRY(csr_make_sliced(A, prec, A.sirt_lanes[prec], s));
         if (sliced && AT.sirt_groups[prec] >= 5 && AT.sirt_groups[prec] <= 8)
             FAIR_TRY(csr_make_sliced(AT, prec, AT.sirt_lanes[prec], s));
-        if (sliced && A.sirt_groups[prec] >= 9 && A.sirt_groups[prec] <= 10)
-            FAIR_TRY(csr_make_tiled(A, prec, s));
-        if (sliced && A.sirt_groups[prec] >= 11) FAIR_TRY(csr_make_delta(A, prec, s));
-        if (sliced && AT.sirt_groups[prec] >= 11) FAIR_TRY(csr_make_delta(AT, prec, s));
+        auto tiled = [](int g) { return g == 9 || g == 10 || g == 14; };
+        auto delta = [](int g) { return g >= 11 && g <= 13; };
+        if (sliced && tiled(A.sirt_groups[prec])) FAIR_TRY(csr_make_tiled(A, prec, s));
+        if (sliced && delta(A.sirt_groups[prec])) FAIR_TRY(csr_make_delta(A, prec, s));
+        if (sliced && delta(AT.sirt_groups[prec])) FAIR_TRY(csr_make_delta(AT, prec, s));
     }
     return FAIR_OK;
 }
@@ -510,12 +516,12 @@ static bool uses_sliced(const DevCSR &M) {
 }
 static bool uses_tiled(const DevCSR &M) {
     for (int g : M.sirt_groups)
-        if (g >= 9 && g <= 10) return true;
+        if (g == 9 || g == 10 || g == 14) return true;
     return false;
 }
 static bool uses_delta(const DevCSR &M) {
     for (int g : M.sirt_groups)
-        if (g >= 11) return true;
+        if (g >= 11 && g <= 13) return true;
     return false;
 }
 
@@ -556,6 +562,7 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
             if (st != FAIR_OK) break;
             if (M.tl.built())
                 for (int code : {9, 10}) cand[nc++] = {code, 8};
+            if (M.tl.built6 && (S.prec == FAIR_PREC_F16 || S.prec == FAIR_PREC_Q16)) cand[nc++] = {14, 8};
         }
         int best_g = M.sirt_lanes[S.prec], best_code = M.sirt_groups[S.prec];
         float best_ms = -1.f;

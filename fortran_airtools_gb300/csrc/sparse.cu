@@ -579,6 +579,7 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
     A.hasp64 = A.hasp32 = A.hasp16 = A.haspq = A.hasf16 = A.hasfq = false;
     A.hassv64 = A.hassv32 = A.hassf16 = A.hassfq = false;
     A.tl.has_v64 = A.tl.has_v32 = A.tl.has_r16 = A.tl.has_rq = false;
+    A.tl.has6_16 = A.tl.has6_q = false;
     for (auto &d : A.dl) d.has_v64 = d.has_v32 = d.has_r16 = d.has_rq = false;
     return FAIR_OK;
 }

@@ -1,5 +1,5 @@
-// tiled.cu -- A x on a copy of a ray matrix cut by image tiles (layout code 9
-// of the residual pass of SIRT, AIRMs.f90:1089-1110).
+// tiled.cu -- A x on a copy of a ray matrix cut by image tiles (layout codes 9,
+// 10 and 14 of the residual pass of SIRT, AIRMs.f90:1089-1110).
 //
 // The columns of a ray matrix are the pixels of an N x N image (column j =
 // c*N + r). On the row layouts the x entries a warp gathers are scattered
@@ -236,21 +236,177 @@ struct PutF64 {
     }
 };
 
+// ---- 6-entry step records (2-byte forms) ------------------------------------
+// Slot k of a chunk lane holds entries 6k..6k+5 of its segment as six 5-bit
+// steps of the tile-local index (the first from the entry before, from the
+// segment's first index for k = 0) and six 2-byte values. Inside a tile a ray
+// steps by +-1 (along a column) or +-(T+1) (to the next column of the shared
+// copy), so the code with S = T + 1 covers every step of a ray matrix.
+constexpr int kT6Cand = 3;
+struct T6Cands {
+    int n = 0;
+    int S[kT6Cand] = {};
+    int L[kT6Cand] = {};
+};
+
+__device__ __forceinline__ void t6_locals(const int32_t *col, int64_t e0, int64_t en, int N, int T,
+                                          int (&li)[6]) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) li[q] = e0 + q < en ? (int)tl_local(col[e0 + q], N, T) : (q ? li[q - 1] : 0);
+}
+
+// Slots of each chunk: 32 x its longest segment in 6-entry slots.
+__global__ void k_t6_len(int64_t nchunks, const int32_t *pslot, const int64_t *sstart,
+                         const int64_t *send, int32_t *cnt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nchunks; c += nw) {
+        const int32_t sg = pslot[c * 32 + lane];
+        const unsigned g = sg >= 0 ? (unsigned)((send[sg] - sstart[sg] + 5) / 6) : 0u;
+        const unsigned mx = __reduce_max_sync(0xffffffffu, g);
+        if (lane == 0) cnt[c] = (int32_t)(32 * mx);
+    }
+}
+
+// Slots whose steps have no code, per candidate (one thread per segment).
+__global__ void k_t6_count(int64_t nseg, const int64_t *sstart, const int64_t *send,
+                           const int32_t *col, int N, int T, T6Cands C, unsigned long long *esc) {
+    unsigned cnt[kT6Cand] = {0, 0, 0};
+    for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg;
+         sg += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t st = sstart[sg], en = send[sg];
+        int prev = (int)tl_local(col[st], N, T);
+        for (int64_t e0 = st; e0 < en; e0 += 6) {
+            int li[6];
+            t6_locals(col, e0, en, N, T, li);
+#pragma unroll
+            for (int c = 0; c < kT6Cand; ++c) {
+                uint32_t w;
+                if (c < C.n && !step_word<6, 5>(li, prev, C.S[c], C.L[c], w)) ++cnt[c];
+            }
+            prev = li[5];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kT6Cand; ++c)
+        if (cnt[c]) atomicAdd(esc + c, (unsigned long long)cnt[c]);
+}
+
+// Step words, first indices and side table (one warp per chunk).
+__global__ void k_t6_fill(int64_t nchunks, const int64_t *soff6, const int32_t *pslot,
+                          const int64_t *sstart, const int64_t *send, const int32_t *col, int N,
+                          int T, int S, int L, uint32_t *code, int32_t *anc, int4 *side,
+                          unsigned long long cap, unsigned long long *nesc) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int zero = T * (T + 1);
+    for (int64_t c = warp; c < nchunks; c += nw) {
+        const int32_t sg = pslot[c * 32 + lane];
+        const int64_t st = sg >= 0 ? sstart[sg] : 0, en = sg >= 0 ? send[sg] : 0;
+        const int64_t base = soff6[c], len = (soff6[c + 1] - base) >> 5;
+        int prev = en > st ? (int)tl_local(col[st], N, T) : zero;
+        anc[c * 32 + lane] = prev;
+        for (int64_t k = 0; k < len; ++k) {
+            const int64_t e0 = st + 6 * k;
+            uint32_t w = 0;  // past the segment: zero steps
+            if (e0 < en) {
+                int li[6];
+                t6_locals(col, e0, en, N, T, li);
+                if (!step_word<6, 5>(li, prev, S, L, w)) {
+                    const unsigned long long slot = atomicAdd(nesc, 1ull);
+                    if (slot < cap) {
+                        side[2 * slot] = make_int4(li[0], li[1], li[2], li[3]);
+                        side[2 * slot + 1] = make_int4(li[4], li[5], 0, 0);
+                    }
+                    w = kStepEsc | (uint32_t)(slot & kStepSlot);
+                }
+                prev = li[5];
+            }
+            code[base + 32 * k + lane] = w;
+        }
+    }
+}
+
+// Records {word, six 2-byte codes} of one 2-byte form.
+__global__ void k_t6_rec(int64_t nchunks, const int64_t *soff6, const int32_t *pslot,
+                         const int64_t *sstart, const int64_t *send, const uint32_t *code,
+                         const uint16_t *src, uint4 *rec) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t c = warp; c < nchunks; c += nw) {
+        const int32_t sg = pslot[c * 32 + lane];
+        const int64_t st = sg >= 0 ? sstart[sg] : 0, en = sg >= 0 ? send[sg] : 0;
+        const int64_t base = soff6[c], len = (soff6[c + 1] - base) >> 5;
+        for (int64_t k = 0; k < len; ++k) {
+            const int64_t slot = base + 32 * k + lane;
+            uint32_t h[6];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const int64_t j = st + 6 * k + q;
+                h[q] = j < en ? src[j] : 0u;
+            }
+            rec[slot] = make_uint4(code[slot], h[0] | (h[1] << 16), h[2] | (h[3] << 16),
+                                   h[4] | (h[5] << 16));
+        }
+    }
+}
+
 // ---- the pass ---------------------------------------------------------------
 // Slot loaders: four local indices and four values.
+// E entries per slot; State is what a lane carries from slot to slot.
 template <typename VT> struct TlFused {
+    static constexpr int E = 4;
     const uint4 *rec;
     using Raw = uint4;
+    struct State {};
+    __device__ __forceinline__ State init(int64_t) const { return {}; }
     __device__ __forceinline__ Raw load(int64_t j) const { return ld_stream(rec + j); }
     __device__ __forceinline__ static Raw none() { return make_uint4(0u, 0u, 0u, 0u); }
-    __device__ __forceinline__ static void open(const Raw &r, uint32_t (&li)[4], float (&v)[4]) {
+    __device__ __forceinline__ void open(const Raw &r, State &, const int *, uint32_t (&li)[4],
+                                         float (&v)[4]) const {
         li[0] = r.x & 0xFFFFu; li[1] = r.x >> 16; li[2] = r.y & 0xFFFFu; li[3] = r.y >> 16;
         Conv2B<VT>::to(r.z, r.w, v);
     }
 };
+template <typename VT> struct TlStep6 {  // 6-entry step records
+    static constexpr int E = 6;
+    const uint4 *rec;
+    const int32_t *anc;
+    const int4 *side;
+    using Raw = uint4;
+    struct State {
+        int li;  // the lane's last local index
+    };
+    __device__ __forceinline__ State init(int64_t lanepos) const { return {__ldg(anc + lanepos)}; }
+    __device__ __forceinline__ Raw load(int64_t j) const { return ld_stream(rec + j); }
+    __device__ __forceinline__ static Raw none() { return make_uint4(0u, 0u, 0u, 0u); }
+    __device__ __forceinline__ void open(const Raw &r, State &st, const int *lut, uint32_t (&li)[6],
+                                         float (&v)[6]) const {
+        const uint32_t w = r.x;
+        if (w & kStepEsc) {
+            const int4 a = __ldg(side + 2 * (int64_t)(w & kStepSlot));
+            const int4 b = __ldg(side + 2 * (int64_t)(w & kStepSlot) + 1);
+            li[0] = a.x; li[1] = a.y; li[2] = a.z; li[3] = a.w; li[4] = b.x; li[5] = b.y;
+        } else {
+            li[0] = (uint32_t)(st.li + lut[w & 31u]);
+#pragma unroll
+            for (int q = 1; q < 6; ++q) li[q] = li[q - 1] + lut[(w >> (5 * q)) & 31u];
+        }
+        st.li = (int)li[5];
+        Conv2B<VT>::two(r.y, v[0], v[1]);
+        Conv2B<VT>::two(r.z, v[2], v[3]);
+        Conv2B<VT>::two(r.w, v[4], v[5]);
+    }
+};
 template <typename VT> struct TlSplit {
+    static constexpr int E = 4;
     const uint2 *idx;
     const VT *val;
+    struct State {};
+    __device__ __forceinline__ State init(int64_t) const { return {}; }
     struct Raw {
         uint2 w;
         VBlk<VT> v;
@@ -267,7 +423,8 @@ template <typename VT> struct TlSplit {
         r.v.clear();
         return r;
     }
-    __device__ __forceinline__ static void open(const Raw &r, uint32_t (&li)[4], VT (&v)[4]) {
+    __device__ __forceinline__ void open(const Raw &r, State &, const int *, uint32_t (&li)[4],
+                                         VT (&v)[4]) const {
         li[0] = r.w.x & 0xFFFFu; li[1] = r.w.x >> 16; li[2] = r.w.y & 0xFFFFu; li[3] = r.w.y >> 16;
         r.v.to(v);
     }
@@ -279,6 +436,7 @@ struct TlArgs {
     const int4 *units;
     int32_t nunits;
     int N, T, ntr;
+    int S6, L6;  // step code of the 6-entry records
 };
 
 // Partial sums of all segments. Persistent CTAs take work units through
@@ -290,9 +448,12 @@ __global__ void __launch_bounds__(kTlThreads) k_tl_partials(TlArgs P, LD ldr,
     extern __shared__ __align__(16) unsigned char tl_smem[];
     XT *xs = reinterpret_cast<XT *>(tl_smem);
     __shared__ int s_unit, s_chunk;
+    __shared__ int lut[32];  // 5-bit step codes of the 6-entry records
     constexpr unsigned FULL = 0xffffffffu;
+    constexpr int E = LD::E;
     const int lane = threadIdx.x & 31;
     const int T = P.T, N = P.N;
+    if (threadIdx.x < 32) lut[threadIdx.x] = step_decode<5>((uint32_t)threadIdx.x, P.S6, P.L6);
     for (;;) {
         if (threadIdx.x == 0) s_unit = (int)atomicAdd(ctr, 1u);
         __syncthreads();
@@ -321,6 +482,7 @@ __global__ void __launch_bounds__(kTlThreads) k_tl_partials(TlArgs P, LD ldr,
             typename LD::Raw ring[D];
 #pragma unroll
             for (int k = 0; k < D; ++k) ring[k] = k < len ? ldr.load(s0 + 32 * k) : LD::none();
+            typename LD::State lst = ldr.init((int64_t)c * 32 + lane);
             ACC acc = 0;
             for (int t0 = 0; t0 < len; t0 += D) {
 #pragma unroll
@@ -329,11 +491,11 @@ __global__ void __launch_bounds__(kTlThreads) k_tl_partials(TlArgs P, LD ldr,
                     if (t >= len) break;
                     const typename LD::Raw cur = ring[k];
                     ring[k] = t + D < len ? ldr.load(s0 + 32 * (int64_t)(t + D)) : LD::none();
-                    uint32_t li[4];
-                    ACC v[4];
-                    LD::open(cur, li, v);
+                    uint32_t li[E];
+                    ACC v[E];
+                    ldr.open(cur, lst, lut, li, v);
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) acc += (ACC)xs[li[q]] * v[q];
+                    for (int q = 0; q < E; ++q) acc += (ACC)xs[li[q]] * v[q];
                 }
             }
             const int ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
@@ -366,8 +528,9 @@ template <class LD, typename XT, typename ACC, class Epi>
 int launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &e,
               unsigned *ctr, cudaStream_t s) {
     const DevCSR::Tiled &tl = M.tl;
-    const TlArgs P{tl.soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.units.as<int4>(), tl.nunits,
-                   tl.N, tl.T, tl.ntr};
+    const DevBuf &soff = LD::E == 6 ? tl.soff6 : tl.soff;
+    const TlArgs P{soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.units.as<int4>(), tl.nunits,
+                   tl.N, tl.T, tl.ntr, tl.S6, tl.L6};
     const size_t smem = sizeof(XT) * ((size_t)tl.T * (tl.T + 1) + 1);
     ACC *part = tl.part.as<ACC>();
     auto run = [&](auto kernel) -> int {
@@ -386,6 +549,65 @@ int launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &
     else FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 2>));
     k_tl_rows<ACC, Epi><<<tl_grid(M.m), 256, 0, s>>>(M.m, tl.segbase.as<int64_t>(), part, e);
     FAIR_CUDA(cudaGetLastError());
+    return FAIR_OK;
+}
+
+// Index part of the 6-entry step records (after the tiled copy is built).
+int t6_build(DevCSR &A, cudaStream_t s) {
+    DevCSR::Tiled &tl = A.tl;
+    const int64_t nch = tl.nchunks;
+    TmpBuf cnt, esc;
+    FAIR_TRY(cnt.grow(sizeof(int32_t) * (nch + 1)));
+    FAIR_TRY(tl.soff6.grow(sizeof(int64_t) * (nch + 1)));
+    k_t6_len<<<tl_grid(nch * 32), 256, 0, s>>>(nch, tl.pslot.as<int32_t>(), tl.sstart.as<int64_t>(),
+                                                tl.send.as<int64_t>(), cnt.as<int32_t>());
+    FAIR_CUDA(cudaGetLastError());
+    FAIR_TRY(scan_counts(cnt.as<int32_t>(), nch, tl.soff6.as<int64_t>(), s));
+    T6Cands C;
+    C.S[0] = tl.T + 1; C.L[0] = 2;
+    C.S[1] = tl.T + 1; C.L[1] = 3;
+    C.S[2] = 0; C.L[2] = 5;
+    C.n = 3;
+    FAIR_TRY(esc.grow(sizeof(unsigned long long) * (kT6Cand + 1)));
+    FAIR_CUDA(cudaMemsetAsync(esc.p, 0, sizeof(unsigned long long) * (kT6Cand + 1), s));
+    k_t6_count<<<tl_grid(tl.nseg), 256, 0, s>>>(tl.nseg, tl.sstart.as<int64_t>(), tl.send.as<int64_t>(),
+                                                  A.col.as<int32_t>(), tl.N, tl.T, C,
+                                                  esc.as<unsigned long long>());
+    FAIR_CUDA(cudaGetLastError());
+    unsigned long long hesc[kT6Cand] = {};
+    FAIR_CUDA(cudaMemcpyAsync(hesc, esc.p, sizeof(hesc), cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaMemcpyAsync(&tl.nslots6, tl.soff6.as<int64_t>() + nch, sizeof(int64_t),
+                              cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    int best = 0;
+    for (int c = 1; c < C.n; ++c)
+        if (hesc[c] < hesc[best]) best = c;
+    // too many slots without codes: the side-table reads would cost more than the codes save
+    if (hesc[best] > (unsigned long long)(A.nnz / 6 / 8) || hesc[best] > kStepSlot) {
+        tl.soff6.release();
+        return FAIR_OK;
+    }
+    const size_t ns = (size_t)std::max<int64_t>(tl.nslots6, 1);
+    FAIR_TRY(tl.code6.grow(sizeof(uint32_t) * ns));
+    FAIR_TRY(tl.anc6.grow(sizeof(int32_t) * 32 * (size_t)std::max<int64_t>(nch, 1)));
+    FAIR_TRY(tl.side6.grow(sizeof(int4) * 2 * (size_t)std::max<unsigned long long>(hesc[best], 1)));
+    unsigned long long *ctr = esc.as<unsigned long long>() + kT6Cand;
+    k_t6_fill<<<tl_grid(nch * 32), 256, 0, s>>>(
+        nch, tl.soff6.as<int64_t>(), tl.pslot.as<int32_t>(), tl.sstart.as<int64_t>(),
+        tl.send.as<int64_t>(), A.col.as<int32_t>(), tl.N, tl.T, C.S[best], C.L[best],
+        tl.code6.as<uint32_t>(), tl.anc6.as<int32_t>(), tl.side6.as<int4>(), hesc[best], ctr);
+    FAIR_CUDA(cudaGetLastError());
+    unsigned long long used = 0;
+    FAIR_CUDA(cudaMemcpyAsync(&used, ctr, sizeof(used), cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    if (used != hesc[best]) {  // the fill must meet exactly the slots the count found
+        set_detail("tiled step records: side-table count mismatch");
+        return FAIR_ERR_STATE;
+    }
+    tl.S6 = C.S[best];
+    tl.L6 = C.L[best];
+    tl.nesc6 = (int64_t)hesc[best];
+    tl.built6 = true;
     return FAIR_OK;
 }
 
@@ -537,6 +759,22 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
         (h ? tl.has_r16 : tl.has_rq) = true;
     }
     FAIR_CUDA(cudaGetLastError());
+    if (prec == FAIR_PREC_F16 || prec == FAIR_PREC_Q16) {  // the 6-entry step records
+        if (!tl.tried6) {
+            tl.tried6 = true;
+            FAIR_TRY(t6_build(A, s));
+        }
+        const bool h = prec == FAIR_PREC_F16;
+        if (tl.built6 && !(h ? tl.has6_16 : tl.has6_q)) {
+            DevBuf &dst = h ? tl.r6_16 : tl.r6_q;
+            FAIR_TRY(dst.grow(sizeof(uint4) * (size_t)std::max<int64_t>(tl.nslots6, 1)));
+            k_t6_rec<<<tl_grid(nch * 32), 256, 0, s>>>(
+                nch, tl.soff6.as<int64_t>(), ps, st, en, tl.code6.as<uint32_t>(),
+                h ? A.v16.as<uint16_t>() : A.vq.as<uint16_t>(), dst.as<uint4>());
+            FAIR_CUDA(cudaGetLastError());
+            (h ? tl.has6_16 : tl.has6_q) = true;
+        }
+    }
     return FAIR_OK;
 }
 
@@ -556,6 +794,18 @@ bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int code, cudaStream_t s
             if (!tl.has_v32) return false;
             st = launch_tl<TlSplit<float>, float, float>(
                 M, code, TlSplit<float>{tl.idx.as<uint2>(), tl.v32.as<float>()}, S.x32, e, S.sched, s);
+        } else if (code == 14 && tl.built6 && (S.prec == FAIR_PREC_F16 ? tl.has6_16 : tl.has6_q)) {
+            const int32_t *anc = tl.anc6.as<int32_t>();
+            const int4 *side = tl.side6.as<int4>();
+            if (S.prec == FAIR_PREC_F16)
+                st = launch_tl<TlStep6<__half>, float, float>(
+                    M, code, TlStep6<__half>{tl.r6_16.as<uint4>(), anc, side}, S.x32, e, S.sched, s);
+            else if (M.qsigned)
+                st = launch_tl<TlStep6<int16_t>, float, float>(
+                    M, code, TlStep6<int16_t>{tl.r6_q.as<uint4>(), anc, side}, S.x32, e, S.sched, s);
+            else
+                st = launch_tl<TlStep6<uint16_t>, float, float>(
+                    M, code, TlStep6<uint16_t>{tl.r6_q.as<uint4>(), anc, side}, S.x32, e, S.sched, s);
         } else if (S.prec == FAIR_PREC_F16) {
             if (!tl.has_r16) return false;
             st = launch_tl<TlFused<__half>, float, float>(M, code, TlFused<__half>{tl.r16.as<uint4>()},

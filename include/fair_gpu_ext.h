@@ -77,16 +77,19 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
  *         columns: four 7-bit steps beside 4 FP32/FP64 values, or one 16-byte
  *         record of six 5-bit steps and six 2-byte values (f16, q16); 11 with
  *         2 slots in flight, 12 with 4 and the gathers one slot ahead, 13
- *         with 2 and the gathers one slot ahead.
+ *         with 2 and the gathers one slot ahead;
+ *   14    (residual pass, f16 and q16) the tiled copy with 16-byte records of
+ *         six 5-bit steps of the tile-local index and six 2-byte values
+ *         (else code 9).
  * A code whose layout the matrix lacks falls back to the nearest one it has.
  * d_b as in fair_sirt_run_device; d_x is scratch (overwritten). */
 int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
                        int32_t *config);
 
 /* Sets {lanes A, lanes A', layout A, layout A'} of the SIRT passes for the
- * handle's current precision: layout codes 0-13 as listed at
+ * handle's current precision: layout codes 0-14 as listed at
  * fair_sirt_autotune, with 4, 8, 16 or 32 lanes per row for codes 0-4 and
- * 9-13 (unused by 9-13) and 0, 1, 2, 4 or 8 for codes 5-8 (else
+ * 9-14 (unused by 9-14) and 0, 1, 2, 4 or 8 for codes 5-8 (else
  * FAIR_ERR_ARG). No reference counterpart. */
 int fair_sirt_set_lanes(fair_csr h, const int32_t *config);
 

@@ -111,10 +111,10 @@ def test_sliced_geometry(request, fair, oracle, case, prec, cfg):
 
 def test_sliced_lanes_checked(par96, fair):
     """Codes 5-8 take 0 (per chunk), 1, 2, 4 or 8 lanes per row; codes 0-4
-    and 9-13 take 4-32; codes past 13 are refused."""
+    and 9-14 take 4-32; codes past 14 are refused."""
     from fortran_airtools_gb300._clib import check, lib
     A = par96[0]
-    for bad in [(16, 8, 5, 1), (8, 2, 1, 0), (8, 8, 14, 1), (3, 8, 6, 1), (1, 8, 9, 1), (8, 2, 11, 0)]:
+    for bad in [(16, 8, 5, 1), (8, 2, 1, 0), (8, 8, 15, 1), (3, 8, 6, 1), (1, 8, 9, 1), (8, 2, 11, 0)]:
         with pytest.raises(fair.FairError):
             check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(*bad)))
     check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(1, 32, 5, 0)))

@@ -1,14 +1,15 @@
-"""The tiled copy of a ray matrix for the residual pass (layout codes 9, 10):
+"""The tiled copy of a ray matrix for the residual pass (layout codes 9, 10;
+14: the 2-byte forms' 6-entry records of tile-local index steps):
 rows cut into segments by 96 x 96 tiles of the N x N image, each tile of x
 staged in shared memory, one partial sum per segment, the partials of a row
 added in row order by a second kernel. The copy holds the same values as the
 CSR layout, so the iterates differ only by summation order: FP64 within
 1e-12 of the CSR iterate (and 1e-10 of the oracle), the FP32-accumulating
 forms within 2e-6. Images of 3 x 3 tiles with partial edge tiles, a single
-partial tile, a square matrix whose rows jump between tiles (its transpose
-also asks for the delta copy, which it refuses: too many steps outside the
-codes), and a matrix whose columns are not a square image (no tiled copy:
-the pass falls back to the row layouts)."""
+partial tile, a square matrix whose rows jump between tiles (its step
+records and the delta copy of its transpose are refused: too many steps
+outside the codes), and a matrix whose columns are not a square image (no
+tiled copy: the pass falls back to the row layouts)."""
 import ctypes as C
 
 import numpy as np
@@ -74,7 +75,7 @@ def jumpy(fair, oracle):
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32", "f16", "q16"])
-@pytest.mark.parametrize("code", [9, 10])
+@pytest.mark.parametrize("code", [9, 10, 14])
 @pytest.mark.parametrize("case", ["par260", "fan90"])
 def test_tiled_geometry(request, fair, oracle, case, prec, code):
     A, R, b = request.getfixturevalue(case)
@@ -87,10 +88,11 @@ def test_tiled_geometry(request, fair, oracle, case, prec, code):
 
 
 @pytest.mark.parametrize("prec", ["f64", "q16"])
-def test_tiled_jumpy_rows(jumpy, fair, oracle, prec):
+@pytest.mark.parametrize("code", [10, 14])
+def test_tiled_jumpy_rows(jumpy, fair, oracle, prec, code):
     A, R, b = jumpy
     o = fair.airms.options(lbound=0.0)
-    xt = run(fair, A, b, prec, (8, 8, 10, 12), "cimmino", 10, o)
+    xt = run(fair, A, b, prec, (8, 8, code, 12), "cimmino", 10, o)
     xc = run(fair, A, b, prec, (8, 8, 0, 0), "cimmino", 10, o)
     assert np.all(np.isfinite(xt))
     assert rel_err(xt, xc) < TOL_SAME[prec]
