@@ -7,18 +7,23 @@
 // from L2: more L2-to-SM bytes than the matrix itself. Here every row is cut
 // into segments, one per T x T tile of the image that the ray crosses (a
 // convex tile is crossed once, so a segment is a run of the row's entries).
-// The segments of a tile are sorted by length (longest first) and stored in
-// chunks of 32, one lane per segment, slot k of lane l at soff[chunk] + 32k +
+// The segments of a tile are sorted by length (longest first; in row order the
+// chunks mix lengths and idle more lanes: 20% slower) and stored in chunks of
+// 32, one lane per segment, slot k of lane l at soff[chunk] + 32k +
 // l (the sliced layout of rows.cuh with G = 1); a slot holds 4 entries as
 // 16-bit indices into the tile's shared-memory copy (column stride T + 1, so
 // that steps along rows and columns fall in different banks) plus their
 // values. Padding entries and slots point at a zero cell with value 0.
 // A work unit is a run of chunks of one tile: a CTA copies the tile of x into
-// shared memory once and its warps take the unit's chunks, every lane summing
-// its segment into one partial (FP32, or FP64 for the FP64 form) stored at
-// the segment's slot in row order; a second kernel adds each row's partials
-// in that fixed order and applies the residual epilogue, so the result does
-// not depend on scheduling.
+// shared memory once and its warps work through the unit's chunks, every lane
+// summing its segment into one partial (FP32, or FP64 for the FP64 form)
+// stored at the segment's slot in row order; a second kernel adds each row's
+// partials in that fixed order and applies the residual epilogue, so the
+// result does not depend on scheduling. With 2 slots in flight (codes 9, 14)
+// warp w of a CTA reads chunks w, w + W, ... of the unit as one stream, the
+// loads of a chunk's first slots issued during the chunk before; its
+// register use is capped so that 4 CTAs (64 warps) fit an SM. Code 10 keeps 4
+// slots in flight per chunk and claims chunks dynamically.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -441,8 +446,8 @@ struct TlArgs {
 
 // Partial sums of all segments. Persistent CTAs take work units through
 // ctr[0] (reset by the last CTA through ctr[1] for the next launch).
-template <class LD, typename XT, typename ACC, int D>
-__global__ void __launch_bounds__(kTlThreads) k_tl_partials(TlArgs P, LD ldr,
+template <class LD, typename XT, typename ACC, int D, bool CONT>
+__global__ void __launch_bounds__(kTlThreads, sizeof(XT) == 8 ? 1 : 4) k_tl_partials(TlArgs P, LD ldr,
                                                             const XT *__restrict__ x,
                                                             ACC *__restrict__ part, unsigned *ctr) {
     extern __shared__ __align__(16) unsigned char tl_smem[];
@@ -471,35 +476,95 @@ __global__ void __launch_bounds__(kTlThreads) k_tl_partials(TlArgs P, LD ldr,
             s_chunk = U.y;
         }
         __syncthreads();
-        for (;;) {
-            int c = 0;
-            if (lane == 0) c = atomicAdd(&s_chunk, 1);
-            c = __shfl_sync(FULL, c, 0);
-            if (c >= U.z) break;
-            const int64_t o0 = __ldg(P.soff + c);
-            const int len = (int)((__ldg(P.soff + c + 1) - o0) >> 5);
-            const int64_t s0 = o0 + lane;
-            typename LD::Raw ring[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) ring[k] = k < len ? ldr.load(s0 + 32 * k) : LD::none();
-            typename LD::State lst = ldr.init((int64_t)c * 32 + lane);
-            ACC acc = 0;
-            for (int t0 = 0; t0 < len; t0 += D) {
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const int t = t0 + k;
-                    if (t >= len) break;
-                    const typename LD::Raw cur = ring[k];
-                    ring[k] = t + D < len ? ldr.load(s0 + 32 * (int64_t)(t + D)) : LD::none();
-                    uint32_t li[E];
-                    ACC v[E];
-                    ldr.open(cur, lst, lut, li, v);
-#pragma unroll
-                    for (int q = 0; q < E; ++q) acc += (ACC)xs[li[q]] * v[q];
+        if constexpr (CONT) {
+            // the warp's chunks of the unit, c = first + w, first + w + W, ...,
+            // as one stream of slots: the loads of the next chunk's first slots
+            // start during the current chunk (D = 2: a next chunk always has a
+            // slot, so the window never reaches past it)
+            static_assert(D == 2, "the continuous stream keeps 2 slots in flight");
+            const int W = blockDim.x >> 5;
+            struct Meta {
+                int64_t s0;
+                int len, ps;
+                typename LD::State st;
+            };
+            auto meta = [&](int c) -> Meta {
+                Meta r{0, 0, -1, typename LD::State{}};
+                if (c < U.z) {
+                    const int64_t o0 = __ldg(P.soff + c);
+                    r.s0 = o0 + lane;
+                    r.len = (int)((__ldg(P.soff + c + 1) - o0) >> 5);
+                    r.ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
+                    r.st = ldr.init((int64_t)c * 32 + lane);
                 }
+                return r;
+            };
+            int c = U.y + (int)(threadIdx.x >> 5);
+            Meta cur = meta(c), nxt = meta(c + W);
+            // slot q of the stream that starts at chunk c (q < cur.len + nxt.len)
+            auto fetch = [&](int q) {
+                return q < cur.len ? ldr.load(cur.s0 + 32 * (int64_t)q)
+                                   : (q - cur.len < nxt.len ? ldr.load(nxt.s0 + 32 * (int64_t)(q - cur.len))
+                                                            : LD::none());
+            };
+            typename LD::Raw ring[2] = {fetch(0), fetch(1)};
+            while (c < U.z) {
+                ACC acc = 0;
+                for (int t0 = 0; t0 < cur.len; t0 += 2) {
+#pragma unroll
+                    for (int k = 0; k < 2; ++k) {
+                        const int t = t0 + k;
+                        if (t >= cur.len) break;
+                        const typename LD::Raw r = ring[k];
+                        ring[k] = fetch(t + 2);
+                        uint32_t li[E];
+                        ACC v[E];
+                        ldr.open(r, cur.st, lut, li, v);
+#pragma unroll
+                        for (int q = 0; q < E; ++q) acc += (ACC)xs[li[q]] * v[q];
+                    }
+                }
+                if (cur.ps >= 0) part[cur.ps] = acc;
+                if (cur.len & 1) {  // the next chunk's slot 0 sits in ring[1]
+                    const typename LD::Raw t = ring[0];
+                    ring[0] = ring[1];
+                    ring[1] = t;
+                }
+                c += W;
+                cur = nxt;
+                nxt = meta(c + W);
             }
-            const int ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
-            if (ps >= 0) part[ps] = acc;
+        } else {
+            for (;;) {
+                int c = 0;
+                if (lane == 0) c = atomicAdd(&s_chunk, 1);
+                c = __shfl_sync(FULL, c, 0);
+                if (c >= U.z) break;
+                const int64_t o0 = __ldg(P.soff + c);
+                const int len = (int)((__ldg(P.soff + c + 1) - o0) >> 5);
+                const int64_t s0 = o0 + lane;
+                typename LD::Raw ring[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) ring[k] = k < len ? ldr.load(s0 + 32 * k) : LD::none();
+                typename LD::State lst = ldr.init((int64_t)c * 32 + lane);
+                ACC acc = 0;
+                for (int t0 = 0; t0 < len; t0 += D) {
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const int t = t0 + k;
+                        if (t >= len) break;
+                        const typename LD::Raw r = ring[k];
+                        ring[k] = t + D < len ? ldr.load(s0 + 32 * (int64_t)(t + D)) : LD::none();
+                        uint32_t li[E];
+                        ACC v[E];
+                        ldr.open(r, lst, lut, li, v);
+#pragma unroll
+                        for (int q = 0; q < E; ++q) acc += (ACC)xs[li[q]] * v[q];
+                    }
+                }
+                const int ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
+                if (ps >= 0) part[ps] = acc;
+            }
         }
         __syncthreads();  // the tile is rewritten by the next unit
     }
@@ -545,8 +610,8 @@ int launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &
         kernel<<<grid, kTlThreads, smem, s>>>(P, ldr, x, part, ctr);
         return FAIR_OK;
     };
-    if (code == 10) FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 4>));
-    else FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 2>));
+    if (code == 10) FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 4, false>));
+    else FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 2, true>));
     k_tl_rows<ACC, Epi><<<tl_grid(M.m), 256, 0, s>>>(M.m, tl.segbase.as<int64_t>(), part, e);
     FAIR_CUDA(cudaGetLastError());
     return FAIR_OK;
@@ -663,6 +728,7 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
         FAIR_CUDA(cudaStreamSynchronize(s));
         std::vector<unsigned long long> ho((size_t)nkeys + 1, 0ull);
         for (int64_t k = 0; k < nkeys; ++k) ho[k + 1] = ho[k] + hc[k];
+        // a tile's segments longest first (chunks of similar lengths)
         FAIR_CUDA(cudaMemcpyAsync(kpos.p, ho.data(), sizeof(unsigned long long) * nkeys,
                                   cudaMemcpyHostToDevice, s));
         k_tl_scatter<<<tl_grid(S), 256, 0, s>>>(S, key.as<int32_t>(), kpos.as<unsigned long long>(),
