@@ -140,22 +140,28 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-def algorithmic_bytes(nnz, m, n, prec, packed=None):
+def algorithmic_bytes(nnz, m, n, prec, packed=None, codes=(0, 0)):
     """Bytes each SIRT pass must move once (matrix streamed, vectors once).
-    `packed` = (info of A, info of A') when the reduced form runs on the
-    packed index stream: 8 bytes of index per group of 4 entries, 4 padded
-    values per group, 16 bytes per escaped group."""
+    `packed` = (info of A, info of A') when the pass reads a layout built on
+    the packed index stream, `codes` the passes' layout codes. Per group of 4
+    entries: 8 bytes of index + 4 values (packed stream, fused records,
+    sliced and tiled copies; 16 bytes per escaped group); delta copies: 4
+    bytes of steps + 4 values per 4 entries (FP32, FP64), 16 bytes per 6
+    entries (2-byte forms, also the tiled step records of code 14)."""
     sv = VAL_BYTES[prec]
     sx = 8 if prec == "f64" else 4
+    two = prec in ("f16", "q16")
 
-    def matrix(info):
-        if info is None or not info["has"]:
+    def matrix(info, code):
+        if info is None or not info["has"] or code == 0:
             return nnz * (sv + 4)
+        if (11 <= code <= 13) or (code == 14 and two):
+            return nnz * 16 / 6 if two else nnz * (4 + 4 * sv) / 4
         return info["ngroups"] * (8 + 4 * sv) + info["nesc"] * 16
 
     pa, pt = packed if packed else (None, None)
-    pass1 = matrix(pa) + (m + 1) * 8 + n * sx + m * 8 + m * 8 + m * sx
-    pass2 = matrix(pt) + (n + 1) * 8 + m * sx + 2 * n * 8 + (0 if prec == "f64" else n * 4)
+    pass1 = matrix(pa, codes[0]) + (m + 1) * 8 + n * sx + m * 8 + m * 8 + m * sx
+    pass2 = matrix(pt, codes[1]) + (n + 1) * 8 + m * sx + 2 * n * 8 + (0 if prec == "f64" else n * 4)
     return pass1, pass2
 
 
@@ -344,7 +350,13 @@ def run_ours(args):
     hp = args.prec
     head = forms[hp]
     peak, peak_kind = hbm_peak()
-    b1, b2 = algorithmic_bytes(nnz, m, n, hp, packed.get(hp))
+    def pass_codes(prec):
+        pc = forms[prec].get("pass_config")
+        if pc:
+            return tuple(pc["groups_per_lane"])
+        return (0, 0) if prec == "f64" else (1, 1)  # the library's default layouts
+
+    b1, b2 = algorithmic_bytes(nnz, m, n, hp, packed.get(hp), pass_codes(hp))
     dom = 2 if head["pass2_ms"] >= head["pass1_ms"] else 1
     pk = packed.get(hp)
     on_pk = bool(pk and pk[dom - 1])
@@ -357,7 +369,7 @@ def run_ours(args):
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     traffic = traffic_from_profiles(kname, hp, nnz)
     for prec in forms:
-        p1, p2 = algorithmic_bytes(nnz, m, n, prec, packed.get(prec))
+        p1, p2 = algorithmic_bytes(nnz, m, n, prec, packed.get(prec), pass_codes(prec))
         f = forms[prec]
         f["iteration_gbs"] = (p1 + p2) / (f["ms_per_step"] / 1e3) / 1e9
         f["iteration_frac_of_hbm"] = f["iteration_gbs"] / peak
