@@ -324,8 +324,13 @@ __device__ __forceinline__ void dl_rows(const DlArgs &P, const LD &ldr, int32_t 
     finish_chunks(sched, nwarps, lane);
 }
 
+// Resident CTAs per SM asked of the register allocator: with 2 slots in
+// flight the 16-byte records fit 48 registers, so 5 CTAs (40 warps) gather
+// through L1 together; the other variants keep their registers.
+template <class LD, int D> constexpr int kDlMinBlocks = LD::E == 6 && D == 2 ? 5 : 1;
+
 template <class LD, typename XT, int D, int PF, class Epi>
-__global__ void __launch_bounds__(256) k_sirt_resid_dl(DlArgs P, LD ldr, int32_t m, const XT *x,
+__global__ void __launch_bounds__(256, kDlMinBlocks<LD, D>) k_sirt_resid_dl(DlArgs P, LD ldr, int32_t m, const XT *x,
                                                        Epi epi, unsigned *sched) {
     __shared__ int lut[128];
     for (int t = threadIdx.x; t < (1 << LD::B); t += blockDim.x) lut[t] = step_decode<LD::B>((uint32_t)t, P.S, P.L);
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(256) k_sirt_resid_dl(DlArgs P, LD ldr, int32_t
     dl_rows<LD, XT, D, PF>(P, ldr, m, lut, x, epi, sched);
 }
 template <class LD, typename XT, int D, int PF, class Epi>
-__global__ void __launch_bounds__(256) k_sirt_update_dl(DlArgs P, LD ldr, int32_t m, const XT *r,
+__global__ void __launch_bounds__(256, kDlMinBlocks<LD, D>) k_sirt_update_dl(DlArgs P, LD ldr, int32_t m, const XT *r,
                                                         Epi epi, unsigned *sched) {
     __shared__ int lut[128];
     for (int t = threadIdx.x; t < (1 << LD::B); t += blockDim.x) lut[t] = step_decode<LD::B>((uint32_t)t, P.S, P.L);
