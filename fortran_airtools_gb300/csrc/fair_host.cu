@@ -66,7 +66,9 @@ void DevCSR::drop_sliced() {
 void DevCSR::Tiled::release() {
     segbase.release(); soff.release(); pslot.release(); units.release(); idx.release();
     v64.release(); v32.release(); r16.release(); rq.release(); part.release();
-    sstart.release(); send.release();
+    sstart.release(); send.release(); bmin.release(); srow.release();
+    kind = p = nth = W = 0;
+    NA = nab = 1;
     soff6.release(); anc6.release(); code6.release(); side6.release(); r6_16.release(); r6_q.release();
     S6 = 0;
     L6 = 5;
@@ -1260,10 +1262,13 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
 int fair_sirt_launches(fair_csr h, int32_t K, int64_t *launches) {
     if (!h || !launches) return FAIR_ERR_NULL;
     // one FP32 shadow conversion per call in reduced precision, one kernel per
-    // pass and iteration (two for a residual pass on the tiled copy)
-    const int g1 = h->A.sirt_groups[h->prec];
-    const int p1 = (g1 == 9 || g1 == 10 || g1 == 14) && h->A.tl.built() ? 2 : 1;
-    *launches = (h->prec != FAIR_PREC_F64 ? 1 : 0) + (int64_t)(p1 + 1) * K;
+    // pass and iteration (two for a pass on a tiled copy)
+    auto kernels = [](const fair::DevCSR &M, int prec) {
+        const int g = M.sirt_groups[prec];
+        return (g == 9 || g == 10 || g == 14) && M.tl.built() ? 2 : 1;
+    };
+    *launches = (h->prec != FAIR_PREC_F64 ? 1 : 0) +
+                (int64_t)(kernels(h->A, h->prec) + kernels(h->AT, h->prec)) * K;
     return FAIR_OK;
 }
 

@@ -106,6 +106,12 @@ struct DevCSR {
     // by chunks of 32 segments), column indices local to the tile.
     struct Tiled {
         int T = 0, N = 0, ntr = 0;      // tile side, image side, tiles per image column
+        // kind 0: tiles of the columns (A: pixels); kind 1: tiles of the rows
+        // (A': pixels) times blocks of NA angles of the columns (rays a*p + b),
+        // each with a window of W bins per angle starting at bmin
+        int kind = 0, p = 0, nth = 0, NA = 1, nab = 1, W = 0;
+        DevBuf bmin;      // int32 [ntr*ntr*nth] (kind 1)
+        DevBuf srow;      // int32 [nseg] row of each segment (value fills)
         int64_t nseg = 0, nchunks = 0, nslots = 0;
         int32_t nunits = 0;
         DevBuf segbase;   // int64 [m+1] first segment (partial slot) of each row
@@ -225,12 +231,14 @@ int sirt_iterations(const SirtDev &S, int K, cudaStream_t s);
 // One SIRT pass (1: residual over A, 2: update over A') with the forms
 // already made; enqueues one kernel.
 void sirt_pass(const SirtDev &S, int pass, cudaStream_t s);
-// Tiled copy of a ray matrix for A x (tiled.cu; needs n = N^2 and the
-// reduced-precision copy of `prec`); does nothing when n is not a square.
-int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s);
-// Pass 1 of SIRT on the tiled copy (layout code 9; two kernels); false when
-// the matrix has no tiled copy of the form.
-bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int code, cudaStream_t s);
+// Tiled copy of a matrix (tiled.cu) for SIRT pass `pass`: pass 1 reads A,
+// whose columns must be an N x N image; pass 2 reads A', whose rows must be
+// an N x N image and whose columns rays of p bins per angle (p = its stride
+// hint). Does nothing for other matrices.
+int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s);
+// A SIRT pass on the tiled copy (layout codes 9, 10, 14; two kernels); false
+// when the matrix has no tiled copy of the form.
+bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s);
 // Delta copy of the form (sirt_delta.cu): does nothing when too many groups
 // would need the side table.
 int csr_make_delta(DevCSR &A, int prec, cudaStream_t s);

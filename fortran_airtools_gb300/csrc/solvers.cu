@@ -337,7 +337,7 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
     const PkArgs P{M.prow.as<int64_t>(), M.gidx.as<uint2>(), M.gside.as<int4>(), M.pk_S, M.pk_L};
     const int G = M.sirt_lanes[S.prec];
     if (code == 14) {  // the tiled copy's step records (else its 4-entry slots)
-        if (pass == 1 && sirt_pass_tiled(S, M, code, s)) return;
+        if (sirt_pass_tiled(S, M, pass, code, s)) return;
         code = 9;
     }
     if (code >= 11) {
@@ -345,7 +345,7 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
         code = code == 11 ? 5 : 8;  // no delta copy: the sliced copy
     }
     if (code >= 9) {
-        if (pass == 1 && sirt_pass_tiled(S, M, code, s)) return;
+        if (sirt_pass_tiled(S, M, pass, code, s)) return;
         code = 3;  // no tiled copy: the fused records (else the packed stream)
     }
     if (code >= 5) {
@@ -411,7 +411,7 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
             const double *pv = M.pv64.as<double>();
             if (NG == 14) NG = 9;  // step records: 2-byte forms only
             if (NG >= 11 && sirt_pass_delta(S, M, pass, NG, s)) return;
-            if (NG >= 9 && NG <= 10 && pass == 1 && sirt_pass_tiled(S, M, NG, s)) return;
+            if (NG >= 9 && NG <= 10 && sirt_pass_tiled(S, M, pass, NG, s)) return;
             if (NG >= 5 && NG <= 8 && sirt_pass_sliced(S, M, pass, NG, s)) return;
             if (NG >= 9) NG = 1;
             if (NG > 2) NG = 2 - (NG & 1);  // 3, 5 -> 1 group per lane; 4, 6 -> 2
@@ -491,7 +491,8 @@ int sirt_make_forms(DevCSR &A, DevCSR &AT, int prec, cudaStream_t s, bool all, b
             FAIR_TRY(csr_make_sliced(AT, prec, AT.sirt_lanes[prec], s));
         auto tiled = [](int g) { return g == 9 || g == 10 || g == 14; };
         auto delta = [](int g) { return g >= 11 && g <= 13; };
-        if (sliced && tiled(A.sirt_groups[prec])) FAIR_TRY(csr_make_tiled(A, prec, s));
+        if (sliced && tiled(A.sirt_groups[prec])) FAIR_TRY(csr_make_tiled(A, prec, 1, s));
+        if (sliced && tiled(AT.sirt_groups[prec])) FAIR_TRY(csr_make_tiled(AT, prec, 2, s));
         if (sliced && delta(A.sirt_groups[prec])) FAIR_TRY(csr_make_delta(A, prec, s));
         if (sliced && delta(AT.sirt_groups[prec])) FAIR_TRY(csr_make_delta(AT, prec, s));
     }
@@ -556,14 +557,13 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
         if (st != FAIR_OK) break;
         if (M.dl[S.prec == FAIR_PREC_F16 || S.prec == FAIR_PREC_Q16].built)
             for (int code : {11, 12, 13}) cand[nc++] = {code, 8};
-        // the tiled copy (9, 10), residual pass only
-        if (pass == 1) {
-            st = csr_make_tiled(M, S.prec, s);
-            if (st != FAIR_OK) break;
-            if (M.tl.built())
-                for (int code : {9, 10}) cand[nc++] = {code, 8};
-            if (M.tl.built6 && (S.prec == FAIR_PREC_F16 || S.prec == FAIR_PREC_Q16)) cand[nc++] = {14, 8};
-        }
+        // the tiled copy (9, 10; 14 its step records): image tiles of A's
+        // columns for pass 1, pixel tiles x angle blocks of A' for pass 2
+        st = csr_make_tiled(M, S.prec, pass, s);
+        if (st != FAIR_OK) break;
+        if (M.tl.built())
+            for (int code : {9, 10}) cand[nc++] = {code, 8};
+        if (M.tl.built6 && (S.prec == FAIR_PREC_F16 || S.prec == FAIR_PREC_Q16)) cand[nc++] = {14, 8};
         int best_g = M.sirt_lanes[S.prec], best_code = M.sirt_groups[S.prec];
         float best_ms = -1.f;
         float t[56];

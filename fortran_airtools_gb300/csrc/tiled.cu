@@ -26,6 +26,7 @@
 // slots in flight per chunk and claims chunks dynamically.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "fair_internal.cuh"
@@ -36,7 +37,9 @@ namespace fair {
 
 namespace {
 
-constexpr int kTile = 96;           // tile side T (local indices < T*(T+1) + 1 < 2^16)
+constexpr int kTile = 96;           // tile side T of A's image tiles (local indices < T*(T+1) + 1 < 2^16)
+constexpr int kPixTile = 32;        // pixel tile side of A' (the residual windows stay small)
+constexpr int kPixCells = 13000;    // most residuals in a tile of A' (NA * W; 52 KB in FP32)
 constexpr int kUnitChunks = 128;    // most chunks per work unit (the tile copy is reloaded per unit)
 constexpr int kTlThreads = 512;     // threads of a tile CTA
 
@@ -54,14 +57,62 @@ int tl_grid(int64_t work_items) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, cap));
 }
 
-__device__ __forceinline__ int tile_of(int32_t col, int N, int T, int ntr) {
-    const int c = col / N, r = col - c * N;
-    return (c / T) * ntr + r / T;
+// Where an entry (row, col) falls: its tile, and its index in the tile's
+// shared-memory copy of the gathered vector.
+//  kind 0 (A, rows = rays, pass 1): the columns are the pixels of an N x N
+//         image (col = c*N + r); a tile is T x T pixels and its copy holds the
+//         tile's x values with column stride T + 1.
+//  kind 1 (A', rows = pixels, pass 2): the rows are the pixels of an N x N
+//         image and the columns the rays a*p + b (angle a, bin b); a tile is
+//         T x T pixels times a block of NA angles, and its copy holds, for
+//         each of those angles, the W residuals from bin bmin[pixel tile,
+//         angle] on (W covers every bin the tile's pixels see at one angle).
+struct TlGeo {
+    int kind = 0;
+    int N = 0, T = 0, ntr = 0;                  // image side, tile side, tiles per image column
+    int p = 0, nth = 0, NA = 1, nab = 1, W = 0; // kind 1
+    const int32_t *bmin = nullptr;              // kind 1: [ntr*ntr*nth]
+    __host__ __device__ int cells() const { return kind == 0 ? T * (T + 1) : NA * W; }  // the zero cell
+    __host__ __device__ int64_t ntiles() const { return (int64_t)ntr * ntr * (kind == 0 ? 1 : nab); }
+    __device__ __forceinline__ int tile(int64_t row, int32_t col) const {
+        if (kind == 0) {
+            const int c = col / N, r = col - c * N;
+            return (c / T) * ntr + r / T;
+        }
+        const int c = (int)(row / N), r = (int)(row - (int64_t)c * N);
+        return ((c / T) * ntr + r / T) * nab + (col / p) / NA;
+    }
+    __device__ __forceinline__ uint32_t local(int64_t row, int32_t col) const {
+        if (kind == 0) {
+            const int c = col / N, r = col - c * N;
+            return (uint32_t)((c % T) * (T + 1) + r % T);
+        }
+        const int c = (int)(row / N), r = (int)(row - (int64_t)c * N);
+        const int pt = (c / T) * ntr + r / T, a = col / p, b = col - a * p;
+        return (uint32_t)((a % NA) * W + (b - bmin[(int64_t)pt * nth + a]));
+    }
+};
+
+// kind 1: first and last bin each pixel tile sees at each angle (one warp per row).
+__global__ void k_tl_bins(const int64_t *rowptr, int32_t m, const int32_t *col, TlGeo G,
+                          int32_t *bmin, int32_t *bmax) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < m; row += nw) {
+        const int c = (int)(row / G.N), r = (int)(row - (int64_t)c * G.N);
+        const int64_t pt = (c / G.T) * G.ntr + r / G.T;
+        for (int64_t k = rowptr[row] + lane; k < rowptr[row + 1]; k += 32) {
+            const int a = col[k] / G.p, b = col[k] - a * G.p;
+            atomicMin(bmin + pt * G.nth + a, b);
+            atomicMax(bmax + pt * G.nth + a, b);
+        }
+    }
 }
 
 // Segments per row (one warp per row): runs of entries in one tile.
-__global__ void k_tl_count(const int64_t *rowptr, int32_t m, const int32_t *col, int N, int T,
-                           int ntr, int32_t *nseg) {
+__global__ void k_tl_count(const int64_t *rowptr, int32_t m, const int32_t *col, TlGeo G,
+                           int32_t *nseg) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -71,7 +122,7 @@ __global__ void k_tl_count(const int64_t *rowptr, int32_t m, const int32_t *col,
         int carry = -1, count = 0;
         for (int64_t k0 = s; k0 < e; k0 += 32) {
             const int64_t k = k0 + lane;
-            const int t = k < e ? tile_of(col[k], N, T, ntr) : -2;
+            const int t = k < e ? G.tile(row, col[k]) : -2;
             int tp = __shfl_up_sync(FULL, t, 1);
             if (lane == 0) tp = carry;
             count += __popc(__ballot_sync(FULL, k < e && t != tp));
@@ -82,9 +133,8 @@ __global__ void k_tl_count(const int64_t *rowptr, int32_t m, const int32_t *col,
 }
 
 // Segment s of row `row`: tile, first entry, row (segments in row order).
-__global__ void k_tl_segs(const int64_t *rowptr, int32_t m, const int32_t *col, int N, int T,
-                          int ntr, const int64_t *segbase, int32_t *stile, int64_t *sstart,
-                          int32_t *srow) {
+__global__ void k_tl_segs(const int64_t *rowptr, int32_t m, const int32_t *col, TlGeo G,
+                          const int64_t *segbase, int32_t *stile, int64_t *sstart, int32_t *srow) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -95,7 +145,7 @@ __global__ void k_tl_segs(const int64_t *rowptr, int32_t m, const int32_t *col, 
         int carry = -1;
         for (int64_t k0 = s; k0 < e; k0 += 32) {
             const int64_t k = k0 + lane;
-            const int t = k < e ? tile_of(col[k], N, T, ntr) : -2;
+            const int t = k < e ? G.tile(row, col[k]) : -2;
             int tp = __shfl_up_sync(FULL, t, 1);
             if (lane == 0) tp = carry;
             const bool head = k < e && t != tp;
@@ -171,28 +221,23 @@ __global__ void k_tl_ends(int64_t nseg, const int64_t *rowptr, const int64_t *se
     }
 }
 
-// Local index of column `col` in the shared copy of its tile.
-__device__ __forceinline__ uint32_t tl_local(int32_t col, int N, int T) {
-    const int c = col / N, r = col - c * N;
-    return (uint32_t)((c % T) * (T + 1) + r % T);
-}
-
 // The slots of every chunk (one warp per chunk, lane l = segment pslot[32c+l]):
 // slot k of a lane holds entries 4k..4k+3 of its segment. Writes the four
 // local indices of each slot (idx, may be null) and the values through `put`
 // (entries past the segment: the zero cell, source -1).
 template <class Put>
 __global__ void k_tl_fill(int64_t nchunks, const int64_t *soff, const int32_t *pslot,
-                          const int64_t *sstart, const int64_t *send, const int32_t *col, int N,
-                          int T, uint2 *idx, Put put) {
+                          const int64_t *sstart, const int64_t *send, const int32_t *srow,
+                          const int32_t *col, TlGeo G, uint2 *idx, Put put) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t zero = (uint32_t)(T * (T + 1));
+    const uint32_t zero = (uint32_t)G.cells();
     for (int64_t c = warp; c < nchunks; c += nw) {
         const int64_t base = soff[c], len = (soff[c + 1] - base) >> 5;
         const int32_t sg = pslot[c * 32 + lane];
         const int64_t st = sg >= 0 ? sstart[sg] : 0, en = sg >= 0 ? send[sg] : 0;
+        const int64_t row = sg >= 0 ? srow[sg] : 0;
         for (int64_t k = 0; k < len; ++k) {
             uint32_t li[4];
             int64_t src[4];
@@ -200,7 +245,7 @@ __global__ void k_tl_fill(int64_t nchunks, const int64_t *soff, const int32_t *p
             for (int q = 0; q < 4; ++q) {
                 const int64_t e = st + 4 * k + q;
                 const bool in = e < en;
-                li[q] = in ? tl_local(col[e], N, T) : zero;
+                li[q] = in ? G.local(row, col[e]) : zero;
                 src[q] = in ? e : -1;
             }
             const int64_t slot = base + 32 * k + lane;
@@ -254,10 +299,10 @@ struct T6Cands {
     int L[kT6Cand] = {};
 };
 
-__device__ __forceinline__ void t6_locals(const int32_t *col, int64_t e0, int64_t en, int N, int T,
-                                          int (&li)[6]) {
+__device__ __forceinline__ void t6_locals(const int32_t *col, int64_t row, int64_t e0, int64_t en,
+                                          const TlGeo &G, int (&li)[6]) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) li[q] = e0 + q < en ? (int)tl_local(col[e0 + q], N, T) : (q ? li[q - 1] : 0);
+    for (int q = 0; q < 6; ++q) li[q] = e0 + q < en ? (int)G.local(row, col[e0 + q]) : (q ? li[q - 1] : 0);
 }
 
 // Slots of each chunk: 32 x its longest segment in 6-entry slots.
@@ -276,15 +321,16 @@ __global__ void k_t6_len(int64_t nchunks, const int32_t *pslot, const int64_t *s
 
 // Slots whose steps have no code, per candidate (one thread per segment).
 __global__ void k_t6_count(int64_t nseg, const int64_t *sstart, const int64_t *send,
-                           const int32_t *col, int N, int T, T6Cands C, unsigned long long *esc) {
+                           const int32_t *srow, const int32_t *col, TlGeo G, T6Cands C,
+                           unsigned long long *esc) {
     unsigned cnt[kT6Cand] = {0, 0, 0};
     for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg;
          sg += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t st = sstart[sg], en = send[sg];
-        int prev = (int)tl_local(col[st], N, T);
+        const int64_t st = sstart[sg], en = send[sg], row = srow[sg];
+        int prev = (int)G.local(row, col[st]);
         for (int64_t e0 = st; e0 < en; e0 += 6) {
             int li[6];
-            t6_locals(col, e0, en, N, T, li);
+            t6_locals(col, row, e0, en, G, li);
 #pragma unroll
             for (int c = 0; c < kT6Cand; ++c) {
                 uint32_t w;
@@ -300,25 +346,26 @@ __global__ void k_t6_count(int64_t nseg, const int64_t *sstart, const int64_t *s
 
 // Step words, first indices and side table (one warp per chunk).
 __global__ void k_t6_fill(int64_t nchunks, const int64_t *soff6, const int32_t *pslot,
-                          const int64_t *sstart, const int64_t *send, const int32_t *col, int N,
-                          int T, int S, int L, uint32_t *code, int32_t *anc, int4 *side,
-                          unsigned long long cap, unsigned long long *nesc) {
+                          const int64_t *sstart, const int64_t *send, const int32_t *srow,
+                          const int32_t *col, TlGeo G, int S, int L, uint32_t *code, int32_t *anc,
+                          int4 *side, unsigned long long cap, unsigned long long *nesc) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int zero = T * (T + 1);
+    const int zero = G.cells();
     for (int64_t c = warp; c < nchunks; c += nw) {
         const int32_t sg = pslot[c * 32 + lane];
         const int64_t st = sg >= 0 ? sstart[sg] : 0, en = sg >= 0 ? send[sg] : 0;
+        const int64_t row = sg >= 0 ? srow[sg] : 0;
         const int64_t base = soff6[c], len = (soff6[c + 1] - base) >> 5;
-        int prev = en > st ? (int)tl_local(col[st], N, T) : zero;
+        int prev = en > st ? (int)G.local(row, col[st]) : zero;
         anc[c * 32 + lane] = prev;
         for (int64_t k = 0; k < len; ++k) {
             const int64_t e0 = st + 6 * k;
             uint32_t w = 0;  // past the segment: zero steps
             if (e0 < en) {
                 int li[6];
-                t6_locals(col, e0, en, N, T, li);
+                t6_locals(col, row, e0, en, G, li);
                 if (!step_word<6, 5>(li, prev, S, L, w)) {
                     const unsigned long long slot = atomicAdd(nesc, 1ull);
                     if (slot < cap) {
@@ -440,7 +487,7 @@ struct TlArgs {
     const int32_t *pslot;
     const int4 *units;
     int32_t nunits;
-    int N, T, ntr;
+    TlGeo G;
     int S6, L6;  // step code of the 6-entry records
 };
 
@@ -457,7 +504,7 @@ __global__ void __launch_bounds__(kTlThreads, sizeof(XT) == 8 ? 1 : 4) k_tl_part
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int E = LD::E;
     const int lane = threadIdx.x & 31;
-    const int T = P.T, N = P.N;
+    const TlGeo &G = P.G;
     if (threadIdx.x < 32) lut[threadIdx.x] = step_decode<5>((uint32_t)threadIdx.x, P.S6, P.L6);
     for (;;) {
         if (threadIdx.x == 0) s_unit = (int)atomicAdd(ctr, 1u);
@@ -465,14 +512,28 @@ __global__ void __launch_bounds__(kTlThreads, sizeof(XT) == 8 ? 1 : 4) k_tl_part
         const int u = s_unit;
         if (u >= P.nunits) break;
         const int4 U = P.units[u];
-        const int tc = U.x / P.ntr, tr = U.x - tc * P.ntr;
-        for (int e = threadIdx.x; e < T * T; e += blockDim.x) {
-            const int lc = e / T, lr = e - lc * T;
-            const int gr = tr * T + lr, gc = tc * T + lc;
-            xs[lc * (T + 1) + lr] = (gr < N && gc < N) ? x[(int64_t)gc * N + gr] : (XT)0;
+        if (G.kind == 0) {  // the T x T pixels of the tile, column stride T + 1
+            const int T = G.T, N = G.N;
+            const int tc = U.x / G.ntr, tr = U.x - tc * G.ntr;
+            for (int e = threadIdx.x; e < T * T; e += blockDim.x) {
+                const int lc = e / T, lr = e - lc * T;
+                const int gr = tr * T + lr, gc = tc * T + lc;
+                xs[lc * (T + 1) + lr] = (gr < N && gc < N) ? x[(int64_t)gc * N + gr] : (XT)0;
+            }
+        } else {  // W bins per angle of the tile's angle block
+            const int pt = U.x / G.nab, a0 = (U.x - pt * G.nab) * G.NA;
+            for (int e = threadIdx.x; e < G.NA * G.W; e += blockDim.x) {
+                const int ai = e / G.W, a = a0 + ai;
+                XT v = (XT)0;
+                if (a < G.nth) {
+                    const int b = __ldg(G.bmin + (int64_t)pt * G.nth + a) + (e - ai * G.W);
+                    if (b < G.p) v = x[(int64_t)a * G.p + b];
+                }
+                xs[e] = v;
+            }
         }
         if (threadIdx.x == 0) {
-            xs[T * (T + 1)] = (XT)0;  // the zero cell of padding entries
+            xs[G.cells()] = (XT)0;  // the zero cell of padding entries
             s_chunk = U.y;
         }
         __syncthreads();
@@ -589,20 +650,36 @@ __global__ void k_tl_rows(int32_t m, const int64_t *__restrict__ segbase,
     }
 }
 
+TlGeo tl_geo(const DevCSR::Tiled &tl) {
+    TlGeo G;
+    G.kind = tl.kind;
+    G.N = tl.N;
+    G.T = tl.T;
+    G.ntr = tl.ntr;
+    G.p = tl.p;
+    G.nth = tl.nth;
+    G.NA = tl.NA;
+    G.nab = tl.nab;
+    G.W = tl.W;
+    G.bmin = tl.bmin.as<int32_t>();
+    return G;
+}
+
 template <class LD, typename XT, typename ACC, class Epi>
 int launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &e,
               unsigned *ctr, cudaStream_t s) {
     const DevCSR::Tiled &tl = M.tl;
     const DevBuf &soff = LD::E == 6 ? tl.soff6 : tl.soff;
+    const TlGeo G = tl_geo(tl);
     const TlArgs P{soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.units.as<int4>(), tl.nunits,
-                   tl.N, tl.T, tl.ntr, tl.S6, tl.L6};
-    const size_t smem = sizeof(XT) * ((size_t)tl.T * (tl.T + 1) + 1);
+                   G, tl.S6, tl.L6};
+    const size_t smem = sizeof(XT) * ((size_t)G.cells() + 1);
     ACC *part = tl.part.as<ACC>();
     auto run = [&](auto kernel) -> int {
-        static thread_local bool attr_set = false;  // per instantiation
-        if (!attr_set) {
+        static thread_local size_t allowed = 0;  // per instantiation: the largest copy asked so far
+        if (smem > allowed) {
             FAIR_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            attr_set = true;
+            allowed = smem;
         }
         int occ = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kTlThreads, smem);
@@ -629,14 +706,16 @@ int t6_build(DevCSR &A, cudaStream_t s) {
     FAIR_CUDA(cudaGetLastError());
     FAIR_TRY(scan_counts(cnt.as<int32_t>(), nch, tl.soff6.as<int64_t>(), s));
     T6Cands C;
-    C.S[0] = tl.T + 1; C.L[0] = 2;
-    C.S[1] = tl.T + 1; C.L[1] = 3;
+    const TlGeo G = tl_geo(tl);
+    const int S6 = G.kind == 0 ? tl.T + 1 : tl.W;  // a step to the next column / angle of the copy
+    C.S[0] = S6; C.L[0] = 2;
+    C.S[1] = S6; C.L[1] = 3;
     C.S[2] = 0; C.L[2] = 5;
     C.n = 3;
     FAIR_TRY(esc.grow(sizeof(unsigned long long) * (kT6Cand + 1)));
     FAIR_CUDA(cudaMemsetAsync(esc.p, 0, sizeof(unsigned long long) * (kT6Cand + 1), s));
     k_t6_count<<<tl_grid(tl.nseg), 256, 0, s>>>(tl.nseg, tl.sstart.as<int64_t>(), tl.send.as<int64_t>(),
-                                                  A.col.as<int32_t>(), tl.N, tl.T, C,
+                                                  tl.srow.as<int32_t>(), A.col.as<int32_t>(), G, C,
                                                   esc.as<unsigned long long>());
     FAIR_CUDA(cudaGetLastError());
     unsigned long long hesc[kT6Cand] = {};
@@ -659,7 +738,7 @@ int t6_build(DevCSR &A, cudaStream_t s) {
     unsigned long long *ctr = esc.as<unsigned long long>() + kT6Cand;
     k_t6_fill<<<tl_grid(nch * 32), 256, 0, s>>>(
         nch, tl.soff6.as<int64_t>(), tl.pslot.as<int32_t>(), tl.sstart.as<int64_t>(),
-        tl.send.as<int64_t>(), A.col.as<int32_t>(), tl.N, tl.T, C.S[best], C.L[best],
+        tl.send.as<int64_t>(), tl.srow.as<int32_t>(), A.col.as<int32_t>(), G, C.S[best], C.L[best],
         tl.code6.as<uint32_t>(), tl.anc6.as<int32_t>(), tl.side6.as<int4>(), hesc[best], ctr);
     FAIR_CUDA(cudaGetLastError());
     unsigned long long used = 0;
@@ -678,23 +757,70 @@ int t6_build(DevCSR &A, cudaStream_t s) {
 
 }  // namespace
 
-int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
+int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s) {
     if (A.m == 0 || A.nnz == 0) return FAIR_OK;
     DevCSR::Tiled &tl = A.tl;
+    const int kind = pass == 1 ? 0 : 1;
+    if (tl.built() && tl.kind != kind) tl.release();
     if (!tl.built()) {
-        const int64_t N = isqrt_exact(A.n);
-        if (N <= 0) return FAIR_OK;  // not an image of N x N pixels
-        const int T = kTile, ntr = (int)((N + T - 1) / T);
-        const int64_t ntiles = (int64_t)ntr * ntr;
-        const int LB = T / 2 + 2;  // length classes of the sort (segments of up to 2T entries)
-        if (ntiles * LB >= (int64_t(1) << 31)) return FAIR_OK;
+        TlGeo G;
+        G.kind = kind;
+        if (kind == 0) {
+            const int64_t N = isqrt_exact(A.n);
+            if (N <= 0) return FAIR_OK;  // the columns are not an image of N x N pixels
+            G.N = (int)N;
+            G.T = kTile;
+            G.ntr = (int)((N + kTile - 1) / kTile);
+        } else {
+            const int64_t N = isqrt_exact(A.m);
+            const int p = A.stride_hint;
+            // the rows are not an N x N image, or the columns not rays of p bins per angle
+            if (N <= 0 || p <= 0 || A.n % p != 0) return FAIR_OK;
+            G.N = (int)N;
+            G.T = kPixTile;
+            G.ntr = (int)((N + kPixTile - 1) / kPixTile);
+            G.p = p;
+            G.nth = A.n / p;
+            // the bins each pixel tile sees at each angle
+            const size_t nb = (size_t)G.ntr * G.ntr * G.nth;
+            TmpBuf bmax;
+            FAIR_TRY(tl.bmin.grow(sizeof(int32_t) * nb));
+            FAIR_TRY(bmax.grow(sizeof(int32_t) * nb));
+            FAIR_CUDA(cudaMemsetAsync(tl.bmin.p, 0x7F, sizeof(int32_t) * nb, s));
+            FAIR_CUDA(cudaMemsetAsync(bmax.p, 0xFF, sizeof(int32_t) * nb, s));
+            k_tl_bins<<<tl_grid((int64_t)A.m * 32), 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m,
+                                                                 A.col.as<int32_t>(), G,
+                                                                 tl.bmin.as<int32_t>(), bmax.as<int32_t>());
+            FAIR_CUDA(cudaGetLastError());
+            std::vector<int32_t> lo(nb), hi(nb);
+            FAIR_CUDA(cudaMemcpyAsync(lo.data(), tl.bmin.p, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
+            FAIR_CUDA(cudaMemcpyAsync(hi.data(), bmax.p, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));
+            FAIR_CUDA(cudaStreamSynchronize(s));
+            int W = 0;
+            for (size_t i = 0; i < nb; ++i) {
+                if (hi[i] < 0) lo[i] = 0;  // no ray of the tile at this angle
+                else W = std::max(W, hi[i] - lo[i] + 1);
+            }
+            if (W <= 0 || W > kPixCells) { tl.release(); return FAIR_OK; }
+            FAIR_CUDA(cudaMemcpyAsync(tl.bmin.p, lo.data(), sizeof(int32_t) * nb, cudaMemcpyHostToDevice, s));
+            FAIR_CUDA(cudaStreamSynchronize(s));
+            G.W = W;
+            G.NA = std::max(1, std::min(G.nth, kPixCells / W));
+            G.nab = (G.nth + G.NA - 1) / G.NA;
+            G.bmin = tl.bmin.as<int32_t>();
+        }
+        const int T = G.T;
+        const int64_t ntiles = G.ntiles();
+        // length classes of the sort: a ray crosses T x T pixels in up to 2T entries; a
+        // pixel sees up to ~3 rays per angle
+        const int LB = (kind == 0 ? T / 2 : G.NA) + 2;
+        if (ntiles * LB >= (int64_t(1) << 31)) { tl.release(); return FAIR_OK; }
         // segments
         TmpBuf nseg;
         FAIR_TRY(nseg.grow(sizeof(int32_t) * ((size_t)A.m + 1)));
         FAIR_TRY(tl.segbase.grow(sizeof(int64_t) * ((size_t)A.m + 1)));
         k_tl_count<<<tl_grid((int64_t)A.m * 32), 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m,
-                                                              A.col.as<int32_t>(), (int)N, T, ntr,
-                                                              nseg.as<int32_t>());
+                                                              A.col.as<int32_t>(), G, nseg.as<int32_t>());
         FAIR_CUDA(cudaGetLastError());
         FAIR_TRY(scan_counts(nseg.as<int32_t>(), A.m, tl.segbase.as<int64_t>(), s));
         int64_t S = 0;
@@ -702,7 +828,8 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
                                   cudaMemcpyDeviceToHost, s));
         FAIR_CUDA(cudaStreamSynchronize(s));
         if (S <= 0 || S >= (int64_t(1) << 31)) { tl.release(); return FAIR_OK; }
-        TmpBuf stile, sstart, srow, sglen, key, kcnt, kpos, perm;
+        TmpBuf stile, sstart, sglen, key, kcnt, kpos, perm;
+        DevBuf &srow = tl.srow;
         FAIR_TRY(stile.grow(sizeof(int32_t) * S));
         FAIR_TRY(sstart.grow(sizeof(int64_t) * S));
         FAIR_TRY(srow.grow(sizeof(int32_t) * S));
@@ -714,8 +841,8 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
         FAIR_TRY(kpos.grow(sizeof(unsigned long long) * (nkeys + 1)));
         FAIR_CUDA(cudaMemsetAsync(kcnt.p, 0, sizeof(unsigned) * (nkeys + 1), s));
         k_tl_segs<<<tl_grid((int64_t)A.m * 32), 256, 0, s>>>(
-            A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(), (int)N, T, ntr,
-            tl.segbase.as<int64_t>(), stile.as<int32_t>(), sstart.as<int64_t>(), srow.as<int32_t>());
+            A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(), G, tl.segbase.as<int64_t>(),
+            stile.as<int32_t>(), sstart.as<int64_t>(), srow.as<int32_t>());
         k_tl_keys<<<tl_grid(S), 256, 0, s>>>(S, A.rowptr.as<int64_t>(), tl.segbase.as<int64_t>(),
                                               stile.as<int32_t>(), sstart.as<int64_t>(),
                                               srow.as<int32_t>(), LB, sglen.as<int32_t>(),
@@ -784,12 +911,19 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
         FAIR_TRY(tl.idx.grow(sizeof(uint2) * std::max<int64_t>(nslots, 1)));
         k_tl_fill<PutNone><<<tl_grid(nch * 32), 256, 0, s>>>(
             nch, tl.soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.sstart.as<int64_t>(),
-            tl.send.as<int64_t>(), A.col.as<int32_t>(), (int)N, T, tl.idx.as<uint2>(), PutNone{});
+            tl.send.as<int64_t>(), tl.srow.as<int32_t>(), A.col.as<int32_t>(), G, tl.idx.as<uint2>(),
+            PutNone{});
         FAIR_CUDA(cudaGetLastError());
         FAIR_TRY(tl.part.grow(sizeof(double) * S));
-        tl.T = T;
-        tl.N = (int)N;
-        tl.ntr = ntr;
+        tl.kind = G.kind;
+        tl.T = G.T;
+        tl.N = G.N;
+        tl.ntr = G.ntr;
+        tl.p = G.p;
+        tl.nth = G.nth;
+        tl.NA = G.NA;
+        tl.nab = G.nab;
+        tl.W = G.W;
         tl.nseg = S;
         tl.nchunks = nch;
         tl.nslots = nslots;
@@ -798,6 +932,7 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
         FAIR_CUDA(cudaStreamSynchronize(s));  // before the scratch buffers go
     }
     // the values of the form, slot by slot
+    const TlGeo G = tl_geo(tl);
     const int64_t nch = tl.nchunks;
     const int grid = tl_grid(nch * 32);
     const int64_t *soff = tl.soff.as<int64_t>(), *st = tl.sstart.as<int64_t>(), *en = tl.send.as<int64_t>();
@@ -805,13 +940,13 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
     const size_t ns = (size_t)std::max<int64_t>(tl.nslots, 1);
     if (prec == FAIR_PREC_F64 && !tl.has_v64) {
         FAIR_TRY(tl.v64.grow(sizeof(double) * 4 * ns));
-        k_tl_fill<PutF64><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, col, tl.N, tl.T, nullptr,
+        k_tl_fill<PutF64><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, tl.srow.as<int32_t>(), col, G, nullptr,
                                                 PutF64{A.v64.as<double>(), tl.v64.as<double2>()});
         tl.has_v64 = true;
     } else if (prec == FAIR_PREC_F32 && !tl.has_v32) {
         FAIR_TRY(csr_make_lowprec(A, prec, s));
         FAIR_TRY(tl.v32.grow(sizeof(float) * 4 * ns));
-        k_tl_fill<PutF32><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, col, tl.N, tl.T, nullptr,
+        k_tl_fill<PutF32><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, tl.srow.as<int32_t>(), col, G, nullptr,
                                                 PutF32{A.v32.as<float>(), tl.v32.as<float4>()});
         tl.has_v32 = true;
     } else if ((prec == FAIR_PREC_F16 && !tl.has_r16) || (prec == FAIR_PREC_Q16 && !tl.has_rq)) {
@@ -820,7 +955,7 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
         DevBuf &dst = h ? tl.r16 : tl.rq;
         FAIR_TRY(dst.grow(sizeof(uint4) * ns));
         const uint16_t *v = h ? A.v16.as<uint16_t>() : A.vq.as<uint16_t>();
-        k_tl_fill<Put2B><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, col, tl.N, tl.T, nullptr,
+        k_tl_fill<Put2B><<<grid, 256, 0, s>>>(nch, soff, ps, st, en, tl.srow.as<int32_t>(), col, G, nullptr,
                                                Put2B{v, dst.as<uint4>()});
         (h ? tl.has_r16 : tl.has_rq) = true;
     }
@@ -844,49 +979,51 @@ int csr_make_tiled(DevCSR &A, int prec, cudaStream_t s) {
     return FAIR_OK;
 }
 
-bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int code, cudaStream_t s) {
+bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s) {
     const DevCSR::Tiled &tl = M.tl;
-    if (!tl.built() || !S.sched) return false;  // the work-unit counters are S.sched
-    int st = FAIR_OK;
+    // the work-unit counters are S.sched; pass 1 reads a copy of A, pass 2 one of A'
+    if (!tl.built() || !S.sched || tl.kind != (pass == 1 ? 0 : 1)) return false;
     if (S.prec == FAIR_PREC_F64) {
         if (!tl.has_v64) return false;
-        st = launch_tl<TlSplit<double>, double, double>(
-            M, code, TlSplit<double>{tl.idx.as<uint2>(), tl.v64.as<double>()}, S.x,
-            EpiResidF64{S.b, S.Minv, (double *)S.r}, S.sched, s);
-    } else {
-        const double scale = S.prec == FAIR_PREC_Q16 ? M.qscale : 1.0;
-        const EpiResidLP e{S.b, S.Minv, (float *)S.r, scale};
-        if (S.prec == FAIR_PREC_F32) {
-            if (!tl.has_v32) return false;
-            st = launch_tl<TlSplit<float>, float, float>(
-                M, code, TlSplit<float>{tl.idx.as<uint2>(), tl.v32.as<float>()}, S.x32, e, S.sched, s);
-        } else if (code == 14 && tl.built6 && (S.prec == FAIR_PREC_F16 ? tl.has6_16 : tl.has6_q)) {
-            const int32_t *anc = tl.anc6.as<int32_t>();
-            const int4 *side = tl.side6.as<int4>();
-            if (S.prec == FAIR_PREC_F16)
-                st = launch_tl<TlStep6<__half>, float, float>(
-                    M, code, TlStep6<__half>{tl.r6_16.as<uint4>(), anc, side}, S.x32, e, S.sched, s);
-            else if (M.qsigned)
-                st = launch_tl<TlStep6<int16_t>, float, float>(
-                    M, code, TlStep6<int16_t>{tl.r6_q.as<uint4>(), anc, side}, S.x32, e, S.sched, s);
-            else
-                st = launch_tl<TlStep6<uint16_t>, float, float>(
-                    M, code, TlStep6<uint16_t>{tl.r6_q.as<uint4>(), anc, side}, S.x32, e, S.sched, s);
-        } else if (S.prec == FAIR_PREC_F16) {
-            if (!tl.has_r16) return false;
-            st = launch_tl<TlFused<__half>, float, float>(M, code, TlFused<__half>{tl.r16.as<uint4>()},
-                                                          S.x32, e, S.sched, s);
-        } else {
-            if (!tl.has_rq) return false;
-            if (M.qsigned)
-                st = launch_tl<TlFused<int16_t>, float, float>(
-                    M, code, TlFused<int16_t>{tl.rq.as<uint4>()}, S.x32, e, S.sched, s);
-            else
-                st = launch_tl<TlFused<uint16_t>, float, float>(
-                    M, code, TlFused<uint16_t>{tl.rq.as<uint4>()}, S.x32, e, S.sched, s);
-        }
+        const TlSplit<double> ld{tl.idx.as<uint2>(), tl.v64.as<double>()};
+        const int st = pass == 1
+            ? launch_tl<TlSplit<double>, double, double>(M, code, ld, S.x, EpiResidF64{S.b, S.Minv, (double *)S.r},
+                                                         S.sched, s)
+            : launch_tl<TlSplit<double>, double, double>(M, code, ld, (const double *)S.r,
+                                                         EpiUpdateF64{S.D, S.x, S.omg, S.lb, S.ub, S.bmode},
+                                                         S.sched, s);
+        return st == FAIR_OK;
     }
-    return st == FAIR_OK;
+    const double scale = S.prec == FAIR_PREC_Q16 ? M.qscale : 1.0;
+    const float *xv = pass == 1 ? S.x32 : (const float *)S.r;
+    auto run = [&](const auto &ld) -> bool {
+        using LD = std::decay_t<decltype(ld)>;
+        const int st = pass == 1
+            ? launch_tl<LD, float, float>(M, code, ld, xv, EpiResidLP{S.b, S.Minv, (float *)S.r, scale}, S.sched, s)
+            : launch_tl<LD, float, float>(M, code, ld, xv,
+                                          EpiUpdateLP{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale},
+                                          S.sched, s);
+        return st == FAIR_OK;
+    };
+    if (S.prec == FAIR_PREC_F32) {
+        if (!tl.has_v32) return false;
+        return run(TlSplit<float>{tl.idx.as<uint2>(), tl.v32.as<float>()});
+    }
+    const bool h = S.prec == FAIR_PREC_F16;
+    if (code == 14 && tl.built6 && (h ? tl.has6_16 : tl.has6_q)) {
+        const int32_t *anc = tl.anc6.as<int32_t>();
+        const int4 *side = tl.side6.as<int4>();
+        if (h) return run(TlStep6<__half>{tl.r6_16.as<uint4>(), anc, side});
+        if (M.qsigned) return run(TlStep6<int16_t>{tl.r6_q.as<uint4>(), anc, side});
+        return run(TlStep6<uint16_t>{tl.r6_q.as<uint4>(), anc, side});
+    }
+    if (h) {
+        if (!tl.has_r16) return false;
+        return run(TlFused<__half>{tl.r16.as<uint4>()});
+    }
+    if (!tl.has_rq) return false;
+    if (M.qsigned) return run(TlFused<int16_t>{tl.rq.as<uint4>()});
+    return run(TlFused<uint16_t>{tl.rq.as<uint4>()});
 }
 
 }  // namespace fair

@@ -1,8 +1,9 @@
-"""The tiled copy of a ray matrix for the residual pass (layout codes 9, 10;
-14: the 2-byte forms' 6-entry records of tile-local index steps):
-rows cut into segments by 96 x 96 tiles of the N x N image, each tile of x
-staged in shared memory, one partial sum per segment, the partials of a row
-added in row order by a second kernel. The copy holds the same values as the
+"""The tiled copies (layout codes 9, 10; 14: the 2-byte forms' 6-entry
+records of tile-local index steps). Pass 1 reads A cut by 96 x 96 tiles of the
+N x N image (each tile of x staged in shared memory); pass 2 reads A' cut by
+32 x 32 pixel tiles times blocks of angles (each tile's window of residual
+bins staged in shared memory); one partial sum per segment, the partials of a
+row added in row order by a second kernel. The copy holds the same values as the
 CSR layout, so the iterates differ only by summation order: FP64 within
 1e-12 of the CSR iterate (and 1e-10 of the oracle), the FP32-accumulating
 forms within 2e-6. Images of 3 x 3 tiles with partial edge tiles, a single
@@ -75,12 +76,12 @@ def jumpy(fair, oracle):
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32", "f16", "q16"])
-@pytest.mark.parametrize("code", [9, 10, 14])
+@pytest.mark.parametrize("codes", [(9, 0), (10, 0), (14, 0), (0, 9), (9, 10), (14, 14)])
 @pytest.mark.parametrize("case", ["par260", "fan90"])
-def test_tiled_geometry(request, fair, oracle, case, prec, code):
+def test_tiled_geometry(request, fair, oracle, case, prec, codes):
     A, R, b = request.getfixturevalue(case)
     o = fair.airms.options(lbound=0.0, ubound=1.0)
-    xt = run(fair, A, b, prec, (8, 8, code, 0), "sart", 15, o)
+    xt = run(fair, A, b, prec, (8, 8) + codes, "sart", 15, o)
     xc = run(fair, A, b, prec, (8, 8, 0, 0), "sart", 15, o)
     assert rel_err(xt, xc) < TOL_SAME[prec]
     xr = oracle.sirt("sart", R, b, 15, opts=oracle.options(lbound=0.0, ubound=1.0))
