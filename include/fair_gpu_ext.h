@@ -67,20 +67,22 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
  *         in flight per warp; lanes per row 0 chooses G per chunk of 32 rows
  *         from the rows' column steps (8 when most steps are +-1, else 1);
  *   7, 8  as 5, 6 with the gathers of x issued one step ahead;
- *   9, 10 (the residual pass over A only, for A with n = N^2 columns) the
- *         tiled copy: rows cut into segments by 128 x 128 tiles of the image,
- *         each tile of x staged in shared memory by the CTA that works on it,
- *         16-bit tile-local indices, one partial sum per segment added up per
- *         row in a second kernel; 2 or 4 steps in flight;
+ *   9, 10 the tiled copy: pass 1 (A, whose n columns are an N x N image)
+ *         cuts the rows by 96 x 96 tiles of the image and stages each tile
+ *         of x in shared memory; pass 2 (A', whose rows are an N x N image
+ *         and whose columns are rays of p bins per angle, p its stride hint)
+ *         cuts the rows by 32 x 32 pixel tiles times blocks of angles and
+ *         stages each tile's window of residual bins; 16-bit tile-local
+ *         indices, one partial sum per segment added up per row in a second
+ *         kernel; 2 slots in flight (9) or 4 (10);
  *   11-13 the delta copy: the sliced layout with one lane per row whose
  *         slots hold column steps from the row's previous entry instead of
  *         columns: four 7-bit steps beside 4 FP32/FP64 values, or one 16-byte
  *         record of six 5-bit steps and six 2-byte values (f16, q16); 11 with
  *         2 slots in flight, 12 with 4 and the gathers one slot ahead, 13
  *         with 2 and the gathers one slot ahead;
- *   14    (residual pass, f16 and q16) the tiled copy with 16-byte records of
- *         six 5-bit steps of the tile-local index and six 2-byte values
- *         (else code 9).
+ *   14    (f16 and q16) the tiled copy with 16-byte records of six 5-bit
+ *         steps of the tile-local index and six 2-byte values (else code 9).
  * A code whose layout the matrix lacks falls back to the nearest one it has.
  * d_b as in fair_sirt_run_device; d_x is scratch (overwritten). */
 int fair_sirt_autotune(fair_csr h, const double *d_b, double *d_x, int32_t reps,
