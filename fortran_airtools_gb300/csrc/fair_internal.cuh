@@ -101,9 +101,10 @@ struct DevCSR {
     DevBuf sv64, sv32;         // 4 values per slot
     DevBuf sf16, sfq;          // fused records per slot (2-byte forms)
     bool hassidx = false, hassv64 = false, hassv32 = false, hassf16 = false, hassfq = false;
-    // Tiled copy for A x (tiled.cu): rows cut into segments by T x T tiles of
-    // the N x N image, segments stored per tile (one lane per segment, sliced
-    // by chunks of 32 segments), column indices local to the tile.
+    // Tiled copy (tiled.cu): rows cut into segments by tiles whose part of the
+    // gathered vector fits in shared memory, segments stored per tile (one
+    // lane per segment, sliced by chunks of 32 segments), column indices local
+    // to the tile's copy.
     struct Tiled {
         int T = 0, N = 0, ntr = 0;      // tile side, image side, tiles per image column
         // kind 0: tiles of the columns (A: pixels); kind 1: tiles of the rows

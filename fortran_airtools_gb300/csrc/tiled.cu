@@ -1,12 +1,16 @@
-// tiled.cu -- A x on a copy of a ray matrix cut by image tiles (layout codes 9,
-// 10 and 14 of the residual pass of SIRT, AIRMs.f90:1089-1110).
+// tiled.cu -- the SIRT passes (AIRMs.f90:1089-1110) on copies of A and A' cut
+// by tiles whose part of the gathered vector fits in shared memory (layout
+// codes 9, 10 and 14).
 //
 // The columns of a ray matrix are the pixels of an N x N image (column j =
 // c*N + r). On the row layouts the x entries a warp gathers are scattered
 // along whole rays, so half of them miss L1 and each costs a 32-byte sector
-// from L2: more L2-to-SM bytes than the matrix itself. Here every row is cut
-// into segments, one per T x T tile of the image that the ray crosses (a
+// from L2: more L2-to-SM bytes than the matrix itself. Here every row of A is
+// cut into segments, one per T x T tile of the image that the ray crosses (a
 // convex tile is crossed once, so a segment is a run of the row's entries).
+// A' (rows = pixels, columns = rays a*p + b) is cut the other way round: by
+// tiles of its rows (32 x 32 pixels) times blocks of angles, whose copy holds
+// a window of residual bins per angle (TlGeo below).
 // The segments of a tile are sorted by length (longest first; in row order the
 // chunks mix lengths and idle more lanes: 20% slower) and stored in chunks of
 // 32, one lane per segment, slot k of lane l at soff[chunk] + 32k +
