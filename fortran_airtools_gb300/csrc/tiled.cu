@@ -30,6 +30,7 @@
 // slots in flight per chunk and claims chunks dynamically.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -495,6 +496,33 @@ struct TlArgs {
     int S6, L6;  // step code of the 6-entry records
 };
 
+// The shared copy of unit U's tile of the gathered vector x (all threads of
+// the CTA), zero cell included.
+template <typename XT>
+__device__ __forceinline__ void tl_fill_tile(const TlGeo &G, int4 U, const XT *__restrict__ x, XT *xs) {
+    if (G.kind == 0) {  // the T x T pixels of the tile, column stride T + 1
+        const int T = G.T, N = G.N;
+        const int tc = U.x / G.ntr, tr = U.x - tc * G.ntr;
+        for (int e = threadIdx.x; e < T * T; e += blockDim.x) {
+            const int lc = e / T, lr = e - lc * T;
+            const int gr = tr * T + lr, gc = tc * T + lc;
+            xs[lc * (T + 1) + lr] = (gr < N && gc < N) ? x[(int64_t)gc * N + gr] : (XT)0;
+        }
+    } else {  // W bins per angle of the tile's angle block
+        const int pt = U.x / G.nab, a0 = (U.x - pt * G.nab) * G.NA;
+        for (int e = threadIdx.x; e < G.NA * G.W; e += blockDim.x) {
+            const int ai = e / G.W, a = a0 + ai;
+            XT v = (XT)0;
+            if (a < G.nth) {
+                const int b = __ldg(G.bmin + (int64_t)pt * G.nth + a) + (e - ai * G.W);
+                if (b < G.p) v = x[(int64_t)a * G.p + b];
+            }
+            xs[e] = v;
+        }
+    }
+    if (threadIdx.x == 0) xs[G.cells()] = (XT)0;  // the zero cell of padding entries
+}
+
 // Partial sums of all segments. Persistent CTAs take work units through
 // ctr[0] (reset by the last CTA through ctr[1] for the next launch).
 template <class LD, typename XT, typename ACC, int D, bool CONT>
@@ -516,30 +544,8 @@ __global__ void __launch_bounds__(kTlThreads, sizeof(XT) == 8 ? 1 : 4) k_tl_part
         const int u = s_unit;
         if (u >= P.nunits) break;
         const int4 U = P.units[u];
-        if (G.kind == 0) {  // the T x T pixels of the tile, column stride T + 1
-            const int T = G.T, N = G.N;
-            const int tc = U.x / G.ntr, tr = U.x - tc * G.ntr;
-            for (int e = threadIdx.x; e < T * T; e += blockDim.x) {
-                const int lc = e / T, lr = e - lc * T;
-                const int gr = tr * T + lr, gc = tc * T + lc;
-                xs[lc * (T + 1) + lr] = (gr < N && gc < N) ? x[(int64_t)gc * N + gr] : (XT)0;
-            }
-        } else {  // W bins per angle of the tile's angle block
-            const int pt = U.x / G.nab, a0 = (U.x - pt * G.nab) * G.NA;
-            for (int e = threadIdx.x; e < G.NA * G.W; e += blockDim.x) {
-                const int ai = e / G.W, a = a0 + ai;
-                XT v = (XT)0;
-                if (a < G.nth) {
-                    const int b = __ldg(G.bmin + (int64_t)pt * G.nth + a) + (e - ai * G.W);
-                    if (b < G.p) v = x[(int64_t)a * G.p + b];
-                }
-                xs[e] = v;
-            }
-        }
-        if (threadIdx.x == 0) {
-            xs[G.cells()] = (XT)0;  // the zero cell of padding entries
-            s_chunk = U.y;
-        }
+        tl_fill_tile(G, U, x, xs);
+        if (threadIdx.x == 0) s_chunk = U.y;
         __syncthreads();
         if constexpr (CONT) {
             // the warp's chunks of the unit, c = first + w, first + w + W, ...,
@@ -669,9 +675,30 @@ TlGeo tl_geo(const DevCSR::Tiled &tl) {
     return G;
 }
 
+// Raise a kernel's dynamic shared-memory limit to `bytes` if it is lower
+// (never lowers it: the tiled copies of A and A' launch the same kernels with
+// tiles of different sizes).
+cudaError_t smem_allow(const void *kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, size_t>> set;
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto &k : set)
+        if (k.first == kernel) {
+            if (bytes <= k.second) return cudaSuccess;
+            const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e == cudaSuccess) k.second = bytes;
+            return e;
+        }
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) set.emplace_back(kernel, bytes);
+    return e;
+}
+
+// Launches one pass on the tiled copy (partials, then row sums); errors are
+// left for the caller's cudaGetLastError.
 template <class LD, typename XT, typename ACC, class Epi>
-int launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &e,
-              unsigned *ctr, cudaStream_t s) {
+void launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &e,
+               unsigned *ctr, cudaStream_t s) {
     const DevCSR::Tiled &tl = M.tl;
     const DevBuf &soff = LD::E == 6 ? tl.soff6 : tl.soff;
     const TlGeo G = tl_geo(tl);
@@ -679,23 +706,21 @@ int launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi &
                    G, tl.S6, tl.L6};
     const size_t smem = sizeof(XT) * ((size_t)G.cells() + 1);
     ACC *part = tl.part.as<ACC>();
-    auto run = [&](auto kernel) -> int {
-        static thread_local size_t allowed = 0;  // per instantiation: the largest copy asked so far
-        if (smem > allowed) {
-            FAIR_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            allowed = smem;
-        }
+    auto run = [&](auto kernel) -> cudaError_t {
+        const cudaError_t e = smem_allow(reinterpret_cast<const void *>(kernel), smem);
+        if (e != cudaSuccess) return e;
         int occ = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kTlThreads, smem);
         const int grid = std::max(1, std::min(sm_count() * std::max(occ, 1), (int)tl.nunits));
         kernel<<<grid, kTlThreads, smem, s>>>(P, ldr, x, part, ctr);
-        return FAIR_OK;
+        return cudaPeekAtLastError();
     };
-    if (code == 10) FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 4, false>));
-    else FAIR_TRY(run(k_tl_partials<LD, XT, ACC, 2, true>));
-    k_tl_rows<ACC, Epi><<<tl_grid(M.m), 256, 0, s>>>(M.m, tl.segbase.as<int64_t>(), part, e);
-    FAIR_CUDA(cudaGetLastError());
-    return FAIR_OK;
+    const cudaError_t err = code == 10 ? run(k_tl_partials<LD, XT, ACC, 4, false>)
+                                       : run(k_tl_partials<LD, XT, ACC, 2, true>);
+    // the row sums only after partials that were launched; a failure stays
+    // the runtime's last error, which the caller's check reports
+    if (err == cudaSuccess)
+        k_tl_rows<ACC, Epi><<<tl_grid(M.m), 256, 0, s>>>(M.m, tl.segbase.as<int64_t>(), part, e);
 }
 
 // Index part of the 6-entry step records (after the tiled copy is built).
@@ -985,29 +1010,33 @@ int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s) {
 
 bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s) {
     const DevCSR::Tiled &tl = M.tl;
-    // the work-unit counters are S.sched; pass 1 reads a copy of A, pass 2 one of A'
+    // the work-unit counters are S.sched; pass 1 reads a copy of A, pass 2 one of A'.
+    // Once launched, the pass is not repeated on another layout: a launch error
+    // stays the runtime's last error for the caller to report.
     if (!tl.built() || !S.sched || tl.kind != (pass == 1 ? 0 : 1)) return false;
     if (S.prec == FAIR_PREC_F64) {
         if (!tl.has_v64) return false;
         const TlSplit<double> ld{tl.idx.as<uint2>(), tl.v64.as<double>()};
-        const int st = pass == 1
-            ? launch_tl<TlSplit<double>, double, double>(M, code, ld, S.x, EpiResidF64{S.b, S.Minv, (double *)S.r},
-                                                         S.sched, s)
-            : launch_tl<TlSplit<double>, double, double>(M, code, ld, (const double *)S.r,
-                                                         EpiUpdateF64{S.D, S.x, S.omg, S.lb, S.ub, S.bmode},
-                                                         S.sched, s);
-        return st == FAIR_OK;
+        if (pass == 1)
+            launch_tl<TlSplit<double>, double, double>(M, code, ld, S.x, EpiResidF64{S.b, S.Minv, (double *)S.r},
+                                                       S.sched, s);
+        else
+            launch_tl<TlSplit<double>, double, double>(M, code, ld, (const double *)S.r,
+                                                       EpiUpdateF64{S.D, S.x, S.omg, S.lb, S.ub, S.bmode},
+                                                       S.sched, s);
+        return true;
     }
     const double scale = S.prec == FAIR_PREC_Q16 ? M.qscale : 1.0;
     const float *xv = pass == 1 ? S.x32 : (const float *)S.r;
     auto run = [&](const auto &ld) -> bool {
         using LD = std::decay_t<decltype(ld)>;
-        const int st = pass == 1
-            ? launch_tl<LD, float, float>(M, code, ld, xv, EpiResidLP{S.b, S.Minv, (float *)S.r, scale}, S.sched, s)
-            : launch_tl<LD, float, float>(M, code, ld, xv,
-                                          EpiUpdateLP{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale},
-                                          S.sched, s);
-        return st == FAIR_OK;
+        if (pass == 1)
+            launch_tl<LD, float, float>(M, code, ld, xv, EpiResidLP{S.b, S.Minv, (float *)S.r, scale}, S.sched, s);
+        else
+            launch_tl<LD, float, float>(M, code, ld, xv,
+                                        EpiUpdateLP{S.D, S.x, S.x32, S.omg, S.lb, S.ub, S.bmode, scale}, S.sched,
+                                        s);
+        return true;
     };
     if (S.prec == FAIR_PREC_F32) {
         if (!tl.has_v32) return false;
