@@ -413,9 +413,15 @@ __global__ void k_t6_rec(int64_t nchunks, const int64_t *soff6, const int32_t *p
 
 // ---- the pass ---------------------------------------------------------------
 // Slot loaders: four local indices and four values.
-// E entries per slot; State is what a lane carries from slot to slot.
+// E entries per slot; State is what a lane carries from slot to slot; CTAS is
+// the number of 512-thread CTAs per SM the pass is compiled for (its register
+// budget: 4 -> 32 registers, 3 -> 40, 1 -> 128). Measured at N = 1024: the
+// 2-byte forms run fastest with 4 although they spill a few words (3: +1.5%
+// per pass, 2: +20%), FP32 with 3 (pass 2 1.03 -> 0.90 ms against 4), FP64
+// with the registers it needs (57 for D = 2, so two CTAs still fit).
 template <typename VT> struct TlFused {
     static constexpr int E = 4;
+    static constexpr int CTAS = 4;
     const uint4 *rec;
     using Raw = uint4;
     struct State {};
@@ -430,6 +436,7 @@ template <typename VT> struct TlFused {
 };
 template <typename VT> struct TlStep6 {  // 6-entry step records
     static constexpr int E = 6;
+    static constexpr int CTAS = 4;
     const uint4 *rec;
     const int32_t *anc;
     const int4 *side;
@@ -460,6 +467,7 @@ template <typename VT> struct TlStep6 {  // 6-entry step records
 };
 template <typename VT> struct TlSplit {
     static constexpr int E = 4;
+    static constexpr int CTAS = sizeof(VT) == 8 ? 1 : 3;
     const uint2 *idx;
     const VT *val;
     struct State {};
@@ -526,7 +534,7 @@ __device__ __forceinline__ void tl_fill_tile(const TlGeo &G, int4 U, const XT *_
 // Partial sums of all segments. Persistent CTAs take work units through
 // ctr[0] (reset by the last CTA through ctr[1] for the next launch).
 template <class LD, typename XT, typename ACC, int D, bool CONT>
-__global__ void __launch_bounds__(kTlThreads, sizeof(XT) == 8 ? 1 : 4) k_tl_partials(TlArgs P, LD ldr,
+__global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, LD ldr,
                                                             const XT *__restrict__ x,
                                                             ACC *__restrict__ part, unsigned *ctr) {
     extern __shared__ __align__(16) unsigned char tl_smem[];
