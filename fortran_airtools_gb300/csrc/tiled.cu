@@ -415,49 +415,66 @@ __global__ void k_t6_rec(int64_t nchunks, const int64_t *soff6, const int32_t *p
 // Slot loaders: four local indices and four values.
 // E entries per slot; State is what a lane carries from slot to slot; CTAS is
 // the number of 512-thread CTAs per SM the pass is compiled for (its register
-// budget: 4 -> 32 registers, 3 -> 40, 1 -> 128). Measured at N = 1024: the
-// 2-byte forms run fastest with 4 although they spill a few words (3: +1.5%
-// per pass, 2: +20%), FP32 with 3 (pass 2 1.03 -> 0.90 ms against 4), FP64
-// with the registers it needs (57 for D = 2, so two CTAs still fit).
+// budget: 4 -> 32 registers, 3 -> 40, 2 -> 64). Measured at N = 1024: 3 for the
+// 2-byte forms and FP32 (FP32 pass 2 0.90 ms against 1.03 ms with 4; 2 is 20%
+// slower), 2 for FP64 (64 registers, no spills at D = 2).
 template <typename VT> struct TlFused {
     static constexpr int E = 4;
-    static constexpr int CTAS = 4;
+    static constexpr int CTAS = 3;
     const uint4 *rec;
     using Raw = uint4;
     struct State {};
     __device__ __forceinline__ State init(int64_t) const { return {}; }
     __device__ __forceinline__ Raw load(int64_t j) const { return ld_stream(rec + j); }
     __device__ __forceinline__ static Raw none() { return make_uint4(0u, 0u, 0u, 0u); }
-    __device__ __forceinline__ void open(const Raw &r, State &, const int *, uint32_t (&li)[4],
-                                         float (&v)[4]) const {
+    __device__ __forceinline__ void open(const Raw &r, State &, uint32_t (&li)[4], float (&v)[4]) const {
         li[0] = r.x & 0xFFFFu; li[1] = r.x >> 16; li[2] = r.y & 0xFFFFu; li[3] = r.y >> 16;
         Conv2B<VT>::to(r.z, r.w, v);
     }
 };
 template <typename VT> struct TlStep6 {  // 6-entry step records
     static constexpr int E = 6;
-    static constexpr int CTAS = 4;
+    static constexpr int CTAS = 3;
     const uint4 *rec;
     const int32_t *anc;
     const int4 *side;
+    int L;       // bits of a code's low field
+    int hs, hm;  // shift of its high field, and the high field's step (0 when L = 5)
     using Raw = uint4;
     struct State {
         int li;  // the lane's last local index
     };
+    TlStep6(const uint4 *r, const int32_t *a, const int4 *sd, int S, int L_)
+        : rec(r), anc(a), side(sd), L(L_), hs(L_ >= 5 ? 31 : 27 + L_), hm(L_ >= 5 ? 0 : S) {}
+    // the step of code q of word w: step_decode<5>((w >> 5q) & 31, S, L) by
+    // shifts alone (the signed low L bits, the signed high 5 - L bits)
+    __device__ __forceinline__ int step(uint32_t w, int q) const {
+        const int lo = (int)(w << (32 - L - 5 * q)) >> (32 - L);
+        const int hi = (int)(w << (27 - 5 * q)) >> hs;
+        return lo + hi * hm;
+    }
     __device__ __forceinline__ State init(int64_t lanepos) const { return {__ldg(anc + lanepos)}; }
     __device__ __forceinline__ Raw load(int64_t j) const { return ld_stream(rec + j); }
     __device__ __forceinline__ static Raw none() { return make_uint4(0u, 0u, 0u, 0u); }
-    __device__ __forceinline__ void open(const Raw &r, State &st, const int *lut, uint32_t (&li)[6],
-                                         float (&v)[6]) const {
+    __device__ __forceinline__ void open(const Raw &r, State &st, uint32_t (&li)[6], float (&v)[6]) const {
         const uint32_t w = r.x;
         if (w & kStepEsc) {
             const int4 a = __ldg(side + 2 * (int64_t)(w & kStepSlot));
             const int4 b = __ldg(side + 2 * (int64_t)(w & kStepSlot) + 1);
             li[0] = a.x; li[1] = a.y; li[2] = a.z; li[3] = a.w; li[4] = b.x; li[5] = b.y;
         } else {
-            li[0] = (uint32_t)(st.li + lut[w & 31u]);
+            int d[6];
 #pragma unroll
-            for (int q = 1; q < 6; ++q) li[q] = li[q - 1] + lut[(w >> (5 * q)) & 31u];
+            for (int q = 0; q < 6; ++q) d[q] = step(w, q);
+            // running sums in a tree of depth 3 instead of a chain of 6
+            const int s01 = d[0] + d[1], s23 = d[2] + d[3], s45 = d[4] + d[5];
+            const int b1 = st.li + s01, b3 = b1 + s23;
+            li[0] = (uint32_t)(st.li + d[0]);
+            li[1] = (uint32_t)b1;
+            li[2] = (uint32_t)(b1 + d[2]);
+            li[3] = (uint32_t)b3;
+            li[4] = (uint32_t)(b3 + d[4]);
+            li[5] = (uint32_t)(b3 + s45);
         }
         st.li = (int)li[5];
         Conv2B<VT>::two(r.y, v[0], v[1]);
@@ -467,7 +484,7 @@ template <typename VT> struct TlStep6 {  // 6-entry step records
 };
 template <typename VT> struct TlSplit {
     static constexpr int E = 4;
-    static constexpr int CTAS = sizeof(VT) == 8 ? 1 : 3;
+    static constexpr int CTAS = sizeof(VT) == 8 ? 2 : 3;
     const uint2 *idx;
     const VT *val;
     struct State {};
@@ -488,8 +505,7 @@ template <typename VT> struct TlSplit {
         r.v.clear();
         return r;
     }
-    __device__ __forceinline__ void open(const Raw &r, State &, const int *, uint32_t (&li)[4],
-                                         VT (&v)[4]) const {
+    __device__ __forceinline__ void open(const Raw &r, State &, uint32_t (&li)[4], VT (&v)[4]) const {
         li[0] = r.w.x & 0xFFFFu; li[1] = r.w.x >> 16; li[2] = r.w.y & 0xFFFFu; li[3] = r.w.y >> 16;
         r.v.to(v);
     }
@@ -501,34 +517,73 @@ struct TlArgs {
     const int4 *units;
     int32_t nunits;
     TlGeo G;
-    int S6, L6;  // step code of the 6-entry records
 };
 
+// One element from global to shared memory as an asynchronous copy (4 or 8
+// bytes, `cp.async.ca`): a thread issues all its copies of a tile before any
+// of them has to arrive, and waits once (cp_async_wait_all).
+template <typename XT>
+__device__ __forceinline__ void cp_async_elem(XT *dst, const XT *src) {
+    static_assert(sizeof(XT) == 4 || sizeof(XT) == 8, "4- or 8-byte elements");
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(XT) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // The shared copy of unit U's tile of the gathered vector x (all threads of
-// the CTA), zero cell included.
+// the CTA), zero cell included. Cells inside the image / sinogram arrive by
+// asynchronous copies, the rest are stored as zeros; the caller's barrier
+// follows each thread's cp_async_wait_all.
 template <typename XT>
 __device__ __forceinline__ void tl_fill_tile(const TlGeo &G, int4 U, const XT *__restrict__ x, XT *xs) {
-    if (G.kind == 0) {  // the T x T pixels of the tile, column stride T + 1
+    if (G.kind == 0) {  // the T x T pixels of the tile, column stride T + 1: a warp per
+                        // column, its lanes along the column's T pixels (contiguous in x)
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
         const int T = G.T, N = G.N;
         const int tc = U.x / G.ntr, tr = U.x - tc * G.ntr;
-        for (int e = threadIdx.x; e < T * T; e += blockDim.x) {
-            const int lc = e / T, lr = e - lc * T;
-            const int gr = tr * T + lr, gc = tc * T + lc;
-            xs[lc * (T + 1) + lr] = (gr < N && gc < N) ? x[(int64_t)gc * N + gr] : (XT)0;
+        for (int lc = wid; lc < T; lc += nw) {
+            const int gc = tc * T + lc;
+            XT *dst = xs + lc * (T + 1);
+            for (int lr = lane; lr < T; lr += 32) {
+                const int gr = tr * T + lr;
+                if (gc < N && gr < N) cp_async_elem(dst + lr, x + (int64_t)gc * N + gr);
+                else dst[lr] = (XT)0;
+            }
         }
-    } else {  // W bins per angle of the tile's angle block
+    } else {  // W bins per angle of the tile's angle block, one cell per thread in
+              // turn (W is about 1.5 warps wide: a warp per angle would idle lanes)
         const int pt = U.x / G.nab, a0 = (U.x - pt * G.nab) * G.NA;
         for (int e = threadIdx.x; e < G.NA * G.W; e += blockDim.x) {
             const int ai = e / G.W, a = a0 + ai;
-            XT v = (XT)0;
+            bool in = false;
+            int b = 0;
             if (a < G.nth) {
-                const int b = __ldg(G.bmin + (int64_t)pt * G.nth + a) + (e - ai * G.W);
-                if (b < G.p) v = x[(int64_t)a * G.p + b];
+                b = __ldg(G.bmin + (int64_t)pt * G.nth + a) + (e - ai * G.W);
+                in = b < G.p;
             }
-            xs[e] = v;
+            if (in) cp_async_elem(xs + e, x + (int64_t)a * G.p + b);
+            else xs[e] = (XT)0;
         }
     }
     if (threadIdx.x == 0) xs[G.cells()] = (XT)0;  // the zero cell of padding entries
+    cp_async_wait_all();
+}
+
+// A segment's partial from its independent sums (one per ring slot), added
+// in a fixed order: (k0 + k1) + (k2 + k3).
+template <typename ACC, int K>
+__device__ __forceinline__ ACC chain_sum(const ACC (&a)[K]) {
+    ACC k[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) k[i] = a[i];
+#pragma unroll
+    for (int w = 1; w < K; w *= 2)
+#pragma unroll
+        for (int i = 0; i + w < K; i += 2 * w) k[i] += k[i + w];
+    return k[0];
 }
 
 // Partial sums of all segments. Persistent CTAs take work units through
@@ -540,12 +595,15 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
     extern __shared__ __align__(16) unsigned char tl_smem[];
     XT *xs = reinterpret_cast<XT *>(tl_smem);
     __shared__ int s_unit, s_chunk;
-    __shared__ int lut[32];  // 5-bit step codes of the 6-entry records
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int E = LD::E;
+    // independent sums: one per ring slot in the FP32 forms, one in FP64 (whose
+    // pass is bound by the FP64 pipe and keeps its registers for a second CTA
+    // per SM)
+    constexpr int KC = sizeof(ACC) == 8 ? 1 : 2;
+    constexpr int KD = sizeof(ACC) == 8 ? 1 : D;
     const int lane = threadIdx.x & 31;
     const TlGeo &G = P.G;
-    if (threadIdx.x < 32) lut[threadIdx.x] = step_decode<5>((uint32_t)threadIdx.x, P.S6, P.L6);
     for (;;) {
         if (threadIdx.x == 0) s_unit = (int)atomicAdd(ctr, 1u);
         __syncthreads();
@@ -556,10 +614,12 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
         if (threadIdx.x == 0) s_chunk = U.y;
         __syncthreads();
         if constexpr (CONT) {
-            // the warp's chunks of the unit, c = first + w, first + w + W, ...,
-            // as one stream of slots: the loads of the next chunk's first slots
-            // start during the current chunk (D = 2: a next chunk always has a
-            // slot, so the window never reaches past it)
+            // the warp's chunks of the unit, one per group of W consecutive
+            // chunks, in snake order (w in even groups, W - 1 - w in odd ones:
+            // the chunks of a tile are sorted longest first, so the warps' sums
+            // of lengths balance), as one stream of slots: the loads of the
+            // next chunk's first slots start during the current chunk (D = 2: a
+            // next chunk always has a slot, so the window never reaches past it)
             static_assert(D == 2, "the continuous stream keeps 2 slots in flight");
             const int W = blockDim.x >> 5;
             struct Meta {
@@ -578,8 +638,12 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
                 }
                 return r;
             };
-            int c = U.y + (int)(threadIdx.x >> 5);
-            Meta cur = meta(c), nxt = meta(c + W);
+            const int wid = (int)(threadIdx.x >> 5);
+            // chunk of group g (past the unit's end once one is: later groups
+            // start after every chunk of group g)
+            auto chunk_of = [&](int g) { return U.y + W * g + ((g & 1) ? W - 1 - wid : wid); };
+            int g = 0, c = chunk_of(0);
+            Meta cur = meta(c), nxt = meta(chunk_of(1));
             // slot q of the stream that starts at chunk c (q < cur.len + nxt.len)
             auto fetch = [&](int q) {
                 return q < cur.len ? ldr.load(cur.s0 + 32 * (int64_t)q)
@@ -588,30 +652,38 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
             };
             typename LD::Raw ring[2] = {fetch(0), fetch(1)};
             while (c < U.z) {
-                ACC acc = 0;
-                for (int t0 = 0; t0 < cur.len; t0 += 2) {
+                ACC acc[KC] = {};
+                int t = 0;
+                for (; t + 2 <= cur.len; t += 2) {  // slot pairs: both slots' work interleaves
 #pragma unroll
                     for (int k = 0; k < 2; ++k) {
-                        const int t = t0 + k;
-                        if (t >= cur.len) break;
                         const typename LD::Raw r = ring[k];
-                        ring[k] = fetch(t + 2);
+                        ring[k] = fetch(t + k + 2);
                         uint32_t li[E];
                         ACC v[E];
-                        ldr.open(r, cur.st, lut, li, v);
+                        ldr.open(r, cur.st, li, v);
 #pragma unroll
-                        for (int q = 0; q < E; ++q) acc += (ACC)xs[li[q]] * v[q];
+                        for (int q = 0; q < E; ++q) acc[k % KC] += (ACC)xs[li[q]] * v[q];
                     }
                 }
-                if (cur.ps >= 0) part[cur.ps] = acc;
-                if (cur.len & 1) {  // the next chunk's slot 0 sits in ring[1]
-                    const typename LD::Raw t = ring[0];
+                if (t < cur.len) {  // an odd last slot, in ring[0]
+                    const typename LD::Raw r = ring[0];
+                    ring[0] = fetch(t + 2);
+                    uint32_t li[E];
+                    ACC v[E];
+                    ldr.open(r, cur.st, li, v);
+#pragma unroll
+                    for (int q = 0; q < E; ++q) acc[0] += (ACC)xs[li[q]] * v[q];
+                    // the next chunk's slot 0 now sits in ring[1]
+                    const typename LD::Raw tmp = ring[0];
                     ring[0] = ring[1];
-                    ring[1] = t;
+                    ring[1] = tmp;
                 }
-                c += W;
+                if (cur.ps >= 0) part[cur.ps] = chain_sum<ACC, KC>(acc);
+                ++g;
+                c = chunk_of(g);
                 cur = nxt;
-                nxt = meta(c + W);
+                nxt = meta(chunk_of(g + 1));
             }
         } else {
             for (;;) {
@@ -626,7 +698,7 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
 #pragma unroll
                 for (int k = 0; k < D; ++k) ring[k] = k < len ? ldr.load(s0 + 32 * k) : LD::none();
                 typename LD::State lst = ldr.init((int64_t)c * 32 + lane);
-                ACC acc = 0;
+                ACC acc[KD] = {};
                 for (int t0 = 0; t0 < len; t0 += D) {
 #pragma unroll
                     for (int k = 0; k < D; ++k) {
@@ -636,13 +708,13 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
                         ring[k] = t + D < len ? ldr.load(s0 + 32 * (int64_t)(t + D)) : LD::none();
                         uint32_t li[E];
                         ACC v[E];
-                        ldr.open(r, lst, lut, li, v);
+                        ldr.open(r, lst, li, v);
 #pragma unroll
-                        for (int q = 0; q < E; ++q) acc += (ACC)xs[li[q]] * v[q];
+                        for (int q = 0; q < E; ++q) acc[k % KD] += (ACC)xs[li[q]] * v[q];
                     }
                 }
                 const int ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
-                if (ps >= 0) part[ps] = acc;
+                if (ps >= 0) part[ps] = chain_sum<ACC, KD>(acc);
             }
         }
         __syncthreads();  // the tile is rewritten by the next unit
@@ -711,7 +783,7 @@ void launch_tl(const DevCSR &M, int code, const LD &ldr, const XT *x, const Epi 
     const DevBuf &soff = LD::E == 6 ? tl.soff6 : tl.soff;
     const TlGeo G = tl_geo(tl);
     const TlArgs P{soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.units.as<int4>(), tl.nunits,
-                   G, tl.S6, tl.L6};
+                   G};
     const size_t smem = sizeof(XT) * ((size_t)G.cells() + 1);
     ACC *part = tl.part.as<ACC>();
     auto run = [&](auto kernel) -> cudaError_t {
@@ -1054,9 +1126,9 @@ bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cuda
     if (code == 14 && tl.built6 && (h ? tl.has6_16 : tl.has6_q)) {
         const int32_t *anc = tl.anc6.as<int32_t>();
         const int4 *side = tl.side6.as<int4>();
-        if (h) return run(TlStep6<__half>{tl.r6_16.as<uint4>(), anc, side});
-        if (M.qsigned) return run(TlStep6<int16_t>{tl.r6_q.as<uint4>(), anc, side});
-        return run(TlStep6<uint16_t>{tl.r6_q.as<uint4>(), anc, side});
+        if (h) return run(TlStep6<__half>(tl.r6_16.as<uint4>(), anc, side, tl.S6, tl.L6));
+        if (M.qsigned) return run(TlStep6<int16_t>(tl.r6_q.as<uint4>(), anc, side, tl.S6, tl.L6));
+        return run(TlStep6<uint16_t>(tl.r6_q.as<uint4>(), anc, side, tl.S6, tl.L6));
     }
     if (h) {
         if (!tl.has_r16) return false;
