@@ -6,21 +6,25 @@
 // dot product (csr_matrowvec, sparse_matrices.f90:252-270) and bounded update
 // (add_mult_row, :795-822). Row k+1 starts only after row k's update is
 // visible, so the iterate follows the reference's sequence of projections.
-// Three roundings differ from the reference: the order of the sums inside a
-// dot product, the update as one fused multiply-add, and the coefficient
-// formed as (b_i - a_i.x) * (omega / nrA_i) instead of
-// omega * (b_i - a_i.x) / nrA_i (AIRMs.f90:842).
+// Three roundings differ from the reference: a_i.x - b_i is exact before its
+// one rounding (the reference rounds each term of its ordered sum), the
+// update is one fused multiply-add, and the coefficient is formed as
+// (b_i - a_i.x) * (omega / nrA_i) instead of omega * (b_i - a_i.x) / nrA_i
+// (AIRMs.f90:842).
 //
 // On GB300 every FP64 warp instruction holds its SM sub-partition's FP64 pipe
 // for 64 cycles (measured: a dependent and an independent chain of DFMA both
 // issue one per 64 cycles per warp), whatever its active lanes, and a
-// row-action sweep runs on one SM; a row is a dependent chain of about ten
-// FP64 operations (dot product, reduction tree, coefficient, update). The kernel therefore spends FP64 instructions only
-// where the arithmetic needs them:
+// row-action sweep runs on one SM; a row is a dependent chain (dot product,
+// reduction, coefficient, update). The kernel therefore spends FP64
+// instructions only where the arithmetic needs them:
 //  * a row's entries are spread densely over the block (len / (32 W)
 //    instructions per lane, skipped by a block-uniform branch past the end);
-//  * partial sums go to shared memory and one warp finishes the sum
-//    (W - 1 + 5 additions) and the coefficient, instead of every warp;
+//  * the row sum a_i.x - b_i is formed exactly on the integer pipes (the
+//    lanes' partials as 64-bit fixed point in a common frame, added by warp
+//    reductions) and rounded once, so the reduction tree and the subtraction
+//    of b_i use no FP64 instruction; each warp adds the W warp sums itself,
+//    so one barrier per row suffices;
 //  * omega / nrA_i, b_i and each step's entry range come from a parallel
 //    schedule kernel, together with the row sampled by row probability
 //    (AIRMs.f90:830-835);
@@ -110,6 +114,98 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// ---- exact sums of doubles on the integer pipes ------------------------------
+// A finite double with exponent field e and significand m (53 bits with the
+// implicit one; e = 0: no implicit one, scale as e = 1) is m * 2^(e - 1075).
+// In the frame E (at least every term's e) it becomes the integer m >> (E - e),
+// which drops less than one unit 2^(E - 1075): an ulp of the largest term. A
+// warp adds its lanes' integers exactly as three 26-bit limbs with
+// __reduce_add_sync, the warps' sums are aligned to the largest frame, and the
+// total is rounded to double once (round to nearest even). A row of up to
+// 8 x 32 lanes x 2 partials + b stays below 2^63.
+__device__ __forceinline__ int fx_exp(double v) {
+    const int e = (int)((__double_as_longlong(v) >> 52) & 0x7FF);
+    return e > 1 ? e : 1;
+}
+__device__ __forceinline__ long long fx_of(double v, int E) {
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    long long m = b & 0xFFFFFFFFFFFFFLL;
+    if (e) m |= 1LL << 52;
+    const int sh = E - (e > 1 ? e : 1);
+    const long long f = sh < 64 ? (m >> sh) : 0LL;
+    return b < 0 ? -f : f;
+}
+__device__ __forceinline__ long long fx_warp_sum(long long F) {  // |F| < 2^55 per lane
+    const unsigned l0 = __reduce_add_sync(0xffffffffu, (unsigned)(F & 0x3FFFFFF));
+    const unsigned l1 = __reduce_add_sync(0xffffffffu, (unsigned)((F >> 26) & 0x3FFFFFF));
+    const int l2 = __reduce_add_sync(0xffffffffu, (int)(F >> 52));
+    return (long long)l2 * (1LL << 52) + (long long)l1 * (1LL << 26) + (long long)l0;
+}
+// total * 2^(E - 1075) rounded to nearest even; ldexp when the result leaves
+// the normal range
+__device__ __forceinline__ double fx_to_double(long long total, int E) {
+    if (total == 0) return 0.0;
+    const bool neg = total < 0;
+    unsigned long long a = neg ? 0ull - (unsigned long long)total : (unsigned long long)total;
+    int nb = 64 - __clzll((long long)a);
+    unsigned long long mant;
+    if (nb <= 53) {
+        mant = a << (53 - nb);
+    } else {
+        const int sh = nb - 53;
+        mant = a >> sh;
+        const unsigned long long rem = a & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+        if (mant == (1ull << 53)) {
+            mant >>= 1;
+            ++nb;
+        }
+    }
+    const int field = nb + E - 53;
+    if (field < 1 || field > 2046) return ldexp((double)total, E - 1075);
+    unsigned long long bits = ((unsigned long long)field << 52) | (mant & 0xFFFFFFFFFFFFFull);
+    if (neg) bits |= 1ull << 63;
+    return __longlong_as_double((long long)bits);
+}
+// A warp's share of a row sum: its integer sum in its frame, or (when a term
+// is Inf or NaN, frame 0x7FF) its FP64 sum.
+struct FxPart {
+    long long s;
+    double d;
+    int e;
+    int pad;
+};
+__device__ __forceinline__ FxPart fx_warp_part(double p0, double p1, double p2) {
+    int e = max(max(fx_exp(p0), fx_exp(p1)), fx_exp(p2));
+    FxPart r{0, 0.0, (int)__reduce_max_sync(0xffffffffu, (unsigned)e), 0};
+    if (r.e < 0x7FF) r.s = fx_warp_sum(fx_of(p0, r.e) + fx_of(p1, r.e) + fx_of(p2, r.e));
+    else r.d = warp_sum(p0 + p1 + p2);
+    return r;
+}
+// The row sum from the warps' shares (FP64 sum of the non-finite shares when
+// there are any: an Inf or NaN term decides the result).
+template <int W>
+__device__ __forceinline__ double fx_total(const FxPart *part) {
+    int E = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) E = max(E, part[w].e);
+    if (E >= 0x7FF) {
+        double d = 0.0;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            if (part[w].e >= 0x7FF) d += part[w].d;
+        return d;
+    }
+    long long t = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int sh = E - part[w].e;
+        if (sh < 64) t += part[w].s >> sh;
+    }
+    return fx_to_double(t, E);
+}
+
 template <int W, int CACHE, bool SMEM_X>
 __global__ void __launch_bounds__(32 * W) k_sweep(const RowStep *__restrict__ steps, int32_t nord,
                                                   const int32_t *__restrict__ col,
@@ -117,9 +213,8 @@ __global__ void __launch_bounds__(32 * W) k_sweep(const RowStep *__restrict__ st
                                                   int32_t n, Box box) {
     constexpr int T = 32 * W;
     extern __shared__ double xs[];
-    __shared__ double part_s[W > 1 ? T : 1];
-    __shared__ double coeff_s;
-    const int tid = threadIdx.x, lane = tid & 31;
+    __shared__ FxPart part_s[W];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     double *x = SMEM_X ? xs : xg;
     if (SMEM_X) {
         for (int32_t j = tid; j < n; j += T) xs[j] = xg[j];
@@ -169,23 +264,19 @@ __global__ void __launch_bounds__(32 * W) k_sweep(const RowStep *__restrict__ st
         }
         for (int k = tid + CACHE * T; k < cur.len; k += T)
             p0 = fma(x[__ldg(col + cur.s + k)], __ldg(val + cur.s + k), p0);
-        const double part = nq > 1 ? p0 + p1 : p0;
-        double coeff;
+        // a_i.x - b_i, summed exactly on the integer pipes (-b_i is a term of
+        // thread 0) and rounded once; every warp forms the same total, so the
+        // coefficient needs no second barrier
+        const FxPart mine = fx_warp_part(p0, p1, tid == 0 ? -cur.b : 0.0);
+        double resid;
         if (W > 1) {
-            part_s[tid] = part;
+            if (lane == 0) part_s[wid] = mine;
             __syncthreads();
-            if (tid < 32) {
-                double t = part_s[lane];
-#pragma unroll
-                for (int w = 1; w < W; ++w) t += part_s[lane + 32 * w];
-                t = warp_sum(t);
-                if (lane == 0) coeff_s = __dmul_rn(__dsub_rn(cur.b, t), cur.w);
-            }
-            __syncthreads();
-            coeff = coeff_s;
+            resid = fx_total<W>(part_s);
         } else {
-            coeff = __dmul_rn(__dsub_rn(cur.b, warp_sum(part)), cur.w);
+            resid = fx_total<1>(&mine);
         }
+        const double coeff = __dmul_rn(-resid, cur.w);
 #pragma unroll
         for (int q = 0; q < CACHE; ++q) {
             if (q >= nq) break;
@@ -233,18 +324,18 @@ long long host_key(double v) {
     return okey(bits);
 }
 
-// Warps per row: FAIR_SWEEP_WARPS (1, 2, 4 or 8) when set, else 2 when x is
-// in shared memory and 8 when it is in global memory (more gathers in
-// flight). Measured on GB300, fan beam N=128 (x in shared memory): 0.76M,
-// 0.90M, 0.88M, 0.80M rows/s for 1, 2, 4, 8 warps; N=512 (x in global
-// memory): 0.18M, 0.32M, 0.41M, 0.42M rows/s.
-int sweep_warps(bool smem) {
+// Warps per row: FAIR_SWEEP_WARPS (1, 2, 4 or 8) when set, else 4. Measured
+// on GB300 (host call, rows/s for 1, 2, 4, 8 warps): fan beam N=128, x in
+// shared memory, Kaczmarz 0.83M, 0.97M, 1.00M, 0.94M; fan beam N=512, x in
+// global memory, symmetric Kaczmarz 0.18M, 0.33M, 0.44M, 0.39M and random
+// Kaczmarz 0.17M, 0.30M, 0.43M, 0.42M.
+int sweep_warps(bool) {
     const char *env = getenv("FAIR_SWEEP_WARPS");
     if (env) {
         int w = atoi(env);
         if (w == 1 || w == 2 || w == 4 || w == 8) return w;
     }
-    return smem ? 2 : 8;
+    return 4;
 }
 
 }  // namespace

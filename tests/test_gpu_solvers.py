@@ -159,6 +159,51 @@ def test_art_order_damp_xref(par, fair, oracle):
     assert rel_err(X, Xr) < TOL64
 
 
+@pytest.mark.parametrize("warps", ["1", "2", "4", "8"])
+def test_art_sweep_warps(par, fair, oracle, monkeypatch, warps):
+    """Every warps-per-row choice of the sweep: the row sums of 1 to 8 warps
+    (exact integer sums of the lanes' FP64 partials) against the oracle."""
+    monkeypatch.setenv("FAIR_SWEEP_WARPS", warps)
+    A, R, _, b = par
+    o = fair.airms.options(relaxpar=0.25, lbound=0.0, ubound=1.0)
+    ro = oracle.options(relaxpar=0.25, lbound=0.0, ubound=1.0)
+    X = fair.airms.art("kaczmarz", A, b, [2], opts=o)
+    Xr = oracle.art("kaczmarz", R, b, [2], opts=ro)
+    assert rel_err(X, Xr) < TOL64
+
+
+@pytest.mark.parametrize("warps", ["2", "8"])
+def test_art_iterate_in_global_memory(fair, oracle, monkeypatch, warps):
+    """N=192 (36,864 unknowns: more than one block's shared memory holds), so the
+    sweep gathers the iterate from global memory."""
+    monkeypatch.setenv("FAIR_SWEEP_WARPS", warps)
+    n, nth, p = 192, 24, 272
+    th = oracle.linspace(0.0, np.pi, nth)
+    A = fair.paralleltomo(fair.Data(n=n, p=p, nth=nth, theta=th))
+    R = oracle.paralleltomo(n, nth, p, th)
+    b = oracle.matvecmul(R, oracle.shepplogan(n))
+    o = fair.airms.options(relaxpar=0.5, lbound=0.0)
+    ro = oracle.options(relaxpar=0.5, lbound=0.0)
+    X = fair.airms.art("symkaczmarz", A, b, [2], opts=o)
+    Xr = oracle.art("symkaczmarz", R, b, [2], opts=ro)
+    assert rel_err(X, Xr) < TOL64
+
+
+def test_art_nonfinite_b(par, fair, oracle):
+    """NaN and +-Inf entries of b: the row sum is then the FP64 sum of the
+    non-finite terms, and the box (MAX/MIN semantics: NaN loses) brings the
+    iterate back to finite values as in the oracle."""
+    A, R, _, b = par
+    bb = b.copy()
+    bb[5], bb[77], bb[300] = np.nan, np.inf, -np.inf
+    o = fair.airms.options(relaxpar=0.25, lbound=0.0, ubound=1.0)
+    ro = oracle.options(relaxpar=0.25, lbound=0.0, ubound=1.0)
+    X = fair.airms.art("kaczmarz", A, bb, [1, 2], opts=o)
+    Xr = oracle.art("kaczmarz", R, bb, [1, 2], opts=ro)
+    assert np.all(np.isfinite(X)) and np.all(np.isfinite(Xr))
+    assert rel_err(X, Xr) < TOL64
+
+
 def test_art_errors(par, fair):
     A, R, _, b = par
     with pytest.raises(fair.FairError) as ei:
