@@ -527,17 +527,27 @@ def run_batch(args):
     N uniform on {64, 96, ..., 512}, angles uniform on 90..720 over [0, 2pi),
     p = ceil(1.42 N) unit bins, source at R = 2N, detector at 2N; Voronoi
     grain phantoms with 50-400 cells and values uniform in [0,1]; 0.5% seeded
-    noise; SART, 50 iterations, box [0,1], FP32 values on the packed index
-    stream with FP64 weights. The whole batch advances with one launch per
-    pass and iteration, the 50 iterations replayed from one CUDA graph; the
-    same iterations launched problem by problem are timed beside it, and the
-    oracle's serial SART on a sample of the problems, scaled by nonzeros,
-    gives the CPU baseline."""
+    noise; SART, 50 iterations, box [0,1], FP32 values with FP64 weights, on
+    each layout of --batch-layout (one line each): 'tiled', the tiled copies
+    of A and A' (two launches per pass for the whole batch: partial sums, row
+    sums), and 'packed', the packed index streams (one launch per pass). The
+    50 iterations are replayed from one CUDA graph; the same iterations
+    launched problem by problem are timed beside it, and the oracle's serial
+    SART on a sample of the problems, scaled by nonzeros, gives the CPU
+    baseline."""
+    for layout in [t for t in args.batch_layout.split(",") if t]:
+        run_batch_layout(args, layout)
+    return 0
+
+
+def run_batch_layout(args, layout):
+    import ctypes as C
     import math
 
     import torch
 
     import fortran_airtools_gb300 as F
+    from fortran_airtools_gb300._clib import check, lib
     from oracle import oracle as O
     K = 50
     nprob = args.batch_problems
@@ -547,7 +557,7 @@ def run_batch(args):
     cells = rng.integers(50, 401, nprob)
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
-    B = F.Batch(args.batch_prec)
+    B = F.Batch(args.batch_prec, layout=layout)
     bs, samples = [], []
     t0 = time.perf_counter()
     for i in range(nprob):
@@ -603,6 +613,9 @@ def run_batch(args):
     xe = B.sirt("sart", ball, K, opts=opts)
     e2e_s = time.perf_counter() - t0
     p1, p2 = B.pass_bytes(True)
+    nl = C.c_int64()
+    check(lib().fair_batch_launches(B.handle, K, C.byref(nl)))
+    per_pass = (nl.value - (0 if args.batch_prec == "f64" else 1)) // (2 * K)
     peak, peak_kind = hbm_peak()
     gbs = (p1 + p2) * K / (ms_b / 1e3) / 1e9
     cpu = None
@@ -623,11 +636,13 @@ def run_batch(args):
                "iteration (3 minus 1), scaled by nonzeros to the whole batch"}
     line = {"metric": "batched SART iter/s (all problems per iteration)",
             "workload": f"{nprob} fan-beam problems, N 64..512, 90..720 angles, p = ceil(1.42N)",
+            "layout": layout,
             "value": K / (ms_b / 1e3), "unit": "batch iter/s", "ms_per_iteration": ms_b / K,
             "iterations": K, "dtype": args.batch_prec, "problems": nprob, "nnz": info["nnz"],
             "device_bytes": info["device_bytes"], "build_s": build_s,
             "unbatched": {"value": K / (ms_u / 1e3), "unit": "batch iter/s",
-                          "ms_per_iteration": ms_u / K, "launches_per_iteration": 2 * nprob,
+                          "ms_per_iteration": ms_u / K,
+                          "launches_per_iteration": 2 * nprob * (2 if per_pass == 2 else 1),
                           "max_abs_diff_vs_batched": float(np.max(np.abs(xu - xb)))},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "peak_kind": peak_kind,
                          "unit": "GB/s", "frac": gbs / peak,
@@ -635,10 +650,10 @@ def run_batch(args):
             "e2e": {"value": K / e2e_s, "unit": "batch iter/s",
                     "h2d_bytes_per_step": 8 * ball.size / K, "d2h_bytes_per_step": 8 * xe.size / K,
                     "note": "one fair_batch_sirt call of 50 iterations: b uploaded, x downloaded"},
-            "gpu_launches": 1 + 2 * K, "pass_config": cfg, "clocks": clocks, "cpu_baseline": cpu}
+            "gpu_launches": nl.value, "launches_per_pass": per_pass, "pass_config": cfg,
+            "clocks": clocks, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
     B.close()
-    return 0
 
 
 def run_mfree(args):
@@ -761,6 +776,8 @@ def main():
                     help="sirt: the headline line; kaczmarz, adjoint, batch, mfree: secondary lines")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--batch-prec", choices=["f64", "f32", "f16", "q16"], default="f32")
+    ap.add_argument("--batch-layout", default="tiled,packed",
+                    help="batch layouts timed, one line each (comma list of tiled, packed)")
     ap.add_argument("--mf-sizes", default="",
                     help="matrix-free cases to run, by N (comma list of 2048, 1024; default both)")
     args = ap.parse_args()

@@ -159,6 +159,7 @@ def _declare(L):
         "fair_batch_create": ([P(h), i32], C.c_int),
         "fair_batch_destroy": ([h], C.c_int),
         "fair_batch_set_stream": ([h, vp], C.c_int),
+        "fair_batch_set_layout": ([h, i32], C.c_int),
         "fair_batch_add": ([h, h, i32], C.c_int),
         "fair_batch_info": ([h, P(i32), P(i64), P(i64), P(i64), P(i64)], C.c_int),
         "fair_batch_offsets": ([h, vp, vp], C.c_int),

@@ -16,10 +16,17 @@ from .airms import options
 
 
 class Batch:
-    def __init__(self, prec: str = "f32"):
+    def __init__(self, prec: str = "f32", layout: str = "packed"):
+        """layout 'packed' (the packed index streams; CSR in f64) or 'tiled'
+        (the tiled copies of A and A' for every problem on an N x N image)."""
+        if layout not in ("packed", "tiled"):
+            raise ValueError("layout must be 'packed' or 'tiled'")
         self._h = C.c_void_p()
         check(lib().fair_batch_create(C.byref(self._h), PREC[prec]))
         self.prec = prec
+        self.layout = layout
+        if layout == "tiled":
+            check(lib().fair_batch_set_layout(self._h, 1))
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -179,6 +179,7 @@ void launch_f64(int G, bool dry, const BPass *P, const int64_t *c0, int np, cons
 struct BatchProb {
     DevCSR A, AT;
     DevBuf M_sart, M_cim, D;  // FP64 weights: row 1-norms, m*|a_i|^2, column 1-norms
+    bool tiled = false;       // passes on the tiled copies of A and A' (else packed / CSR)
     void release() {
         A.release(); AT.release();
         M_sart.release(); M_cim.release(); D.release();
@@ -201,6 +202,9 @@ struct fair_batch_s {
     std::vector<int64_t> row_off{0}, col_off{0};
     int64_t nnz = 0;
     int cfg[4] = {8, 8, 1, 1};  // lanes A, lanes A', groups A, groups A'
+    int layout = 0;             // 0: packed streams (CSR in FP64); 1: tiled copies where they build
+    int ntiled = 0;             // problems on their tiled copies
+    fair::TlBatch tb1, tb2;     // device tables of the tiled problems' passes
     // prepared state
     bool ready = false, sart = false;
     fair::BOpts opts{1.0, 0.0, 0.0, 0};
@@ -225,6 +229,10 @@ int64_t device_bytes(const fair_batch_s *B) {
         for (const DevCSR *M : {&p->A, &p->AT}) {
             add(M->rowptr); add(M->col); add(M->v64); add(M->v32); add(M->v16); add(M->vq);
             add(M->prow); add(M->gidx); add(M->gside); add(M->pv32); add(M->pv16); add(M->pvq);
+            const DevCSR::Tiled &tl = M->tl;
+            for (const DevBuf *d : {&tl.bmin, &tl.segbase, &tl.soff, &tl.pslot, &tl.units, &tl.idx, &tl.v64,
+                                    &tl.v32, &tl.r16, &tl.rq, &tl.part})
+                add(*d);
         }
         add(p->M_sart); add(p->M_cim); add(p->D);
     }
@@ -246,12 +254,22 @@ int bind_vectors(fair_batch_s *B, const double *d_b, double *d_x) {
     const bool red = B->prec != FAIR_PREC_F64;
     std::vector<BPass> t1(np), t2(np);
     std::vector<int64_t> c1(np + 1, 0), c2(np + 1, 0);
+    std::vector<TlBatchProb> l1, l2;
     const size_t sx = red ? sizeof(float) : sizeof(double);
     for (int p = 0; p < np; ++p) {
         BatchProb &q = *B->probs[p];
         const int64_t ro = B->row_off[p], co = B->col_off[p];
         char *r = (char *)B->r.p + sx * ro;
         const void *xin = red ? (const void *)(B->x32.as<float>() + co) : (const void *)(d_x + co);
+        if (q.tiled) {  // no chunks in the packed / CSR launch
+            c1[p + 1] = c1[p];
+            c2[p + 1] = c2[p];
+            l1.push_back(TlBatchProb{&q.A, xin, d_b + ro, B->sart ? q.M_sart.as<double>() : q.M_cim.as<double>(),
+                                     r, nullptr, nullptr, nullptr});
+            l2.push_back(TlBatchProb{&q.AT, r, nullptr, nullptr, nullptr, B->sart ? q.D.as<double>() : nullptr,
+                                     d_x + co, red ? B->x32.as<float>() + co : nullptr});
+            continue;
+        }
         for (int pass = 1; pass <= 2; ++pass) {
             const DevCSR &M = pass == 1 ? q.A : q.AT;
             BPass d{};
@@ -300,6 +318,8 @@ int bind_vectors(fair_batch_s *B, const double *d_b, double *d_x) {
     FAIR_CUDA(cudaMemcpy(B->desc2.p, t2.data(), sizeof(BPass) * np, cudaMemcpyHostToDevice));
     FAIR_CUDA(cudaMemcpy(B->c0_1.p, c1.data(), sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice));
     FAIR_CUDA(cudaMemcpy(B->c0_2.p, c2.data(), sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice));
+    FAIR_TRY(tl_batch_bind(B->tb1, B->prec, l1));
+    FAIR_TRY(tl_batch_bind(B->tb2, B->prec, l2));
     B->bound_b = d_b;
     B->bound_x = d_x;
     return FAIR_OK;
@@ -307,6 +327,11 @@ int bind_vectors(fair_batch_s *B, const double *d_b, double *d_x) {
 
 void batch_pass(fair_batch_s *B, int pass, cudaStream_t s, bool dry = false) {
     const int np = (int)B->probs.size();
+    const BOpts &ot = B->opts;
+    if (B->ntiled > 0)
+        tl_batch_launch(pass == 1 ? B->tb1 : B->tb2, B->prec, pass, ot.omg, ot.lb, ot.ub, ot.bmode,
+                        B->sched.as<unsigned>(), s, dry);
+    if (B->ntiled == np) return;  // no problem on the packed streams / CSR
     const BPass *P = (pass == 1 ? B->desc1 : B->desc2).as<BPass>();
     const int64_t *c0 = (pass == 1 ? B->c0_1 : B->c0_2).as<int64_t>();
     unsigned *sched = B->sched.as<unsigned>();
@@ -344,13 +369,22 @@ int enqueue_iterations(fair_batch_s *B, int K, cudaStream_t s) {
 }
 
 // Keep of a problem's matrices only what the batch's passes read.
-void compact(DevCSR &M, int prec) {
+void compact(DevCSR &M, int prec, bool tiled) {
     M.drop_sliced();
-    M.tl.release();
     M.dl[0].release();
     M.dl[1].release();
     M.v32.release(); M.v16.release(); M.vq.release();
     M.has32 = M.has16 = M.hasq = false;
+    if (tiled) {  // the tiled copy is all the passes read
+        tl_drop_build(M);
+        M.rowptr.release(); M.col.release(); M.v64.release();
+        M.prow.release(); M.gidx.release(); M.gside.release();
+        M.pv64.release(); M.pv32.release(); M.pv16.release(); M.pvq.release();
+        M.pf16.release(); M.pfq.release();
+        M.haspk = M.hasp64 = M.hasp32 = M.hasp16 = M.haspq = M.hasf16 = M.hasfq = false;
+        return;
+    }
+    M.tl.release();
     if (prec == FAIR_PREC_F64) {
         M.prow.release(); M.gidx.release(); M.gside.release();
         M.pv64.release(); M.pv32.release(); M.pv16.release(); M.pvq.release();
@@ -396,7 +430,17 @@ int finish_problem(fair_batch_s *B, BatchProb &q) {
     FAIR_TRY(q.D.grow(sizeof(double) * ((size_t)q.A.n + 1)));
     FAIR_TRY(sirt_weights(q.A, q.AT, true, q.M_sart.as<double>(), q.D.as<double>(), s));
     FAIR_TRY(sirt_weights(q.A, q.AT, false, q.M_cim.as<double>(), nullptr, s));
-    if (B->prec != FAIR_PREC_F64) {
+    if (B->layout == 1) {  // tiled copies of A (pass 1) and A' (pass 2) where both build
+        FAIR_TRY(csr_make_tiled(q.A, B->prec, 1, s));
+        FAIR_TRY(csr_make_tiled(q.AT, B->prec, 2, s));
+        FAIR_CUDA(cudaStreamSynchronize(s));
+        q.tiled = tl_batch_ready(q.A, B->prec) && tl_batch_ready(q.AT, B->prec);
+        if (!q.tiled) {
+            q.A.tl.release();
+            q.AT.tl.release();
+        }
+    }
+    if (B->prec != FAIR_PREC_F64 && !q.tiled) {
         FAIR_TRY(sirt_make_forms(q.A, q.AT, B->prec, s, false, false));
         FAIR_CUDA(cudaStreamSynchronize(s));
         if (q.A.nnz > 0 && (!q.A.haspk || !q.AT.haspk)) {
@@ -409,8 +453,8 @@ int finish_problem(fair_batch_s *B, BatchProb &q) {
         }
     }
     FAIR_CUDA(cudaStreamSynchronize(s));
-    compact(q.A, B->prec);
-    compact(q.AT, B->prec);
+    compact(q.A, B->prec, q.tiled);
+    compact(q.AT, B->prec, q.tiled);
     return FAIR_OK;
 }
 
@@ -475,6 +519,8 @@ int fair_batch_destroy(fair_batch B) {
     for (DevBuf *d : {&B->desc1, &B->desc2, &B->c0_1, &B->c0_2, &B->sched, &B->x32, &B->r,
                       &B->w_b, &B->w_x})
         d->release();
+    B->tb1.release();
+    B->tb2.release();
     if (B->own_stream) cudaStreamDestroy(B->stream);
     delete B;
     return FAIR_OK;
@@ -493,6 +539,21 @@ int fair_batch_set_stream(fair_batch B, void *cuda_stream) {
         B->own_stream = true;
     }
     fair::drop_graph(B);
+    return FAIR_OK;
+}
+
+int fair_batch_set_layout(fair_batch B, int32_t layout) {
+    BENTER(B);
+    if (layout != 0 && layout != 1) {
+        fair::set_detail("layout must be 0 (packed streams) or 1 (tiled copies)");
+        return FAIR_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(B->mu);
+    if (!B->probs.empty()) {
+        fair::set_detail("the layout is chosen before the first problem is added");
+        return FAIR_ERR_STATE;
+    }
+    B->layout = layout;
     return FAIR_OK;
 }
 
@@ -529,6 +590,7 @@ int fair_batch_add(fair_batch B, fair_csr h, int32_t take) {
         return st;
     }
     B->probs.push_back(q);
+    B->ntiled += q->tiled ? 1 : 0;
     B->row_off.push_back(B->row_off.back() + q->A.m);
     B->col_off.push_back(B->col_off.back() + q->A.n);
     B->nnz += q->A.nnz;
@@ -553,15 +615,18 @@ int fair_batch_pass_bytes(fair_batch B, int32_t sart, int64_t *pass1, int64_t *p
     const bool red = B->prec != FAIR_PREC_F64;
     const int64_t sv = B->prec == FAIR_PREC_F64 ? 8 : B->prec == FAIR_PREC_F32 ? 4 : 2;
     const int64_t sx = red ? 4 : 8;
-    auto matrix = [&](const DevCSR &M) -> int64_t {
+    auto matrix = [&](const DevCSR &M, bool tiled) -> int64_t {
+        // tiled copies: per 4 entries 8 bytes of local indices and 4 values, or
+        // one 16-byte record (2-byte forms); row ends as a row pointer
+        if (tiled) return M.nnz * (sv == 2 ? 4 : 2 + sv) + ((int64_t)M.m + 1) * 8;
         if (!red) return M.nnz * 12 + ((int64_t)M.m + 1) * 8;
         return M.ngroups * (8 + 4 * sv) + M.nesc * 16 + ((int64_t)M.m + 1) * 8;
     };
     int64_t p1 = 0, p2 = 0;
     for (const BatchProb *q : B->probs) {
         const int64_t m = q->A.m, n = q->A.n;
-        p1 += matrix(q->A) + n * sx + m * 8 + m * 8 + m * sx;  // x, b, M, r
-        p2 += matrix(q->AT) + m * sx + 2 * n * 8 + (sart ? n * 8 : 0) + (red ? n * 4 : 0);
+        p1 += matrix(q->A, q->tiled) + n * sx + m * 8 + m * 8 + m * sx;  // x, b, M, r
+        p2 += matrix(q->AT, q->tiled) + m * sx + 2 * n * 8 + (sart ? n * 8 : 0) + (red ? n * 4 : 0);
     }
     *pass1 = p1;
     *pass2 = p2;
@@ -653,7 +718,7 @@ int fair_batch_run_device_unbatched(fair_batch B, const double *d_b, double *d_x
         BatchProb &q = *B->probs[p];
         for (DevCSR *M : {&q.A, &q.AT}) {
             M->sirt_lanes[B->prec] = B->cfg[M == &q.A ? 0 : 1];
-            M->sirt_groups[B->prec] = B->cfg[M == &q.A ? 2 : 3];
+            M->sirt_groups[B->prec] = q.tiled ? 9 : B->cfg[M == &q.A ? 2 : 3];
         }
         fair::SirtDev &d = S[p];
         d.prec = B->prec;
@@ -684,7 +749,9 @@ int fair_batch_run_device_unbatched(fair_batch B, const double *d_b, double *d_x
 
 int fair_batch_launches(fair_batch B, int32_t K, int64_t *launches) {
     if (!B || !launches) return FAIR_ERR_NULL;
-    *launches = (B->prec != FAIR_PREC_F64 ? 1 : 0) + 2 * (int64_t)K;
+    // per pass: one packed / CSR launch, and partials + row sums for the tiled problems
+    const int64_t per_pass = (B->ntiled < (int)B->probs.size() ? 1 : 0) + (B->ntiled > 0 ? 2 : 0);
+    *launches = (B->prec != FAIR_PREC_F64 ? 1 : 0) + 2 * per_pass * (int64_t)K;
     return FAIR_OK;
 }
 
@@ -728,6 +795,11 @@ int fair_batch_autotune(fair_batch B, const double *d_b, double *d_x, int32_t re
     if (reps < 1) { fair::set_detail("reps >= 1 required"); return FAIR_ERR_ARG; }
     std::lock_guard<std::mutex> lk(B->mu);
     FAIR_TRY(batch_bind(B, d_b, d_x));
+    if (B->ntiled == (int)B->probs.size()) {  // every problem on its tiled copies: nothing to tune
+        if (config)
+            for (int i = 0; i < 4; ++i) config[i] = B->cfg[i];
+        return FAIR_OK;
+    }
     cudaStream_t s = B->stream;
     if (B->prec != FAIR_PREC_F64 && B->col_off.back() > 0)
         FAIR_TRY(fair::vec_to_f32(d_x, B->col_off.back(), B->x32.as<float>(), s));

@@ -11,6 +11,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "fair_gpu.h"
 
@@ -240,6 +241,38 @@ int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s);
 // A SIRT pass on the tiled copy (layout codes 9, 10, 14; two kernels); false
 // when the matrix has no tiled copy of the form.
 bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s);
+
+// Tiled passes of many problems at once (batches, tiled.cu): one launch of
+// partial sums over the work units of every problem, one of row sums and
+// epilogues. TlBatchProb describes one problem's pass; TlBatch holds the
+// device tables built from them.
+struct TlBatchProb {
+    const DevCSR *M;          // A (pass 1) or A' (pass 2), its tiled copy built
+    const void *xin;          // the gathered vector: x32 or x (pass 1), r (pass 2)
+    const double *b, *Minv;   // pass 1: r = (b - A x) / M
+    void *r;
+    const double *D;          // pass 2: x = P(x + omega A'r / D); null: D = 1
+    double *x;
+    float *x32;
+};
+struct TlBatch {
+    DevBuf desc, uoff, roff;  // per-problem descriptors, unit and row offsets
+    int np = 0;
+    int64_t units = 0, rows = 0;
+    size_t smem = 0;          // shared memory of the largest tile
+    void release() {
+        desc.release(); uoff.release(); roff.release();
+        np = 0; units = rows = 0; smem = 0;
+    }
+};
+// True when M's tiled copy holds what a batched pass in `prec` reads.
+bool tl_batch_ready(const DevCSR &M, int prec);
+// Frees the parts of M's tiled copy that only its builders read.
+void tl_drop_build(DevCSR &M);
+int tl_batch_bind(TlBatch &T, int prec, const std::vector<TlBatchProb> &probs);
+// dry: only the kernel attributes and grids (outside a graph capture).
+int tl_batch_launch(const TlBatch &T, int prec, int pass, double omg, double lb, double ub, int bmode,
+                    unsigned *ctr, cudaStream_t s, bool dry);
 // Delta copy of the form (sirt_delta.cu): does nothing when too many groups
 // would need the side table.
 int csr_make_delta(DevCSR &A, int prec, cudaStream_t s);

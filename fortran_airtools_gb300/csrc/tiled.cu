@@ -30,6 +30,7 @@
 // slots in flight per chunk and claims chunks dynamically.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <mutex>
 #include <type_traits>
 #include <vector>
@@ -588,13 +589,12 @@ __device__ __forceinline__ ACC chain_sum(const ACC (&a)[K]) {
 
 // Partial sums of all segments. Persistent CTAs take work units through
 // ctr[0] (reset by the last CTA through ctr[1] for the next launch).
+// One work unit U (a tile and a range of its chunks) by the whole CTA: the
+// tile's shared copy, then the partial sums of the unit's segments; ends with
+// a barrier (the tile is rewritten by the next unit).
 template <class LD, typename XT, typename ACC, int D, bool CONT>
-__global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, LD ldr,
-                                                            const XT *__restrict__ x,
-                                                            ACC *__restrict__ part, unsigned *ctr) {
-    extern __shared__ __align__(16) unsigned char tl_smem[];
-    XT *xs = reinterpret_cast<XT *>(tl_smem);
-    __shared__ int s_unit, s_chunk;
+__device__ __forceinline__ void tl_unit(const TlArgs &P, const LD &ldr, const XT *__restrict__ x,
+                                        ACC *__restrict__ part, int4 U, XT *xs, int &s_chunk) {
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int E = LD::E;
     // independent sums: one per ring slot in the FP32 forms, one in FP64 (whose
@@ -603,14 +603,8 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
     constexpr int KC = sizeof(ACC) == 8 ? 1 : 2;
     constexpr int KD = sizeof(ACC) == 8 ? 1 : D;
     const int lane = threadIdx.x & 31;
-    const TlGeo &G = P.G;
-    for (;;) {
-        if (threadIdx.x == 0) s_unit = (int)atomicAdd(ctr, 1u);
-        __syncthreads();
-        const int u = s_unit;
-        if (u >= P.nunits) break;
-        const int4 U = P.units[u];
-        tl_fill_tile(G, U, x, xs);
+    {
+        tl_fill_tile(P.G, U, x, xs);
         if (threadIdx.x == 0) s_chunk = U.y;
         __syncthreads();
         if constexpr (CONT) {
@@ -718,6 +712,22 @@ __global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, 
             }
         }
         __syncthreads();  // the tile is rewritten by the next unit
+    }
+}
+
+template <class LD, typename XT, typename ACC, int D, bool CONT>
+__global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tl_partials(TlArgs P, LD ldr,
+                                                            const XT *__restrict__ x,
+                                                            ACC *__restrict__ part, unsigned *ctr) {
+    extern __shared__ __align__(16) unsigned char tl_smem[];
+    XT *xs = reinterpret_cast<XT *>(tl_smem);
+    __shared__ int s_unit, s_chunk;
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = (int)atomicAdd(ctr, 1u);
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= P.nunits) break;
+        tl_unit<LD, XT, ACC, D, CONT>(P, ldr, x, part, P.units[u], xs, s_chunk);
     }
     if (threadIdx.x == 0) {
         const unsigned done = atomicAdd(ctr + 1, 1u);
@@ -1137,6 +1147,237 @@ bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cuda
     if (!tl.has_rq) return false;
     if (M.qsigned) return run(TlFused<int16_t>{tl.rq.as<uint4>()});
     return run(TlFused<uint16_t>{tl.rq.as<uint4>()});
+}
+
+// ---- batches: the tiled passes of many problems in one launch ---------------
+namespace {
+
+// One problem's tiled pass (device table entry).
+struct TlbDesc {
+    TlArgs P;                  // its chunks, units and tile geometry
+    const void *idx, *val;     // split copy: local indices and values; fused: records
+    const void *x;             // the gathered vector
+    void *part;                // its partial sums
+    const int64_t *segbase;
+    const double *b, *M;       // pass 1 epilogue
+    void *r;
+    const double *D;           // pass 2 epilogue
+    double *x64;
+    float *x32;
+    double scale;              // 1, or the fixed-point scale of 16-bit codes
+};
+
+// last p in [0, np) with off[p] <= v (off[0] = 0 <= v < off[np])
+__device__ __forceinline__ int tlb_owner(const int64_t *__restrict__ off, int np, int64_t v) {
+    int lo = 0, hi = np;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <class LD> struct TlbMake;
+template <typename VT> struct TlbMake<TlSplit<VT>> {
+    __device__ static TlSplit<VT> make(const TlbDesc &d) {
+        return TlSplit<VT>{(const uint2 *)d.idx, (const VT *)d.val};
+    }
+};
+template <typename VT> struct TlbMake<TlFused<VT>> {
+    __device__ static TlFused<VT> make(const TlbDesc &d) { return TlFused<VT>{(const uint4 *)d.idx}; }
+};
+
+// The units of all problems numbered consecutively (uoff): a CTA takes the
+// next unit, finds its problem and runs the single-problem unit body on it, so
+// problems of any sizes share the GPU without tails.
+template <class LD, typename XT, typename ACC>
+__global__ void __launch_bounds__(kTlThreads, LD::CTAS) k_tlb_partials(const TlbDesc *__restrict__ desc,
+                                                             const int64_t *__restrict__ uoff, int np,
+                                                             unsigned *ctr) {
+    extern __shared__ __align__(16) unsigned char tl_smem[];
+    XT *xs = reinterpret_cast<XT *>(tl_smem);
+    __shared__ int s_unit, s_chunk;
+    const int64_t total = __ldg(uoff + np);
+    for (;;) {
+        if (threadIdx.x == 0) s_unit = (int)atomicAdd(ctr, 1u);
+        __syncthreads();
+        const int64_t u = s_unit;
+        if (u >= total) break;
+        const int p = tlb_owner(uoff, np, u);
+        const TlbDesc &d = desc[p];
+        const TlArgs P = d.P;
+        tl_unit<LD, XT, ACC, 2, true>(P, TlbMake<LD>::make(d), (const XT *)d.x, (ACC *)d.part,
+                                      P.units[u - __ldg(uoff + p)], xs, s_chunk);
+    }
+    if (threadIdx.x == 0) {
+        const unsigned done = atomicAdd(ctr + 1, 1u);
+        if (done == gridDim.x - 1) {  // every CTA has stopped taking units
+            ctr[0] = 0u;
+            ctr[1] = 0u;
+        }
+    }
+}
+
+// Row sums of the partials (in row order) and each problem's epilogue.
+template <int PASS, typename ACC>
+__global__ void k_tlb_rows(const TlbDesc *__restrict__ desc, const int64_t *__restrict__ roff, int np,
+                           double omg, double lb, double ub, int bmode) {
+    const int64_t total = __ldg(roff + np);
+    // a thread's rows only grow, so its problem is looked up (and its
+    // pointers loaded) only when a row passes the current problem's end
+    int64_t lo = 0, hi = 0;
+    const int64_t *segbase = nullptr;
+    const ACC *part = nullptr;
+    const double *b = nullptr, *M = nullptr, *D = nullptr;
+    void *r = nullptr;
+    double *x64 = nullptr;
+    float *x32 = nullptr;
+    double scale = 1.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i >= hi) {
+            const int p = tlb_owner(roff, np, i);
+            const TlbDesc &d = desc[p];
+            lo = __ldg(roff + p);
+            hi = __ldg(roff + p + 1);
+            segbase = d.segbase;
+            part = (const ACC *)d.part;
+            b = d.b; M = d.M; r = d.r;
+            D = d.D; x64 = d.x64; x32 = d.x32;
+            scale = d.scale;
+        }
+        const int64_t row = i - lo;
+        ACC acc = 0;
+        for (int64_t k = segbase[row]; k < segbase[row + 1]; ++k) acc += part[k];
+        if constexpr (sizeof(ACC) == 8) {
+            if (PASS == 1) EpiResidF64{b, M, (double *)r}(row, acc);
+            else EpiUpdateF64{D, x64, omg, lb, ub, bmode}(row, acc);
+        } else {
+            if (PASS == 1) EpiResidLP{b, M, (float *)r, scale}(row, acc);
+            else EpiUpdateLP{D, x64, x32, omg, lb, ub, bmode, scale}(row, acc);
+        }
+    }
+}
+
+// Resident CTAs of a partials kernel at `smem` bytes, looked up once (so no
+// occupancy query runs while a graph is captured).
+int tlb_occupancy(const void *kernel, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, size_t>, int> table;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_pair(kernel, smem);
+    const auto it = table.find(key);
+    if (it != table.end()) return it->second;
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kTlThreads, smem);
+    table[key] = std::max(occ, 1);
+    return table[key];
+}
+
+template <class LD, typename XT, typename ACC>
+int tlb_run(const TlBatch &T, int pass, double omg, double lb, double ub, int bmode, unsigned *ctr,
+            cudaStream_t s, bool dry) {
+    auto kernel = k_tlb_partials<LD, XT, ACC>;
+    const void *kp = reinterpret_cast<const void *>(kernel);
+    FAIR_CUDA(smem_allow(kp, T.smem));
+    const int occ = tlb_occupancy(kp, T.smem);
+    if (dry) return FAIR_OK;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, T.units));
+    const TlbDesc *d = T.desc.as<TlbDesc>();
+    kernel<<<grid, kTlThreads, T.smem, s>>>(d, T.uoff.as<int64_t>(), T.np, ctr);
+    if (pass == 1)
+        k_tlb_rows<1, ACC><<<tl_grid(T.rows), 256, 0, s>>>(d, T.roff.as<int64_t>(), T.np, omg, lb, ub, bmode);
+    else
+        k_tlb_rows<2, ACC><<<tl_grid(T.rows), 256, 0, s>>>(d, T.roff.as<int64_t>(), T.np, omg, lb, ub, bmode);
+    return FAIR_OK;
+}
+
+}  // namespace
+
+bool tl_batch_ready(const DevCSR &M, int prec) {
+    const DevCSR::Tiled &tl = M.tl;
+    if (!tl.built() || (!tl.has_idx && (prec == FAIR_PREC_F64 || prec == FAIR_PREC_F32))) return false;
+    switch (prec) {
+        case FAIR_PREC_F64: return tl.has_v64;
+        case FAIR_PREC_F32: return tl.has_v32;
+        case FAIR_PREC_F16: return tl.has_r16;
+        default: return tl.has_rq && !M.qsigned;
+    }
+}
+
+void tl_drop_build(DevCSR &M) {
+    DevCSR::Tiled &tl = M.tl;
+    tl.srow.release();
+    tl.sstart.release();
+    tl.send.release();
+    // the 6-entry step records (a batched pass reads the 4-entry slots)
+    tl.soff6.release(); tl.anc6.release(); tl.code6.release(); tl.side6.release();
+    tl.r6_16.release(); tl.r6_q.release();
+    tl.built6 = tl.has6_16 = tl.has6_q = false;
+    tl.tried6 = true;
+}
+
+int tl_batch_bind(TlBatch &T, int prec, const std::vector<TlBatchProb> &probs) {
+    const int np = (int)probs.size();
+    std::vector<TlbDesc> d(np);
+    std::vector<int64_t> uo(np + 1, 0), ro(np + 1, 0);
+    int64_t cells = 1;
+    for (int p = 0; p < np; ++p) {
+        const DevCSR &M = *probs[p].M;
+        const DevCSR::Tiled &tl = M.tl;
+        if (!tl_batch_ready(M, prec)) {
+            set_detail("batched tiled pass: a problem without its tiled copy");
+            return FAIR_ERR_STATE;
+        }
+        TlbDesc &e = d[p];
+        e.P = TlArgs{tl.soff.as<int64_t>(), tl.pslot.as<int32_t>(), tl.units.as<int4>(), tl.nunits, tl_geo(tl)};
+        switch (prec) {
+            case FAIR_PREC_F64: e.idx = tl.idx.p; e.val = tl.v64.p; break;
+            case FAIR_PREC_F32: e.idx = tl.idx.p; e.val = tl.v32.p; break;
+            case FAIR_PREC_F16: e.idx = tl.r16.p; e.val = nullptr; break;
+            default: e.idx = tl.rq.p; e.val = nullptr; break;
+        }
+        e.x = probs[p].xin;
+        e.part = tl.part.p;
+        e.segbase = tl.segbase.as<int64_t>();
+        e.b = probs[p].b;
+        e.M = probs[p].Minv;
+        e.r = probs[p].r;
+        e.D = probs[p].D;
+        e.x64 = probs[p].x;
+        e.x32 = probs[p].x32;
+        e.scale = prec == FAIR_PREC_Q16 ? M.qscale : 1.0;
+        uo[p + 1] = uo[p] + tl.nunits;
+        ro[p + 1] = ro[p] + M.m;
+        cells = std::max<int64_t>(cells, (int64_t)e.P.G.cells() + 1);
+    }
+    FAIR_TRY(T.desc.grow(sizeof(TlbDesc) * std::max(np, 1)));
+    FAIR_TRY(T.uoff.grow(sizeof(int64_t) * (np + 1)));
+    FAIR_TRY(T.roff.grow(sizeof(int64_t) * (np + 1)));
+    // synchronous copies: the host tables go out of scope on return
+    FAIR_CUDA(cudaMemcpy(T.desc.p, d.data(), sizeof(TlbDesc) * np, cudaMemcpyHostToDevice));
+    FAIR_CUDA(cudaMemcpy(T.uoff.p, uo.data(), sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice));
+    FAIR_CUDA(cudaMemcpy(T.roff.p, ro.data(), sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice));
+    T.np = np;
+    T.units = uo[np];
+    T.rows = ro[np];
+    T.smem = (size_t)cells * (prec == FAIR_PREC_F64 ? sizeof(double) : sizeof(float));
+    return FAIR_OK;
+}
+
+int tl_batch_launch(const TlBatch &T, int prec, int pass, double omg, double lb, double ub, int bmode,
+                    unsigned *ctr, cudaStream_t s, bool dry) {
+    if (T.np == 0) return FAIR_OK;
+    switch (prec) {
+        case FAIR_PREC_F64:
+            return tlb_run<TlSplit<double>, double, double>(T, pass, omg, lb, ub, bmode, ctr, s, dry);
+        case FAIR_PREC_F32:
+            return tlb_run<TlSplit<float>, float, float>(T, pass, omg, lb, ub, bmode, ctr, s, dry);
+        case FAIR_PREC_F16:
+            return tlb_run<TlFused<__half>, float, float>(T, pass, omg, lb, ub, bmode, ctr, s, dry);
+        default:
+            return tlb_run<TlFused<uint16_t>, float, float>(T, pass, omg, lb, ub, bmode, ctr, s, dry);
+    }
 }
 
 }  // namespace fair

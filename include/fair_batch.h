@@ -30,6 +30,17 @@ int fair_batch_destroy(fair_batch b);
 /* Use the caller's stream (NULL: back to a stream of the batch's own). */
 int fair_batch_set_stream(fair_batch b, void *cuda_stream);
 
+/* Layout of the problems' passes, chosen before the first fair_batch_add:
+ * 0 (default) the packed index streams (the CSR in FAIR_PREC_F64); 1 the
+ * tiled copies of A (rays cut by 96 x 96 image tiles) and A' (pixels cut by
+ * 32 x 32 tiles times angle blocks), the vector gathered into shared memory
+ * per tile (the layout of fair_sirt_set_lanes code 9), for every problem
+ * whose columns form an N x N image and whose rays are p bins per angle;
+ * other problems keep the packed layout. A tiled pass is two launches
+ * (partial sums per ray segment, then row sums in row order), each covering
+ * every tiled problem; the results equal fair_sirt with layout code 9. */
+int fair_batch_set_layout(fair_batch b, int32_t layout);
+
 /* Appends the matrix of handle h as the next problem. take = 1 moves the
  * matrix out of h (h is left holding no matrix, as after fair_csr_create);
  * take = 0 copies it. The weights of both SIRT methods are computed in FP64

@@ -115,6 +115,91 @@ def test_device_api_graph_reuse_and_unbatched(problems, fair):
     B.close()
 
 
+def single_code9(fair, A, b, prec, method, K, opts):
+    """fair_sirt on the tiled copies (layout code 9 for both passes)."""
+    from fortran_airtools_gb300._clib import check, lib
+    A.set_precision(prec)
+    try:
+        check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, 9, 9)))
+        return fair.airms.sirt(method, A, b, K, opts=opts)
+    finally:
+        default = (8, 8, 0, 0) if prec == "f64" else (8, 8, 1, 1)
+        check(lib().fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(*default)))
+        A.set_precision("f64")
+
+
+@pytest.mark.parametrize("method", ["sart", "cimmino"])
+@pytest.mark.parametrize("prec", ["f64", "f32", "f16", "q16"])
+def test_tiled_batch_equals_single(problems, fair, oracle, prec, method):
+    """layout 'tiled': every problem on its tiled copies of A and A' (two
+    launches per pass for the whole batch); the same numbers as fair_sirt
+    on the tiled copies, problem by problem, bit for bit."""
+    B = fair.Batch(prec, layout="tiled")
+    for A, _, _ in problems:
+        B.add(A)
+    info = B.info()
+    o = fair.airms.options(lbound=0.0, ubound=1.0)
+    ball = np.concatenate([b for _, _, b in problems])
+    X = B.sirt(method, ball, 20, opts=o)
+    _, co = B.offsets()
+    tol = {"f64": 1e-10, "f32": 1e-5, "f16": 5e-3, "q16": 1e-4}[prec]
+    for p, (A, R, b) in enumerate(problems):
+        xs = single_code9(fair, A, b, prec, method, 20, o)
+        assert np.array_equal(X[co[p]:co[p + 1]], xs)
+        xr = oracle.sirt(method, R, b, 20, opts=oracle.options(lbound=0.0, ubound=1.0))
+        assert rel_err(X[co[p]:co[p + 1]], xr) < tol
+    from fortran_airtools_gb300._clib import check, lib
+    n = C.c_int64()
+    check(lib().fair_batch_launches(B.handle, 20, C.byref(n)))
+    assert n.value == (0 if prec == "f64" else 1) + 2 * 2 * 20  # partials + row sums per pass
+    assert info["device_bytes"] > 0
+    B.close()
+
+
+def test_tiled_batch_mixed_and_device_api(problems, fair, oracle):
+    """A problem whose columns are not an N x N image keeps the packed layout
+    beside the tiled ones (three launches per pass); the device-resident
+    graph, its reuse and the problem-by-problem launches give the same numbers."""
+    import torch
+    rng = np.random.default_rng(5)
+    m, n, L = 60, 150, 10  # 150 columns: no square image, no tiled copy
+    # banded rows of 10 consecutive columns that cover every column
+    starts = np.minimum((np.arange(m) * 2.5).astype(np.int64), n - L)
+    IA = np.arange(0, L * (m + 1), L, dtype=np.int64)
+    JA = (starts[:, None] + np.arange(L)[None, :]).ravel().astype(np.int32) + 1
+    vA = rng.random(IA[-1]) + 0.05
+    odd = fair.CSRMatrix.construct(m, n, vA, IA.astype(np.int32), JA)
+    Rodd = oracle.OracleCSR(m, n, IA, JA, vA)
+    bodd = oracle.matvecmul(Rodd, rng.random(n))
+    probs = [(A, R, b) for A, R, b in problems[:3]] + [(odd, Rodd, bodd)] + [problems[3]]
+    B = fair.Batch("f32", layout="tiled")
+    for A, _, _ in probs:
+        B.add(A)
+    from fortran_airtools_gb300._clib import check, lib
+    cnt = C.c_int64()
+    check(lib().fair_batch_launches(B.handle, 10, C.byref(cnt)))
+    assert cnt.value == 1 + 2 * 3 * 10
+    o = fair.airms.options(lbound=0.0, ubound=1.0)
+    ball = np.concatenate([b for _, _, b in probs])
+    ref = B.sirt("sart", ball, 10, opts=o)
+    _, co = B.offsets()
+    for p, (A, R, b) in enumerate(probs):
+        xr = oracle.sirt("sart", R, b, 10, opts=oracle.options(lbound=0.0, ubound=1.0))
+        assert rel_err(ref[co[p]:co[p + 1]], xr) < 1e-5
+    B.prepare("sart", o)
+    stream = torch.cuda.Stream()
+    B.set_stream(stream.cuda_stream)
+    d_b = torch.from_numpy(ball).cuda()
+    for batched in (True, True, False):
+        d_x = torch.zeros(B.info()["cols"], dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        B.run_device(d_b.data_ptr(), d_x.data_ptr(), 10, batched=batched)
+        stream.synchronize()
+        assert np.array_equal(d_x.cpu().numpy(), ref)
+    B.close()
+    odd.close()
+
+
 def test_take_moves_matrix(fair, oracle):
     A, R = build(fair, oracle, "par", 16, 12, 24)
     B = fair.Batch("f64")
@@ -127,8 +212,18 @@ def test_take_moves_matrix(fair, oracle):
     B.close()
 
 
-def test_batch_errors(fair):
+def test_batch_errors(fair, oracle):
+    from fortran_airtools_gb300._clib import lib
+    with pytest.raises(ValueError):
+        fair.Batch("f32", layout="rows")
     B = fair.Batch("f32")
+    assert lib().fair_batch_set_layout(B.handle, 2) == 4  # FAIR_ERR_ARG
+    Bt = fair.Batch("f64")
+    At, _ = build(fair, oracle, "par", 16, 12, 24)
+    Bt.add(At)
+    assert lib().fair_batch_set_layout(Bt.handle, 1) == 9  # FAIR_ERR_STATE: after the first add
+    Bt.close()
+    At.close()
     with pytest.raises(fair.FairError):
         B.prepare("sart")  # empty batch
     with pytest.raises(fair.FairError):
