@@ -433,26 +433,30 @@ template <typename VT> struct TlFused {
         Conv2B<VT>::to(r.z, r.w, v);
     }
 };
-template <typename VT> struct TlStep6 {  // 6-entry step records
+// LB: bits of a code's low field (the copy's L6: 2, 3 or 5), a compile-time
+// constant so that the decode's shifts are immediates.
+template <typename VT, int LB> struct TlStep6 {  // 6-entry step records
     static constexpr int E = 6;
     static constexpr int CTAS = 3;
     const uint4 *rec;
     const int32_t *anc;
     const int4 *side;
-    int L;       // bits of a code's low field
-    int hs, hm;  // shift of its high field, and the high field's step (0 when L = 5)
+    int hm;  // the high field's step S
     using Raw = uint4;
     struct State {
         int li;  // the lane's last local index
     };
-    TlStep6(const uint4 *r, const int32_t *a, const int4 *sd, int S, int L_)
-        : rec(r), anc(a), side(sd), L(L_), hs(L_ >= 5 ? 31 : 27 + L_), hm(L_ >= 5 ? 0 : S) {}
-    // the step of code q of word w: step_decode<5>((w >> 5q) & 31, S, L) by
-    // shifts alone (the signed low L bits, the signed high 5 - L bits)
+    TlStep6(const uint4 *r, const int32_t *a, const int4 *sd, int S) : rec(r), anc(a), side(sd), hm(S) {}
+    // the step of code q of word w: step_decode<5>((w >> 5q) & 31, S, LB) by
+    // shifts alone (the signed low LB bits, the signed high 5 - LB bits)
     __device__ __forceinline__ int step(uint32_t w, int q) const {
-        const int lo = (int)(w << (32 - L - 5 * q)) >> (32 - L);
-        const int hi = (int)(w << (27 - 5 * q)) >> hs;
-        return lo + hi * hm;
+        const int lo = (int)(w << (32 - LB - 5 * q)) >> (32 - LB);
+        if constexpr (LB >= 5) {
+            return lo;
+        } else {
+            const int hi = (int)(w << (27 - 5 * q)) >> (27 + LB);
+            return lo + hi * hm;
+        }
     }
     __device__ __forceinline__ State init(int64_t lanepos) const { return {__ldg(anc + lanepos)}; }
     __device__ __forceinline__ Raw load(int64_t j) const { return ld_stream(rec + j); }
@@ -1136,9 +1140,17 @@ bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cuda
     if (code == 14 && tl.built6 && (h ? tl.has6_16 : tl.has6_q)) {
         const int32_t *anc = tl.anc6.as<int32_t>();
         const int4 *side = tl.side6.as<int4>();
-        if (h) return run(TlStep6<__half>(tl.r6_16.as<uint4>(), anc, side, tl.S6, tl.L6));
-        if (M.qsigned) return run(TlStep6<int16_t>(tl.r6_q.as<uint4>(), anc, side, tl.S6, tl.L6));
-        return run(TlStep6<uint16_t>(tl.r6_q.as<uint4>(), anc, side, tl.S6, tl.L6));
+        // the copy's step code: L6 is one of the builder's candidates 2, 3, 5
+        auto run6 = [&](auto vt) -> bool {
+            using VT = decltype(vt);
+            const uint4 *rec = (h ? tl.r6_16 : tl.r6_q).as<uint4>();
+            if (tl.L6 == 2) return run(TlStep6<VT, 2>(rec, anc, side, tl.S6));
+            if (tl.L6 == 3) return run(TlStep6<VT, 3>(rec, anc, side, tl.S6));
+            return run(TlStep6<VT, 5>(rec, anc, side, tl.S6));
+        };
+        if (h) return run6(__half());
+        if (M.qsigned) return run6(int16_t());
+        return run6(uint16_t());
     }
     if (h) {
         if (!tl.has_r16) return false;
