@@ -32,7 +32,8 @@ namespace fair {
 
 namespace {
 
-constexpr int kG = 8;  // lanes per row of the multi-vector engine
+constexpr int kG = 8;        // lanes per row of the multi-vector engine (one right-hand side)
+constexpr int kRhsRows = 8;  // rows per chunk of the engine with right-hand sides across lanes
 
 template <typename T, int NR>
 __device__ __forceinline__ void load_row_vec(const T *__restrict__ p, T (&o)[NR]) {
@@ -89,6 +90,66 @@ __device__ __forceinline__ void chunk_rows_multi(const int64_t *__restrict__ row
     finish_chunks(sched, nwarps, lane);
 }
 
+// The same products with the right-hand sides across the lanes (NR = 4 or
+// 16): lane l handles right-hand side l % NR of entry slot l / NR, so a warp
+// step covers E = 32 / NR entries of one row and each entry's NR values of x
+// are one contiguous run of NR x sizeof(T) bytes. The warp reads a row's
+// entries 32 at a time (lane l loads entry l of the block: one coalesced load
+// of columns and one of values, the next block's issued before the current
+// one is used), hands each entry to its slot's lanes by shuffles, and keeps
+// the block's 32 / E gathers of x in flight. The E slots are added by
+// shuffles at the row's end and lanes 0..NR-1 apply the epilogue to the row's
+// NR sums (Epi::one). A warp walks the kRhsRows rows of a chunk in turn;
+// small chunks keep every warp of a persistent grid busy.
+template <typename T, int NR, class Epi>
+__device__ __forceinline__ void chunk_rows_rhs(const int64_t *__restrict__ rowptr, int32_t m,
+                                               const int32_t *__restrict__ col,
+                                               const T *__restrict__ val, const T *__restrict__ x,
+                                               const Epi &epi, unsigned *sched) {
+    static_assert(NR == 4 || NR == 16, "4 or 16 right-hand sides");
+    constexpr int E = 32 / NR, STEPS = 32 / E, NA = 4, CR = kRhsRows;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, slot = lane / NR, c = lane % NR;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nchunks = ((int64_t)m + CR - 1) / CR;
+    for (int64_t ch = next_chunk(sched, 0, nwarps, lane); ch < nchunks;
+         ch = next_chunk(sched, ch, nwarps, lane)) {
+        const int64_t base = ch * CR;
+        const int rows = (int)((int64_t)m - base < CR ? (int64_t)m - base : CR);
+        for (int rr = 0; rr < rows; ++rr) {
+            const int64_t row = base + rr;
+            const int64_t s = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
+            T acc[NA];
+#pragma unroll
+            for (int a = 0; a < NA; ++a) acc[a] = 0;
+            int64_t kk = s + lane;
+            int32_t cl = kk < e ? __ldcs(col + kk) : 0;
+            T vl = kk < e ? __ldcs(val + kk) : (T)0;
+            for (int64_t kb = s; kb < e; kb += 32) {
+                // the next block's entries, loaded while this one is used
+                const int64_t kn = kb + 32 + lane;
+                const int32_t cn = kn < e ? __ldcs(col + kn) : 0;
+                const T vn = kn < e ? __ldcs(val + kn) : (T)0;
+                const int nb = (int)(e - kb < 32 ? e - kb : 32);
+#pragma unroll
+                for (int t = 0; t < STEPS; ++t) {
+                    const int src = t * E + slot;
+                    const int32_t cj = __shfl_sync(FULL, cl, src);
+                    const T vj = __shfl_sync(FULL, vl, src);
+                    if (src < nb) acc[t % NA] += vj * __ldg(x + (size_t)cj * NR + c);
+                }
+                cl = cn;
+                vl = vn;
+            }
+            T v = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+            for (int o = 16; o >= NR; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if (lane < NR) epi.one(row, c, v);
+        }
+    }
+    finish_chunks(sched, nwarps, lane);
+}
+
 template <typename T>
 __device__ __forceinline__ T boxT(T t, int bmode, T lb, T ub) {
     if (bmode & 1) t = t < ub || t != t ? t : ub;   // min(t, ub), the non-NaN wins
@@ -101,9 +162,10 @@ template <typename T, int NR>
 struct EpiFwdResid {
     const T *b, *M;
     T *r;
+    __device__ void one(int64_t i, int c, T v) const { r[i * NR + c] = (b[i * NR + c] - v) / M[i]; }
     __device__ void operator()(int64_t i, const T (&acc)[NR]) const {
 #pragma unroll
-        for (int c = 0; c < NR; ++c) r[i * NR + c] = (b[i * NR + c] - acc[c]) / M[i];
+        for (int c = 0; c < NR; ++c) one(i, c, acc[c]);
     }
 };
 // forward pass 2: g = A' r (kept when recording), x = P(x + lam g / D)
@@ -113,14 +175,15 @@ struct EpiFwdUpdate {
     T *x, *gsave;
     T lb, ub;
     int bmode;
+    __device__ void one(int64_t j, int c, T v) const {
+        T u = lam[c] * v;
+        if (D) u = u / D[j];
+        if (gsave) gsave[j * NR + c] = v;
+        x[j * NR + c] = boxT<T>(x[j * NR + c] + u, bmode, lb, ub);
+    }
     __device__ void operator()(int64_t j, const T (&acc)[NR]) const {
 #pragma unroll
-        for (int c = 0; c < NR; ++c) {
-            T u = lam[c] * acc[c];
-            if (D) u = u / D[j];
-            if (gsave) gsave[j * NR + c] = acc[c];
-            x[j * NR + c] = boxT<T>(x[j * NR + c] + u, bmode, lb, ub);
-        }
+        for (int c = 0; c < NR; ++c) one(j, c, acc[c]);
     }
 };
 // reverse, over A: w = (A t) / M (0 on empty rows), gb += lam w
@@ -128,13 +191,14 @@ template <typename T, int NR>
 struct EpiAdjA {
     const T *M, *lam;
     T *w, *gb;
+    __device__ void one(int64_t i, int c, T v) const {
+        T wi = M[i] != (T)0 ? v / M[i] : (T)0;
+        w[i * NR + c] = wi;
+        gb[i * NR + c] += lam[c] * wi;
+    }
     __device__ void operator()(int64_t i, const T (&acc)[NR]) const {
 #pragma unroll
-        for (int c = 0; c < NR; ++c) {
-            T wi = M[i] != (T)0 ? acc[c] / M[i] : (T)0;
-            w[i * NR + c] = wi;
-            gb[i * NR + c] += lam[c] * wi;
-        }
+        for (int c = 0; c < NR; ++c) one(i, c, acc[c]);
     }
 };
 // reverse, over A': gx = gz - lam A' w
@@ -142,16 +206,23 @@ template <typename T, int NR>
 struct EpiAdjAT {
     const T *gz, *lam;
     T *gx;
+    __device__ void one(int64_t j, int c, T v) const { gx[j * NR + c] = gz[j * NR + c] - lam[c] * v; }
     __device__ void operator()(int64_t j, const T (&acc)[NR]) const {
 #pragma unroll
-        for (int c = 0; c < NR; ++c) gx[j * NR + c] = gz[j * NR + c] - lam[c] * acc[c];
+        for (int c = 0; c < NR; ++c) one(j, c, acc[c]);
     }
 };
 
+// (256, 4): up to 64 registers, so the 16 gathers of a block stay in flight
+// without spills (measured: FP32 39 ms per 16-problem adjoint against 58 ms
+// when the compiler chose 32 registers).
 template <typename T, int NR, class Epi>
-__global__ void __launch_bounds__(256) k_multi(const int64_t *rowptr, int32_t m, const int32_t *col,
+__global__ void __launch_bounds__(256, 4) k_multi(const int64_t *rowptr, int32_t m, const int32_t *col,
                                                const T *val, const T *x, Epi epi, unsigned *sched) {
-    chunk_rows_multi<T, NR>(rowptr, m, col, val, x, epi, sched);
+    if constexpr (NR == 1)
+        chunk_rows_multi<T, NR>(rowptr, m, col, val, x, epi, sched);
+    else
+        chunk_rows_rhs<T, NR>(rowptr, m, col, val, x, epi, sched);
 }
 
 // Elementwise reverse step: gz = gx * [P does not clamp z], t = gz / D,
@@ -230,12 +301,15 @@ int egrid(int64_t n) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm_count() * 4));
 }
 
+// Blocks of 8 warps for the chunks of m rows (32 rows per chunk for one
+// right-hand side, kRhsRows for more), at most the resident blocks.
 template <class K>
-int mgrid(K kernel, int64_t m) {
+int mgrid(K kernel, int64_t m, int nr) {
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0);
     if (occ < 1) occ = 1;
-    int64_t need = (((int64_t)m + 31) / 32 + 7) / 8;
+    const int64_t rpc = nr == 1 ? 32 : kRhsRows;
+    int64_t need = (((int64_t)m + rpc - 1) / rpc + 7) / 8;
     return (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, need));
 }
 
@@ -298,11 +372,11 @@ int run_group(const DevCSR &A, const DevCSR &AT, const T *vA, const T *vAT, bool
     auto fwd_step = [&](T *gsave) -> int {
         EpiFwdResid<T, NR> e1{B.b.as<T>(), B.M.as<T>(), B.r.as<T>()};
         auto k1 = k_multi<T, NR, EpiFwdResid<T, NR>>;
-        k1<<<mgrid(k1, m), 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(), vA,
+        k1<<<mgrid(k1, m, NR), 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(), vA,
                                         B.x.as<T>(), e1, sched);
         EpiFwdUpdate<T, NR> e2{D, B.lam.as<T>(), B.x.as<T>(), gsave, tlb, tub, bmode};
         auto k2 = k_multi<T, NR, EpiFwdUpdate<T, NR>>;
-        k2<<<mgrid(k2, n), 256, 0, s>>>(AT.rowptr.as<int64_t>(), AT.m, AT.col.as<int32_t>(), vAT,
+        k2<<<mgrid(k2, n, NR), 256, 0, s>>>(AT.rowptr.as<int64_t>(), AT.m, AT.col.as<int32_t>(), vAT,
                                         B.r.as<T>(), e2, sched);
         FAIR_CUDA(cudaGetLastError());
         return FAIR_OK;
@@ -344,11 +418,11 @@ int run_group(const DevCSR &A, const DevCSR &AT, const T *vA, const T *vAT, bool
                                       cudaMemcpyDeviceToHost, s));
             EpiAdjA<T, NR> ea{B.M.as<T>(), B.lam.as<T>(), B.w.as<T>(), B.gb.as<T>()};
             auto ka = k_multi<T, NR, EpiAdjA<T, NR>>;
-            ka<<<mgrid(ka, m), 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(), vA,
+            ka<<<mgrid(ka, m, NR), 256, 0, s>>>(A.rowptr.as<int64_t>(), A.m, A.col.as<int32_t>(), vA,
                                             B.t.as<T>(), ea, sched);
             EpiAdjAT<T, NR> eb{B.gz.as<T>(), B.lam.as<T>(), B.gx.as<T>()};
             auto kb = k_multi<T, NR, EpiAdjAT<T, NR>>;
-            kb<<<mgrid(kb, n), 256, 0, s>>>(AT.rowptr.as<int64_t>(), AT.m, AT.col.as<int32_t>(),
+            kb<<<mgrid(kb, n, NR), 256, 0, s>>>(AT.rowptr.as<int64_t>(), AT.m, AT.col.as<int32_t>(),
                                             vAT, B.w.as<T>(), eb, sched);
             FAIR_CUDA(cudaGetLastError());
             FAIR_CUDA(cudaStreamSynchronize(s));
