@@ -329,7 +329,7 @@ long long host_key(double v) {
 // shared memory, Kaczmarz 0.83M, 0.97M, 1.00M, 0.94M; fan beam N=512, x in
 // global memory, symmetric Kaczmarz 0.18M, 0.33M, 0.44M, 0.39M and random
 // Kaczmarz 0.17M, 0.30M, 0.43M, 0.42M.
-int sweep_warps(bool) {
+int sweep_warps() {
     const char *env = getenv("FAIR_SWEEP_WARPS");
     if (env) {
         int w = atoi(env);
@@ -365,7 +365,7 @@ int kaczmarz_sweep(const SweepDev &S, int dir, cudaStream_t s) {
     FAIR_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const size_t need = sizeof(double) * (size_t)A.n;
     const bool smem = need + 4096 <= (size_t)optin;
-    const int W = sweep_warps(smem);
+    const int W = sweep_warps();
     // entries per lane held in registers (longer rows finish in a loop)
     const int per_lane = (A.max_row + 32 * W - 1) / (32 * W);
     switch (W) {
