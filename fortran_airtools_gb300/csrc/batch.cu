@@ -325,13 +325,15 @@ int bind_vectors(fair_batch_s *B, const double *d_b, double *d_x) {
     return FAIR_OK;
 }
 
-void batch_pass(fair_batch_s *B, int pass, cudaStream_t s, bool dry = false) {
+// One batched pass (dry: only the kernel attributes and grids, outside a
+// graph capture); launch errors are left for the caller's cudaGetLastError.
+int batch_pass(fair_batch_s *B, int pass, cudaStream_t s, bool dry = false) {
     const int np = (int)B->probs.size();
     const BOpts &ot = B->opts;
     if (B->ntiled > 0)
-        tl_batch_launch(pass == 1 ? B->tb1 : B->tb2, B->prec, pass, ot.omg, ot.lb, ot.ub, ot.bmode,
-                        B->sched.as<unsigned>(), s, dry);
-    if (B->ntiled == np) return;  // no problem on the packed streams / CSR
+        FAIR_TRY(tl_batch_launch(pass == 1 ? B->tb1 : B->tb2, B->prec, pass, ot.omg, ot.lb, ot.ub, ot.bmode,
+                                 B->sched.as<unsigned>(), s, dry));
+    if (B->ntiled == np) return FAIR_OK;  // no problem on the packed streams / CSR
     const BPass *P = (pass == 1 ? B->desc1 : B->desc2).as<BPass>();
     const int64_t *c0 = (pass == 1 ? B->c0_1 : B->c0_2).as<int64_t>();
     unsigned *sched = B->sched.as<unsigned>();
@@ -355,14 +357,15 @@ void batch_pass(fair_batch_s *B, int pass, cudaStream_t s, bool dry = false) {
             else launch_pk<uint16_t, 2>(G, NG, dry, P, c0, np, o, sched, s);
             break;
     }
+    return FAIR_OK;
 }
 
 int enqueue_iterations(fair_batch_s *B, int K, cudaStream_t s) {
     if (B->prec != FAIR_PREC_F64 && B->col_off.back() > 0)
         FAIR_TRY(vec_to_f32(B->bound_x, B->col_off.back(), B->x32.as<float>(), s));
     for (int it = 0; it < K; ++it) {
-        batch_pass(B, 1, s);
-        batch_pass(B, 2, s);
+        FAIR_TRY(batch_pass(B, 1, s));
+        FAIR_TRY(batch_pass(B, 2, s));
     }
     FAIR_CUDA(cudaGetLastError());
     return FAIR_OK;
@@ -683,8 +686,8 @@ int fair_batch_run_device(fair_batch B, const double *d_b, double *d_x, int32_t 
     if (K == 0) return FAIR_OK;
     if (!B->gexec || B->g_K != K || B->g_x != d_x || memcmp(B->g_cfg, B->cfg, sizeof(B->cfg)) != 0) {
         fair::drop_graph(B);
-        fair::batch_pass(B, 1, B->stream, true);  // grids looked up outside the capture
-        fair::batch_pass(B, 2, B->stream, true);
+        FAIR_TRY(fair::batch_pass(B, 1, B->stream, true));  // grids looked up outside the capture
+        FAIR_TRY(fair::batch_pass(B, 2, B->stream, true));
         fair::sm_count();
         cudaGraph_t g = nullptr;
         FAIR_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
@@ -817,9 +820,11 @@ int fair_batch_autotune(fair_batch B, const double *d_b, double *d_x, int32_t re
                 for (int c = 0; c < 4 && st == FAIR_OK; ++c) {
                     B->cfg[pass - 1] = lanes[c];
                     B->cfg[pass + 1] = ng;
-                    fair::batch_pass(B, pass, s);  // warm-up
+                    st = fair::batch_pass(B, pass, s);  // warm-up
+                    if (st != FAIR_OK) break;
                     cudaEventRecord(ev[0], s);
-                    for (int r = 0; r < reps; ++r) fair::batch_pass(B, pass, s);
+                    for (int r = 0; r < reps && st == FAIR_OK; ++r) st = fair::batch_pass(B, pass, s);
+                    if (st != FAIR_OK) break;
                     cudaEventRecord(ev[1], s);
                     cudaError_t e = cudaEventSynchronize(ev[1]);
                     if (e != cudaSuccess) { st = fair::cuda_fail(e, "autotune", __FILE__, __LINE__); break; }
