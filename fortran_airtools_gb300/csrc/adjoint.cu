@@ -133,6 +133,9 @@ __device__ __forceinline__ void chunk_rows_rhs(const int64_t *__restrict__ rowpt
                 const int nb = (int)(e - kb < 32 ? e - kb : 32);
 #pragma unroll
                 for (int t = 0; t < STEPS; ++t) {
+                    // steps past the row's end stay predicated: leaving the loop there
+                    // (a warp-uniform break) keeps the gathers from issuing ahead, and
+                    // measured FP32 throughput fell from 25 to 11 batch gradients/s
                     const int src = t * E + slot;
                     const int32_t cj = __shfl_sync(FULL, cl, src);
                     const T vj = __shfl_sync(FULL, vl, src);
