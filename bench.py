@@ -14,8 +14,9 @@ restatement of the reference's Fortran) on a bounded sample of the same
 iteration.
 
 --impl reference times the CPU restatement of the reference (oracle/, all
-host threads for the row-parallel product, serial transposed product) on the
-same workload, one bounded sample of the iteration per step.
+host threads for the row-parallel product and for the transposed product, the
+latter race-free with per-thread copies) on the same workload, one bounded
+sample of the iteration per step.
 """
 from __future__ import annotations
 

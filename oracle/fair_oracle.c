@@ -434,6 +434,45 @@ void or_transvecmul(const or_csr *A, const double *v, double *w) {
     }
 }
 
+/* The same product on nthreads threads, for timing the reference's CPU path:
+ * the reference runs this scatter under OpenMP into one shared vector (a data
+ * race, sparse_matrices.f90:382-392); here each thread scatters a static
+ * range of rows into its own copy of w and the copies are added in thread
+ * order, so the result is deterministic for a given thread count (it differs
+ * from the serial order only by rounding). */
+int or_transvecmul_mt(const or_csr *A, const double *v, double *w, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 1) {
+        const int64_t n = A->n;
+        double *part = calloc((size_t)nthreads * (size_t)(n ? n : 1), sizeof(double));
+        if (!part) return OR_ERR_ALLOC;
+#pragma omp parallel num_threads(nthreads)
+        {
+            const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+            double *wt = part + (size_t)t * (size_t)n;
+            const int64_t k0 = (int64_t)A->m * t / nt, k1 = (int64_t)A->m * (t + 1) / nt;
+            for (int64_t k = k0; k < k1; ++k)
+                for (int64_t i = A->IA[k]; i < A->IA[k + 1]; ++i) {
+                    int32_t c = A->JA[i] - 1;
+                    wt[c] = wt[c] + v[k] * A->vA[i];
+                }
+#pragma omp barrier
+#pragma omp for schedule(static)
+            for (int64_t c = 0; c < n; ++c) {
+                double s = 0.0;
+                for (int u = 0; u < nt; ++u) s = s + part[(size_t)u * (size_t)n + (size_t)c];
+                w[c] = s;
+            }
+        }
+        free(part);
+        return OR_OK;
+    }
+#endif
+    (void)nthreads;
+    or_transvecmul(A, v, w);
+    return OR_OK;
+}
+
 /* reorder, sparse_matrices.f90:492-570: stable counting sort; B is the CSR
  * form of A^T (B.m = A.n, B.JA holds 1-based row indices of A). */
 int or_reorder(const or_csr *A, or_csr *B) {
@@ -566,7 +605,12 @@ int or_sirt(const char *method, const or_csr *A, const double *b, int maxits,
     for (int it = 1; it <= maxits; ++it) {
         or_matvecmul(A, x, r, nthreads);
         for (int64_t i = 0; i < m; ++i) r[i] = (b[i] - r[i]) / M[i];
-        or_transvecmul(A, r, g);
+        if (nthreads > 1) {
+            int st = or_transvecmul_mt(A, r, g, nthreads);
+            if (st) { free(x); free(xn); free(D); free(M); free(r); free(g); return st; }
+        } else {
+            or_transvecmul(A, r, g);
+        }
         for (int64_t j = 0; j < n; ++j) xn[j] = x[j] + omg * g[j] / D[j];
         apply_box(xn, n, upb, lwrb, ub, lb);
         memcpy(x, xn, sizeof(double) * n);

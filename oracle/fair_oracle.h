@@ -66,6 +66,8 @@ int or_add_white_noise(int64_t m, const double *b, double eta, double *bt, doubl
 double or_rowvecmult(const or_csr *A, int k, const double *v);
 void or_matvecmul(const or_csr *A, const double *v, double *w, int nthreads);
 void or_transvecmul(const or_csr *A, const double *v, double *w);
+/* The same on nthreads threads (per-thread copies added in thread order). */
+int or_transvecmul_mt(const or_csr *A, const double *v, double *w, int nthreads);
 int or_reorder(const or_csr *A, or_csr *B);
 void or_row_norms(const or_csr *A, int p, double *nrA, int nthreads);
 int or_column_norms(const or_csr *A, int p, double *ncA);
