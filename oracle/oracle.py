@@ -84,6 +84,7 @@ def _declare(L):
     L.or_rowvecmult.restype = d
     L.or_matvecmul.argtypes = [P(_CSR), vp, vp, i32]
     L.or_transvecmul.argtypes = [P(_CSR), vp, vp]
+    L.or_transvecmul_mt.argtypes = [P(_CSR), vp, vp, i32]
     L.or_reorder.argtypes = [P(_CSR), P(_CSR)]
     L.or_row_norms.argtypes = [P(_CSR), i32, vp, i32]
     L.or_column_norms.argtypes = [P(_CSR), i32, vp]
@@ -223,13 +224,18 @@ def matvecmul(A: OracleCSR, v, nthreads=1):
     return w
 
 
-def transvecmul(A: OracleCSR, v):
-    """MMCS (serial order), sparse_matrices.f90:370-393"""
+def transvecmul(A: OracleCSR, v, nthreads=1):
+    """MMCS, sparse_matrices.f90:370-393: the serial scatter order, or with
+    nthreads > 1 the race-free multi-threaded form (per-thread copies added
+    in thread order) used to time the reference's CPU path"""
     v = _f64(v)
     if v.size != A.m:
         raise OracleError(1)
     w = np.empty(A.n, np.float64)
-    lib().or_transvecmul(C.byref(A._c()), _p(v), _p(w))
+    if nthreads > 1:
+        _check(lib().or_transvecmul_mt(C.byref(A._c()), _p(v), _p(w), nthreads))
+    else:
+        lib().or_transvecmul(C.byref(A._c()), _p(v), _p(w))
     return w
 
 

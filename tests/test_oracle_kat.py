@@ -165,6 +165,14 @@ def test_operators_against_dense(oracle):
     assert np.allclose(oracle.row_norms(R, 1), np.abs(D).sum(1), rtol=1e-14)
     assert np.allclose(oracle.column_norms(R, 1), np.abs(D).sum(0), rtol=1e-14)
     assert abs(oracle.matvecmul(R, x) @ y - x @ oracle.transvecmul(R, y)) < 1e-10
+    # the multi-threaded forms used for the CPU baseline: the row-parallel product
+    # is exact per row; the transposed product differs from the serial order
+    # by rounding only, and is the same on every call for a thread count
+    assert np.array_equal(oracle.matvecmul(R, x, nthreads=4), oracle.matvecmul(R, x))
+    for t in (2, 3, 7):
+        w = oracle.transvecmul(R, y, nthreads=t)
+        assert np.allclose(w, oracle.transvecmul(R, y), rtol=1e-13, atol=1e-13)
+        assert np.array_equal(w, oracle.transvecmul(R, y, nthreads=t))
     k = 5
     assert abs(oracle.rowvecmult(R, k, x) - D[k - 1] @ x) < 1e-12
 
