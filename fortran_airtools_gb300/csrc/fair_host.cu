@@ -1296,6 +1296,18 @@ int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslot
     return FAIR_OK;
 }
 
+int fair_csr_tiled_info(fair_csr h, int32_t which, int32_t *shape) {
+    if (!h || !shape) return FAIR_ERR_NULL;
+    if (which != 0 && which != 1) { set_detail("which must be 0 (A) or 1 (A')"); return FAIR_ERR_ARG; }
+    const DevCSR &M = which == 0 ? h->A : h->AT;
+    const DevCSR::Tiled &t = M.tl;
+    const bool ok = t.built() && (which == 0 || h->at_valid);
+    const int32_t v[8] = {ok ? 1 : 0, ok ? t.T : 0, ok ? t.ntr : 0, ok ? t.NA : 0,
+                          ok ? t.nab : 0, ok ? t.W : 0, ok ? t.nunits : 0, ok ? t.kind : 0};
+    for (int i = 0; i < 8; ++i) shape[i] = v[i];
+    return FAIR_OK;
+}
+
 int fair_spmv_device(fair_csr h, int32_t trans, const void *d_x, void *d_y) {
     ENTER(h);
     NEED_MATRIX(h);

@@ -616,8 +616,11 @@ __device__ __forceinline__ void tl_unit(const TlArgs &P, const LD &ldr, const XT
             // chunks, in snake order (w in even groups, W - 1 - w in odd ones:
             // the chunks of a tile are sorted longest first, so the warps' sums
             // of lengths balance), as one stream of slots: the loads of the
-            // next chunk's first slots start during the current chunk (D = 2: a
-            // next chunk always has a slot, so the window never reaches past it)
+            // next chunks' first slots start during the current chunk. With 2
+            // slots in flight the window reaches at most one slot past the
+            // current chunk: into the next chunk, or, when that chunk has a
+            // single slot, into the first slot of the chunk after it (every
+            // chunk has at least one slot).
             static_assert(D == 2, "the continuous stream keeps 2 slots in flight");
             const int W = blockDim.x >> 5;
             struct Meta {
@@ -642,11 +645,15 @@ __device__ __forceinline__ void tl_unit(const TlArgs &P, const LD &ldr, const XT
             auto chunk_of = [&](int g) { return U.y + W * g + ((g & 1) ? W - 1 - wid : wid); };
             int g = 0, c = chunk_of(0);
             Meta cur = meta(c), nxt = meta(chunk_of(1));
-            // slot q of the stream that starts at chunk c (q < cur.len + nxt.len)
+            // slot q of the stream that starts at chunk c = chunk_of(g) (q <=
+            // cur.len + 1); the chunk after nxt is looked up only when the
+            // window reaches it (a 1-slot nxt: the tiles' shortest segments)
             auto fetch = [&](int q) {
-                return q < cur.len ? ldr.load(cur.s0 + 32 * (int64_t)q)
-                                   : (q - cur.len < nxt.len ? ldr.load(nxt.s0 + 32 * (int64_t)(q - cur.len))
-                                                            : LD::none());
+                if (q < cur.len) return ldr.load(cur.s0 + 32 * (int64_t)q);
+                q -= cur.len;
+                if (q < nxt.len) return ldr.load(nxt.s0 + 32 * (int64_t)q);
+                const int c2 = chunk_of(g + 2);
+                return q == nxt.len && c2 < U.z ? ldr.load(__ldg(P.soff + c2) + lane) : LD::none();
             };
             typename LD::Raw ring[2] = {fetch(0), fetch(1)};
             while (c < U.z) {

@@ -74,6 +74,18 @@ class CSRMatrix:
                 "stride": S.value, "low_bits": L.value, "sliced": bool(sl.value),
                 "nslots": ns.value}
 
+    def tiled_info(self, transposed: bool = False) -> dict:
+        """Tiled copy of A (or A') for the SIRT passes on layouts 9, 10, 14:
+        {'has', 'tile', 'tiles_per_side', 'angles_per_block', 'angle_blocks',
+        'window', 'units', 'kind'}."""
+        v = (C.c_int32 * 8)()
+        check(lib().fair_csr_tiled_info(self._h, 1 if transposed else 0, v))
+        keys = ("has", "tile", "tiles_per_side", "angles_per_block", "angle_blocks", "window",
+                "units", "kind")
+        d = dict(zip(keys, list(v)))
+        d["has"] = bool(d["has"])
+        return d
+
     def set_stream(self, cuda_stream_ptr: int | None):
         check(lib().fair_csr_set_stream(self._h, cuda_stream_ptr))
 

@@ -109,6 +109,14 @@ int fair_csr_packed_info(fair_csr h, int32_t which, int32_t *has, int64_t *ngrou
  * the padding of each chunk of 32 rows to its longest row). */
 int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslots);
 
+/* Shape of the tiled copy of A (which = 0) or A' (which = 1), built when a
+ * SIRT pass is set to layout 9, 10 or 14 or by the autotuner (no reference
+ * counterpart). shape receives 8 values: {built (0/1), tile side T, tiles per
+ * image side, angles per block NA, angle blocks, residual window W (bins per
+ * angle; A' only), work units, kind (0: tiles of A's image columns, 1: pixel
+ * tiles of A' times angle blocks)}; all zero when no copy is built. */
+int fair_csr_tiled_info(fair_csr h, int32_t which, int32_t *shape);
+
 /* Capacity, in doubles, of the fixed device array behind
  * fair_matvecmul_noalloc (32 MiB): n + m of the matrix must fit in it. */
 #define FAIR_NOALLOC_MAX_ENTRIES 4194304
@@ -121,8 +129,9 @@ int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslot
  * reference. The vectors are staged in one fixed device array of
  * FAIR_NOALLOC_MAX_ENTRIES doubles that every GPU loading the library holds
  * until exit; larger problems fail with FAIR_ERR_ARG. Computed in FP64 for
- * any handle precision. The first call on a device looks up the array's
- * address with that device current: make it before any stream capture.
+ * any handle precision. Every call looks up the array's address with the
+ * handle's device current; the first call on a device also loads it: make
+ * that call before any stream capture.
  * Calls share the array, so calls that overlap on the GPU race. */
 int fair_matvecmul_noalloc(fair_csr h, const double *v, int64_t size_v, double *w);
 

@@ -14,6 +14,7 @@
 #include "fair_oracle.h"
 
 #include <math.h>
+#include <stdatomic.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -256,34 +257,35 @@ int or_paralleltomo(int n, int nth, int p, const double *theta, or_csr *A) {
     return st;
 }
 
-/* paralleltomo with the rays split over threads (OpenMP): the same per-ray
- * code as or_paralleltomo, so the result is identical; used to build large
- * inputs for the CPU timing only. */
-int or_paralleltomo_mt(int n, int nth, int p, const double *theta, int nthreads, or_csr *A) {
-    memset(A, 0, sizeof(*A));
+/* The two-pass build of build_two_pass with the rays split over threads
+ * (OpenMP): the same per-ray code, so the result is identical; used to build
+ * the large parity and timing inputs. grid holds the n+1 grid lines (the same
+ * for x and y). */
+static int build_two_pass_mt(int n, int nth, int p, const double *grid, ray_param_fn fn,
+                             void *ctx, int nthreads, or_csr *A) {
     int64_t m = (int64_t)nth * p;
-    double *x0 = malloc(sizeof(double) * p), *y0 = malloc(sizeof(double) * p);
-    double d = p - 1;
-    or_linspace(-.5 * d, .5 * d, p, x0);
-    for (int j = 0; j < p; ++j) y0[j] = 0 * x0[j];
-    double *grid = malloc(sizeof(double) * (n + 1));
-    or_linspace(-.5 * n, .5 * n, n + 1, grid);
-    par_ctx ctx = {n, p, theta, x0, y0};
     A->IA = calloc((size_t)m + 1, sizeof(int64_t));
-    int64_t *cnt = calloc((size_t)m, sizeof(int64_t));
+    int64_t *cnt = calloc((size_t)(m ? m : 1), sizeof(int64_t));
+    if (!A->IA || !cnt) { free(cnt); return OR_ERR_ALLOC; }
     int st = OR_OK;
     if (nthreads < 1) nthreads = 1;
 #pragma omp parallel num_threads(nthreads)
     {
         ray_work w;
-        ray_work_alloc(&w, n);
-        memcpy(w.x + 1, grid, sizeof(double) * (n + 1));
-        memcpy(w.y + 1, grid, sizeof(double) * (n + 1));
+        int ok = ray_work_alloc(&w, n) == 0;
+        if (!ok) {
+#pragma omp atomic write
+            st = OR_ERR_ALLOC;
+        } else {
+            memcpy(w.x + 1, grid, sizeof(double) * (n + 1));
+            memcpy(w.y + 1, grid, sizeof(double) * (n + 1));
+        }
 #pragma omp for schedule(dynamic, 64)
         for (int64_t r = 0; r < m; ++r) {
+            if (!ok) continue;
             double a, b, x0th, y0th;
             int excl;
-            par_params(&ctx, (int)(r / p) + 1, (int)(r % p) + 1, &a, &b, &x0th, &y0th, &excl);
+            fn(ctx, (int)(r / p) + 1, (int)(r % p) + 1, &a, &b, &x0th, &y0th, &excl);
             int n_int = ray_points(&w, a, b, x0th, y0th);
             cnt[r] = ray_segments(&w, n_int, excl, NULL, NULL);
         }
@@ -293,12 +295,14 @@ int or_paralleltomo_mt(int n, int nth, int p, const double *theta, int nthreads,
             A->nnz = A->IA[m];
             A->vA = malloc(sizeof(double) * (size_t)(A->nnz ? A->nnz : 1));
             A->JA = malloc(sizeof(int32_t) * (size_t)(A->nnz ? A->nnz : 1));
+            if (!A->vA || !A->JA) st = OR_ERR_ALLOC;
         }
 #pragma omp for schedule(dynamic, 64)
         for (int64_t r = 0; r < m; ++r) {
+            if (!ok || st == OR_ERR_ALLOC) continue;
             double a, b, x0th, y0th;
             int excl;
-            par_params(&ctx, (int)(r / p) + 1, (int)(r % p) + 1, &a, &b, &x0th, &y0th, &excl);
+            fn(ctx, (int)(r / p) + 1, (int)(r % p) + 1, &a, &b, &x0th, &y0th, &excl);
             int n_int = ray_points(&w, a, b, x0th, y0th);
             int64_t c = ray_segments(&w, n_int, excl, A->JA + A->IA[r], A->vA + A->IA[r]);
             if (c < 0) {
@@ -306,11 +310,27 @@ int or_paralleltomo_mt(int n, int nth, int p, const double *theta, int nthreads,
                 st = OR_ERR_GEOMETRY;
             }
         }
-        ray_work_free(&w);
+        if (ok) ray_work_free(&w);
     }
     A->m = (int32_t)m;
     A->n = n * n;
-    free(cnt); free(x0); free(y0); free(grid);
+    free(cnt);
+    return st;
+}
+
+/* paralleltomo with the rays split over threads (identical result). */
+int or_paralleltomo_mt(int n, int nth, int p, const double *theta, int nthreads, or_csr *A) {
+    memset(A, 0, sizeof(*A));
+    double *x0 = malloc(sizeof(double) * p), *y0 = malloc(sizeof(double) * p);
+    double *grid = malloc(sizeof(double) * (n + 1));
+    if (!x0 || !y0 || !grid) { free(x0); free(y0); free(grid); return OR_ERR_ALLOC; }
+    double d = p - 1;
+    or_linspace(-.5 * d, .5 * d, p, x0);
+    for (int j = 0; j < p; ++j) y0[j] = 0 * x0[j];
+    or_linspace(-.5 * n, .5 * n, n + 1, grid);
+    par_ctx ctx = {n, p, theta, x0, y0};
+    int st = build_two_pass_mt(n, nth, p, grid, par_params, &ctx, nthreads, A);
+    free(x0); free(y0); free(grid);
     return st;
 }
 
@@ -332,20 +352,10 @@ static void fan_params(void *vctx, int i, int j, double *a, double *b,
     *excluded = 0;
 }
 
-/* geometry_fix = 0 reproduces the odd-p ray angles of :122 (offset .5 where
+/* Per-bin ray angles of fanlineartomo, system_generation.f90:114-130.
+ * geometry_fix = 0 reproduces the odd-p ray angles of :122 (offset .5 where
  * the even branch at :129 has .5*pi); geometry_fix = 1 uses .5*pi for both. */
-int or_fanlineartomo(int n, int nth, int p, double r, double dw, double sd,
-                     const double *theta, int geometry_fix, or_csr *A) {
-    memset(A, 0, sizeof(*A));
-    ray_work w;
-    if (ray_work_alloc(&w, n)) return OR_ERR_ALLOC;
-    double R = r * n, dwn = dw * n, sdn = sd * n;
-    double dew = dwn / p;
-    for (int i = 1; i <= n + 1; ++i) {
-        w.x[i] = i - .5 * n - 1.0;
-        w.y[i] = i - .5 * n - 1.0;
-    }
-    double *omega = malloc(sizeof(double) * p);
+static void fan_omega(int p, double dew, double sdn, int geometry_fix, double *omega) {
     if (p % 2 == 1) {
         int h = (p - 1) / 2;
         for (int i = 1; i <= h; ++i) {
@@ -362,10 +372,44 @@ int or_fanlineartomo(int n, int nth, int p, double r, double dw, double sd,
             omega[h + i - 1] = .5 * PI - atan(sdn / dep);
         }
     }
+}
+
+/* fanlineartomo, system_generation.f90:79-307 (grid lines i - n/2 - 1,
+ * :104-108; source at (0, R) rotated by theta, :146-157). */
+int or_fanlineartomo(int n, int nth, int p, double r, double dw, double sd,
+                     const double *theta, int geometry_fix, or_csr *A) {
+    memset(A, 0, sizeof(*A));
+    ray_work w;
+    if (ray_work_alloc(&w, n)) return OR_ERR_ALLOC;
+    double R = r * n, dwn = dw * n, sdn = sd * n;
+    double dew = dwn / p;
+    for (int i = 1; i <= n + 1; ++i) {
+        w.x[i] = i - .5 * n - 1.0;
+        w.y[i] = i - .5 * n - 1.0;
+    }
+    double *omega = malloc(sizeof(double) * p);
+    if (!omega) { ray_work_free(&w); return OR_ERR_ALLOC; }
+    fan_omega(p, dew, sdn, geometry_fix, omega);
     fan_ctx ctx = {R, 0.0, R, theta, omega};
     int st = build_two_pass(n, nth, p, &w, fan_params, &ctx, A);
     free(omega);
     ray_work_free(&w);
+    return st;
+}
+
+/* fanlineartomo with the rays split over threads (identical result). */
+int or_fanlineartomo_mt(int n, int nth, int p, double r, double dw, double sd,
+                        const double *theta, int geometry_fix, int nthreads, or_csr *A) {
+    memset(A, 0, sizeof(*A));
+    double R = r * n, dwn = dw * n, sdn = sd * n;
+    double dew = dwn / p;
+    double *grid = malloc(sizeof(double) * (n + 1)), *omega = malloc(sizeof(double) * p);
+    if (!grid || !omega) { free(grid); free(omega); return OR_ERR_ALLOC; }
+    for (int i = 1; i <= n + 1; ++i) grid[i - 1] = i - .5 * n - 1.0;
+    fan_omega(p, dew, sdn, geometry_fix, omega);
+    fan_ctx ctx = {R, 0.0, R, theta, omega};
+    int st = build_two_pass_mt(n, nth, p, grid, fan_params, &ctx, nthreads, A);
+    free(grid); free(omega);
     return st;
 }
 
@@ -433,6 +477,31 @@ void or_transvecmul(const or_csr *A, const double *v, double *w) {
         }
     }
 }
+
+/* The shipped OpenMP form of MMCS (sparse_matrices.f90:382-392): rows split
+ * statically over the threads, every thread scattering into the one shared w
+ * with no atomics, so concurrent updates of a column can be lost. The loads
+ * and stores are relaxed atomics: on the CPU they are the plain moves of the
+ * reference's loop and lose updates the same way, without making the program
+ * undefined. For timing the reference as shipped; its result differs from
+ * run to run. */
+void or_transvecmul_racy(const or_csr *A, const double *v, double *w, int nthreads) {
+    _Atomic double *aw = (_Atomic double *)w;
+    const int64_t n = A->n;
+    for (int64_t j = 0; j < n; ++j) atomic_store_explicit(&aw[j], 0.0, memory_order_relaxed);
+#pragma omp parallel for num_threads(nthreads > 1 ? nthreads : 1) schedule(static)
+    for (int64_t k = 0; k < (int64_t)A->m; ++k)
+        for (int64_t i = A->IA[k]; i < A->IA[k + 1]; ++i) {
+            int32_t c = A->JA[i] - 1;
+            double cur = atomic_load_explicit(&aw[c], memory_order_relaxed);
+            atomic_store_explicit(&aw[c], cur + v[k] * A->vA[i], memory_order_relaxed);
+        }
+}
+
+/* How or_sirt forms A'r when nthreads > 1: 0 race-free per-thread copies
+ * (default), 1 the shipped racy scatter. Serial when nthreads <= 1. */
+static int g_mmcs_mode = 0;
+void or_set_mmcs_mode(int mode) { g_mmcs_mode = mode; }
 
 /* The same product on nthreads threads, for timing the reference's CPU path:
  * the reference runs this scatter under OpenMP into one shared vector (a data
@@ -605,7 +674,9 @@ int or_sirt(const char *method, const or_csr *A, const double *b, int maxits,
     for (int it = 1; it <= maxits; ++it) {
         or_matvecmul(A, x, r, nthreads);
         for (int64_t i = 0; i < m; ++i) r[i] = (b[i] - r[i]) / M[i];
-        if (nthreads > 1) {
+        if (nthreads > 1 && g_mmcs_mode == 1) {
+            or_transvecmul_racy(A, r, g, nthreads);
+        } else if (nthreads > 1) {
             int st = or_transvecmul_mt(A, r, g, nthreads);
             if (st) { free(x); free(xn); free(D); free(M); free(r); free(g); return st; }
         } else {

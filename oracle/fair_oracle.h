@@ -59,6 +59,9 @@ int or_paralleltomo(int n, int nth, int p, const double *theta, or_csr *A);
 int or_paralleltomo_mt(int n, int nth, int p, const double *theta, int nthreads, or_csr *A);
 int or_fanlineartomo(int n, int nth, int p, double r, double dw, double sd,
                      const double *theta, int geometry_fix, or_csr *A);
+/* The same with the rays split over nthreads threads (identical result). */
+int or_fanlineartomo_mt(int n, int nth, int p, double r, double dw, double sd,
+                        const double *theta, int geometry_fix, int nthreads, or_csr *A);
 void or_csr_free(or_csr *A);
 int or_add_white_noise(int64_t m, const double *b, double eta, double *bt, double *e);
 
@@ -68,6 +71,11 @@ void or_matvecmul(const or_csr *A, const double *v, double *w, int nthreads);
 void or_transvecmul(const or_csr *A, const double *v, double *w);
 /* The same on nthreads threads (per-thread copies added in thread order). */
 int or_transvecmul_mt(const or_csr *A, const double *v, double *w, int nthreads);
+/* The shipped OpenMP scatter into one shared vector (racy: updates can be
+ * lost; for timing the reference as shipped). */
+void or_transvecmul_racy(const or_csr *A, const double *v, double *w, int nthreads);
+/* or_sirt's threaded transposed product: 0 race-free copies, 1 the racy scatter. */
+void or_set_mmcs_mode(int mode);
 int or_reorder(const or_csr *A, or_csr *B);
 void or_row_norms(const or_csr *A, int p, double *nrA, int nthreads);
 int or_column_norms(const or_csr *A, int p, double *ncA);

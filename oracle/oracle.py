@@ -78,6 +78,7 @@ def _declare(L):
     L.or_paralleltomo.argtypes = [i32, i32, i32, vp, P(_CSR)]
     L.or_paralleltomo_mt.argtypes = [i32, i32, i32, vp, i32, P(_CSR)]
     L.or_fanlineartomo.argtypes = [i32, i32, i32, d, d, d, vp, i32, P(_CSR)]
+    L.or_fanlineartomo_mt.argtypes = [i32, i32, i32, d, d, d, vp, i32, i32, P(_CSR)]
     L.or_csr_free.argtypes = [P(_CSR)]
     L.or_add_white_noise.argtypes = [i64, vp, d, vp, vp]
     L.or_rowvecmult.argtypes = [P(_CSR), i32, vp]
@@ -85,6 +86,8 @@ def _declare(L):
     L.or_matvecmul.argtypes = [P(_CSR), vp, vp, i32]
     L.or_transvecmul.argtypes = [P(_CSR), vp, vp]
     L.or_transvecmul_mt.argtypes = [P(_CSR), vp, vp, i32]
+    L.or_transvecmul_racy.argtypes = [P(_CSR), vp, vp, i32]
+    L.or_set_mmcs_mode.argtypes = [i32]
     L.or_reorder.argtypes = [P(_CSR), P(_CSR)]
     L.or_row_norms.argtypes = [P(_CSR), i32, vp, i32]
     L.or_column_norms.argtypes = [P(_CSR), i32, vp]
@@ -200,6 +203,15 @@ def fanlineartomo(n, nth, p, r, dw, sd, theta, geometry_fix=False) -> OracleCSR:
     return _take(s)
 
 
+def fanlineartomo_mt(n, nth, p, r, dw, sd, theta, nthreads, geometry_fix=False) -> OracleCSR:
+    """fanlineartomo with rays split over threads (identical result)"""
+    th = _f64(theta)
+    s = _CSR()
+    _check(lib().or_fanlineartomo_mt(n, nth, p, r, dw, sd, _p(th), int(geometry_fix), nthreads,
+                                     C.byref(s)))
+    return _take(s)
+
+
 def add_white_noise(b, eta):
     """system_generation.f90:709-745; returns (bt, e)"""
     b = _f64(b)
@@ -237,6 +249,23 @@ def transvecmul(A: OracleCSR, v, nthreads=1):
     else:
         lib().or_transvecmul(C.byref(A._c()), _p(v), _p(w))
     return w
+
+
+def transvecmul_racy(A: OracleCSR, v, nthreads):
+    """MMCS as shipped under OpenMP (sparse_matrices.f90:382-392): every thread
+    scatters into one shared vector, so updates can be lost; for timing only"""
+    v = _f64(v)
+    if v.size != A.m:
+        raise OracleError(1)
+    w = np.empty(A.n, np.float64)
+    lib().or_transvecmul_racy(C.byref(A._c()), _p(v), _p(w), nthreads)
+    return w
+
+
+def set_mmcs_mode(mode: str):
+    """The threaded transposed product of sirt(..., nthreads > 1): 'racefree'
+    (per-thread copies, default) or 'racy' (the shipped shared scatter)"""
+    lib().or_set_mmcs_mode({"racefree": 0, "racy": 1}[mode])
 
 
 def reorder(A: OracleCSR) -> OracleCSR:

@@ -10,7 +10,10 @@ forms within 2e-6. Images of 3 x 3 tiles with partial edge tiles, a single
 partial tile, a square matrix whose rows jump between tiles (its step
 records and the delta copy of its transpose are refused: too many steps
 outside the codes), and a matrix whose columns are not a square image (no
-tiled copy: the pass falls back to the row layouts)."""
+tiled copy: the pass falls back to the row layouts). Many angles (720) make
+every tile hold thousands of chunks, so each warp streams several chunks per
+work unit and the tiles' shortest segments form chunks of a single slot,
+which the stream's lookahead must cross (a missed slot drops entries)."""
 import ctypes as C
 
 import numpy as np
@@ -114,3 +117,24 @@ def test_tiled_needs_a_square_image(fair, oracle):
     x = run(fair, A, b, "f32", (8, 8, 9, 1), "cimmino", 10, fair.airms.options())
     assert rel_err(x, oracle.sirt("cimmino", R, b, 10)) < 1e-5
     A.close()
+
+
+@pytest.fixture(scope="module")
+def par200(fair, oracle):
+    n, nth, p = 200, 720, 284
+    th = np.pi * np.arange(nth) / nth
+    A = fair.paralleltomo(fair.Data(n=n, p=p, nth=nth, theta=th))
+    R = oracle.paralleltomo_mt(n, nth, p, th, 8)
+    b = oracle.matvecmul(R, fair.phantomgallery.gaussians(n, 20, seed=1))
+    yield A, R, b
+    A.close()
+
+
+@pytest.mark.parametrize("prec,codes", [("f64", (9, 0)), ("f64", (9, 9)), ("f32", (9, 14)),
+                                        ("q16", (14, 14)), ("f16", (14, 0))])
+def test_tiled_many_chunks_per_unit(par200, fair, oracle, prec, codes):
+    A, R, b = par200
+    xt = run(fair, A, b, prec, (8, 8) + codes, "cimmino", 5, fair.airms.options())
+    xc = run(fair, A, b, prec, (8, 8, 0, 0), "cimmino", 5, fair.airms.options())
+    assert rel_err(xt, xc) < TOL_SAME[prec]
+    assert rel_err(xt, oracle.sirt("cimmino", R, b, 5, nthreads=8)) < (1e-10 if prec == "f64" else 1e-5)

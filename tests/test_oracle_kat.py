@@ -143,6 +143,38 @@ def test_fan_odd_p_angle_offset(oracle):
     assert not mirror_ok(oracle.fanlineartomo(N, 1, p, 2.0, 1.0, 2.0, th, geometry_fix=False))
 
 
+@pytest.mark.parametrize("threads", [2, 5])
+def test_threaded_builders_equal_serial(oracle, threads):
+    """The multi-threaded builds (used for the large parity inputs) run the
+    same per-ray code: identical IA, JA and vA, odd and even p, with and
+    without the odd-p angle fix, and a grid-line (NaN-key) parallel case."""
+    def same(A, B):
+        return (np.array_equal(A.IA, B.IA) and np.array_equal(A.JA, B.JA)
+                and np.array_equal(A.vA, B.vA))
+
+    th = 2 * np.pi * np.arange(90) / 90
+    for p, fix in ((73, False), (73, True), (74, False)):
+        assert same(oracle.fanlineartomo(48, 90, p, 2.0, p / 48, 2.0, th, geometry_fix=fix),
+                    oracle.fanlineartomo_mt(48, 90, p, 2.0, p / 48, 2.0, th, threads,
+                                            geometry_fix=fix))
+    th = np.concatenate([[0.0, np.pi / 4, np.pi / 2 - 1e-3], np.pi * np.arange(3, 37) / 37])
+    for p in (47, 48, 31):
+        assert same(oracle.paralleltomo(32, th.size, p, th),
+                    oracle.paralleltomo_mt(32, th.size, p, th, threads))
+
+
+def test_racy_transposed_product(oracle):
+    """The shipped scatter (sparse_matrices.f90:382-392) on one thread is the
+    serial product; on several threads it may lose updates, never add any."""
+    th = np.pi * np.arange(60) / 60
+    R = oracle.paralleltomo(48, 60, 70, th)
+    y = np.random.default_rng(3).random(R.m)
+    ref = oracle.transvecmul(R, y)
+    assert np.array_equal(oracle.transvecmul_racy(R, y, 1), ref)
+    w = oracle.transvecmul_racy(R, y, 4)
+    assert np.all(w <= ref * (1 + 1e-12) + 1e-12)  # positive terms: lost updates only lower w
+
+
 def test_reorder_is_stable_transpose(oracle):
     N, nth, p = 16, 10, 24
     R = oracle.paralleltomo(N, nth, p, oracle.linspace(0, np.pi, nth))
