@@ -86,6 +86,10 @@ def max_over_ranks(v, world, device):
     return float(t.item())
 
 
+def sm_count(torch, device):
+    return torch.cuda.get_device_properties(device).multi_processor_count
+
+
 def hbm_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -193,11 +197,22 @@ def traffic_from_profiles(kernel, prec, nnz):
 
 
 # --------------------------------------------------------------- CPU timing ----
-def cpu_sirt_rate(O, R, b, budget_s, nthreads, steps=None, warmup=0):
+def workload_config(m, n, nnz):
+    """The `config` of both arms (the same keys and values for the same workload)."""
+    return {"workload": WORKLOAD, "n": N, "angles": NTH, "bins": P, "m": m, "ncols": n,
+            "nnz": nnz, "method": "cimmino", "precision": "f64",
+            "l2": "inputs larger than L2 (FP64 matrix %.1f GB per pass)" % (nnz * 12 / 1e9)}
+
+
+def cpu_sirt_rate(O, R, b, budget_s, nthreads, steps=None, warmup=0, mode="racefree"):
     """Time the oracle's SIRT iteration (Cimmino) on a contiguous block of
     angles of R sized to `budget_s`; returns (iterations/s of the full
-    problem, description, seconds per sample step)."""
+    problem, description, seconds per sample step). `mode` is the threaded
+    transposed product: 'racefree' (per-thread copies added in thread order)
+    or 'racy' (the reference's shared scatter, sparse_matrices.f90:382-392)."""
     m, p = R.m, P
+    O.set_mmcs_mode(mode)
+
     # trial on ~1% of the angles to size the sample
     def sub(nang):
         r1 = nang * p
@@ -206,25 +221,51 @@ def cpu_sirt_rate(O, R, b, budget_s, nthreads, steps=None, warmup=0):
         S = O.OracleCSR(r1, R.n, IA, R.JA[:nz], R.vA[:nz])
         return S, b[:r1], nz
 
-    S, bs, nz = sub(max(1, NTH // 100))
-    t0 = time.perf_counter(); O.sirt("cimmino", S, bs, 0, nthreads=nthreads)
-    t1 = time.perf_counter(); O.sirt("cimmino", S, bs, 1, nthreads=nthreads)
-    t2 = time.perf_counter()
-    per_nnz = max((t2 - t1) - (t1 - t0), 1e-9) / max(nz, 1)
-    k = steps if steps else 3
-    nang = int(min(NTH, max(1, budget_s / (per_nnz * R.nnz / NTH) / (k + warmup))))
-    S, bs, nz = sub(nang)
-    if warmup:
-        O.sirt("cimmino", S, bs, warmup, nthreads=nthreads)
-    t0 = time.perf_counter(); O.sirt("cimmino", S, bs, 0, nthreads=nthreads)
-    t1 = time.perf_counter(); O.sirt("cimmino", S, bs, k, nthreads=nthreads)
-    t2 = time.perf_counter()
+    try:
+        S, bs, nz = sub(max(1, NTH // 100))
+        t0 = time.perf_counter(); O.sirt("cimmino", S, bs, 0, nthreads=nthreads)
+        t1 = time.perf_counter(); O.sirt("cimmino", S, bs, 1, nthreads=nthreads)
+        t2 = time.perf_counter()
+        per_nnz = max((t2 - t1) - (t1 - t0), 1e-9) / max(nz, 1)
+        k = steps if steps else 3
+        nang = int(min(NTH, max(1, budget_s / (per_nnz * R.nnz / NTH) / (k + warmup))))
+        S, bs, nz = sub(nang)
+        if warmup:
+            O.sirt("cimmino", S, bs, warmup, nthreads=nthreads)
+        t0 = time.perf_counter(); O.sirt("cimmino", S, bs, 0, nthreads=nthreads)
+        t1 = time.perf_counter(); O.sirt("cimmino", S, bs, k, nthreads=nthreads)
+        t2 = time.perf_counter()
+    finally:
+        O.set_mmcs_mode("racefree")
     step = ((t2 - t1) - (t1 - t0)) / k
     frac = nz / R.nnz
     rate = frac / step
     desc = (f"SIRT (Cimmino) iteration restricted to the first {nang} of {NTH} angles "
             f"({frac:.3f} of the nonzeros), {k} iterations, scaled to full iterations")
     return rate, desc, step
+
+
+def cpu_variants(O, R, b, budget_s, nthreads):
+    """The reference's CPU iteration three ways on the machine's host cores: the
+    row-parallel product with the transposed product on all threads made
+    race-free (the headline CPU figure: the fastest correct form), the same
+    with the transposed product as the reference ships it (a shared scatter
+    with no atomics: racy, updates are lost; its error is one full-size
+    product against the serial one), and everything on one thread."""
+    out = {}
+    r, d, _ = cpu_sirt_rate(O, R, b, budget_s, nthreads)
+    out["racefree_all_threads"] = {"value": r, "unit": "iter/s", "cores": nthreads, "sample": d}
+    r, d, _ = cpu_sirt_rate(O, R, b, budget_s, nthreads, mode="racy")
+    y = np.random.default_rng(7).random(R.m)
+    w_serial = O.transvecmul(R, y)
+    w_racy = O.transvecmul_racy(R, y, nthreads)
+    err = float(np.linalg.norm(w_racy - w_serial) / np.linalg.norm(w_serial))
+    out["racy_all_threads"] = {"value": r, "unit": "iter/s", "cores": nthreads, "sample": d,
+                               "label": "racy: the shipped shared scatter of MMCS",
+                               "rel_err_one_product_vs_serial": err}
+    r, d, _ = cpu_sirt_rate(O, R, b, budget_s, 1)
+    out["one_thread"] = {"value": r, "unit": "iter/s", "cores": 1, "sample": d}
+    return out
 
 
 def run_reference(args):
@@ -242,13 +283,18 @@ def run_reference(args):
     budget = float(os.environ.get("FAIR_REF_BUDGET_S", "60"))
     rate, desc, step = cpu_sirt_rate(O, R, bt, budget, nthreads, steps=args.steps,
                                      warmup=args.warmup)
+    variants = None
+    if not args.no_cpu:
+        variants = cpu_variants(O, R, bt, float(os.environ.get("FAIR_CPU_BUDGET_S", "8")),
+                                nthreads)
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "iter/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "n": N, "angles": NTH, "bins": P, "nnz": R.nnz},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded 20-Gaussian phantom, 1% noise)",
+            "config": workload_config(R.m, R.n, R.nnz),
             "cpu_baseline": {"value": rate, "unit": "iter/s", "cores": nthreads, "kind": "port",
-                             "sample": desc},
+                             "sample": desc + "; transposed product race-free on all threads",
+                             "variants": variants},
             "e2e": {"value": rate, "unit": "iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -289,6 +335,8 @@ def run_ours(args):
 
     forms = {}
     results = {}
+    results_or = {}  # the iterate after k_or iterations, compared with the oracle's
+    k_or = max(1, min(args.steps, 20))
     packed = {}
     form_list = ["f64"] + [f for f in args.forms.split(",") if f and f != "f64"]
     if args.prec not in form_list:
@@ -322,6 +370,14 @@ def run_ours(args):
         clocks = sampler.stop() if sampler else None
         ms = max_over_ranks(e0.elapsed_time(e1), world, f"cuda:{local}")
         results[prec] = d_x.cpu().numpy()
+        if k_or == args.steps:
+            results_or[prec] = results[prec]
+        else:  # outside the timed region
+            with torch.cuda.stream(stream):
+                d_x.zero_()
+            check(L.fair_sirt_run_device(h, d_b.data_ptr(), d_x.data_ptr(), k_or))
+            stream.synchronize()
+            results_or[prec] = d_x.cpu().numpy()
         # per-pass launch durations (CUDA events around each kernel)
         ms1, ms2 = C.c_float(), C.c_float()
         with torch.cuda.stream(stream):
@@ -368,6 +424,15 @@ def run_ours(args):
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    fp64_pipe = None
+    if hp == "f64":
+        # the FP64 form is bound by the FP64 pipe: one multiply-add per nonzero
+        # against 2 FP64 lanes per clock per SM at the sampled SM clock
+        mhz = (head.get("clocks") or {}).get("sm_mhz") or 2070.0
+        dpeak = 2 * sm_count(torch, local) * mhz * 1e6
+        fp64_pipe = {"achieved_dfma_per_s": nnz / (dom_ms / 1e3), "peak_dfma_per_s": dpeak,
+                     "frac": nnz / (dom_ms / 1e3) / dpeak,
+                     "peak_basis": "2 FP64 lanes/clock/SM x SMs x median sampled SM clock"}
     traffic = traffic_from_profiles(kname, hp, nnz)
     for prec in forms:
         p1, p2 = algorithmic_bytes(nnz, m, n, prec, packed.get(prec), pass_codes(prec))
@@ -383,16 +448,38 @@ def run_ours(args):
     F.airms.sirt("cimmino", A, bt, args.steps, opts=opts)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, f"cuda:{local}")
 
+    # the oracle (outside every timed region): its own matrix, compared with
+    # the GPU's, and its FP64 iterate after k_or iterations, against which
+    # every form's iterate is reported
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    oracle_check = None
+    if rank == 0 and world == 1 and not args.no_oracle:
         from oracle import oracle as O
-        vA, IA, JA = A.arrays()
-        R = O.OracleCSR(m, n, IA, JA, vA)
         nthreads = os.cpu_count() or 1
-        rate, desc, _ = cpu_sirt_rate(O, R, bt, float(os.environ.get("FAIR_CPU_BUDGET_S", "15")),
-                                      nthreads)
-        cpu = {"value": rate, "unit": "iter/s", "cores": nthreads, "kind": "port", "sample": desc}
-        del R, vA, IA, JA
+        t0 = time.perf_counter()
+        R = O.paralleltomo_mt(N, NTH, P, th, nthreads)
+        ob_s = time.perf_counter() - t0
+        vA, IA, JA = A.arrays()
+        same = bool(np.array_equal(IA, R.IA) and np.array_equal(JA, R.JA))
+        vrel = (float(np.max(np.abs(vA - R.vA) / np.maximum(np.abs(R.vA), 1e-300)))
+                if same and R.nnz else None)
+        del vA, IA, JA
+        xo = O.sirt("cimmino", R, bt, k_or, nthreads=nthreads)
+        no = np.linalg.norm(xo)
+        for prec in forms:
+            forms[prec]["rel_err_vs_oracle"] = float(np.linalg.norm(results_or[prec] - xo) / no)
+            forms[prec]["oracle_iterations"] = k_or
+        oracle_check = {"matrix_ia_ja_equal": same, "matrix_va_max_rel_diff": vrel,
+                        "iterations": k_or, "oracle_build_s": ob_s, "threads": nthreads,
+                        "note": "oracle FP64 Cimmino iterate after `iterations` steps from x = 0, "
+                                "on the oracle's own matrix, vs each form's GPU iterate"}
+        if not args.no_cpu:
+            var = cpu_variants(O, R, bt, float(os.environ.get("FAIR_CPU_BUDGET_S", "8")), nthreads)
+            head_cpu = var["racefree_all_threads"]
+            cpu = {"value": head_cpu["value"], "unit": "iter/s", "cores": nthreads, "kind": "port",
+                   "sample": head_cpu["sample"] + "; transposed product race-free on all threads",
+                   "variants": var}
+        del R
 
     if rank == 0:
         line = {
@@ -400,16 +487,16 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": hp, "data": "synthetic (seeded 20-Gaussian phantom, 1% noise)",
-            "config": {"workload": WORKLOAD, "n": N, "angles": NTH, "bins": P, "m": m,
-                       "ncols": n, "nnz": nnz, "method": "cimmino", "precision": hp,
-                       "l2": "inputs larger than L2 (matrix %.1f GB per pass)"
-                             % ((nnz * (VAL_BYTES[hp] + 4)) / 1e9),
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "geometry_build_s": build_s},
+            "config": workload_config(m, n, nnz),
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "geometry_build_s": build_s,
+            "oracle_check": oracle_check,
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "algorithmic_bytes_per_launch": dom_bytes,
-                         "traffic": traffic},
+                         "traffic": traffic,
+                         "limiter": "fp64 pipe" if fp64_pipe else "hbm / load latency",
+                         "fp64_pipe": fp64_pipe},
             "forms": forms,
             "e2e": {"value": world * args.steps / e2e_s, "unit": "iter/s",
                     "h2d_bytes_per_step": 8 * m / args.steps,
@@ -769,6 +856,8 @@ def main():
     ap.add_argument("--forms", default="f32,f16,q16",
                     help="reduced forms timed after FP64 (comma list of f32, f16, q16)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
+    ap.add_argument("--no-oracle", action="store_true",
+                    help="skip the oracle check (its matrix and iterate) and the CPU baseline")
     ap.add_argument("--n", type=int, default=1024, help="image size N (profiling cases)")
     ap.add_argument("--angles", type=int, default=720)
     ap.add_argument("--bins", type=int, default=1448)

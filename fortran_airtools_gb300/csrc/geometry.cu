@@ -361,6 +361,66 @@ constexpr int kExactBatch = 2048;  // special rays traced per launch (scratch bo
 
 }  // namespace
 
+namespace {
+// The count pass (k_geom_count, then the exact path for the rays whose keys
+// need the quicksort replay): entries per ray into counts [m]; the special
+// rays, their number and the exact path's scratch stay for the fill.
+struct GeomCount {
+    DevBuf counts, special, nsp, scr_d, scr_i;
+    int32_t h_nsp = 0, batch = 0;
+    int blocks = 1;
+    static constexpr int threads = 128;
+    void release() {
+        counts.release(); special.release(); nsp.release(); scr_d.release(); scr_i.release();
+    }
+};
+
+int geometry_count(const GeomTables &T, const GeomDev &G, GeomCount &C, cudaStream_t s) {
+    const int64_t m = (int64_t)T.nth * T.p;
+    FAIR_TRY(C.counts.grow(sizeof(int32_t) * (m > 0 ? m : 1)));
+    FAIR_TRY(C.special.grow(sizeof(int32_t) * (m > 0 ? m : 1)));
+    FAIR_TRY(C.nsp.grow(sizeof(int32_t)));
+    FAIR_CUDA(cudaMemsetAsync(C.nsp.p, 0, sizeof(int32_t), s));
+    int64_t blocks64 = (m + C.threads - 1) / C.threads;
+    C.blocks = (int)(blocks64 < (int64_t)sm_count() * 64 ? (blocks64 > 0 ? blocks64 : 1)
+                                                         : (int64_t)sm_count() * 64);
+    k_geom_count<<<C.blocks, C.threads, 0, s>>>(G, C.counts.as<int32_t>(), C.special.as<int32_t>(),
+                                                C.nsp.as<int32_t>());
+    FAIR_CUDA(cudaGetLastError());
+    FAIR_CUDA(cudaMemcpyAsync(&C.h_nsp, C.nsp.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    // Scratch for the exact path: keys, two coordinate arrays, permutation.
+    const int nt = 2 * T.N + 2;
+    C.batch = C.h_nsp < kExactBatch ? C.h_nsp : kExactBatch;
+    if (C.h_nsp > 0) {
+        FAIR_TRY(C.scr_d.grow(sizeof(double) * 3 * (size_t)nt * C.batch));
+        FAIR_TRY(C.scr_i.grow(sizeof(int32_t) * (size_t)nt * C.batch));
+        for (int32_t q0 = 0; q0 < C.h_nsp; q0 += C.batch) {
+            int32_t nq = C.h_nsp - q0 < C.batch ? C.h_nsp - q0 : C.batch;
+            k_geom_count_exact<<<(nq + 63) / 64, 64, 0, s>>>(G, C.special.as<int32_t>() + q0, nq,
+                                                            C.scr_d.as<double>(),
+                                                            C.scr_i.as<int32_t>(),
+                                                            C.counts.as<int32_t>());
+            FAIR_CUDA(cudaGetLastError());
+        }
+    }
+    return FAIR_OK;
+}
+}  // namespace
+
+int geometry_nnz(const GeomTables &T, int64_t *nnz, cudaStream_t s) {
+    const int64_t m = (int64_t)T.nth * T.p;
+    GeomDev G = to_dev(T);
+    GeomCount C;
+    FAIR_TRY(geometry_count(T, G, C, s));
+    DevBuf rp;
+    FAIR_TRY(rp.grow(sizeof(int64_t) * (m + 1)));
+    FAIR_TRY(scan_counts(C.counts.as<int32_t>(), m, rp.as<int64_t>(), s));
+    FAIR_CUDA(cudaMemcpyAsync(nnz, rp.as<int64_t>() + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    return FAIR_OK;
+}
+
 int build_geometry(const GeomTables &T, DevCSR &A, cudaStream_t s) {
     const int64_t m = (int64_t)T.nth * T.p;
     const int32_t ncols = T.N * T.N;
@@ -371,41 +431,14 @@ int build_geometry(const GeomTables &T, DevCSR &A, cudaStream_t s) {
     A.stride_hint = T.N;   // pixel (x, y) is column x*N + (N - y)
     A.tstride_hint = T.p;  // ray (angle i, bin j) is row i*p + j
 
-    DevBuf counts, special, nsp, err;
-    FAIR_TRY(counts.grow(sizeof(int32_t) * (m > 0 ? m : 1)));
-    FAIR_TRY(special.grow(sizeof(int32_t) * (m > 0 ? m : 1)));
-    FAIR_TRY(nsp.grow(sizeof(int32_t)));
+    GeomCount C;
+    FAIR_TRY(geometry_count(T, G, C, s));
+    DevBuf err;
     FAIR_TRY(err.grow(sizeof(int)));
-    FAIR_CUDA(cudaMemsetAsync(nsp.p, 0, sizeof(int32_t), s));
     FAIR_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-
-    const int threads = 128;
-    int64_t blocks64 = (m + threads - 1) / threads;
-    int blocks = (int)(blocks64 < (int64_t)sm_count() * 64 ? (blocks64 > 0 ? blocks64 : 1)
-                                                          : (int64_t)sm_count() * 64);
-    k_geom_count<<<blocks, threads, 0, s>>>(G, counts.as<int32_t>(), special.as<int32_t>(),
-                                            nsp.as<int32_t>());
-    FAIR_CUDA(cudaGetLastError());
-    int32_t h_nsp = 0;
-    FAIR_CUDA(cudaMemcpyAsync(&h_nsp, nsp.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    FAIR_CUDA(cudaStreamSynchronize(s));
-
-    // Scratch for the exact path: keys, two coordinate arrays, permutation.
-    const int nt = 2 * T.N + 2;
-    DevBuf scr_d, scr_i;
-    int32_t batch = h_nsp < kExactBatch ? h_nsp : kExactBatch;
-    if (h_nsp > 0) {
-        FAIR_TRY(scr_d.grow(sizeof(double) * 3 * (size_t)nt * batch));
-        FAIR_TRY(scr_i.grow(sizeof(int32_t) * (size_t)nt * batch));
-        for (int32_t q0 = 0; q0 < h_nsp; q0 += batch) {
-            int32_t nq = h_nsp - q0 < batch ? h_nsp - q0 : batch;
-            k_geom_count_exact<<<(nq + 63) / 64, 64, 0, s>>>(G, special.as<int32_t>() + q0, nq,
-                                                            scr_d.as<double>(),
-                                                            scr_i.as<int32_t>(),
-                                                            counts.as<int32_t>());
-            FAIR_CUDA(cudaGetLastError());
-        }
-    }
+    DevBuf &counts = C.counts, &special = C.special, &scr_d = C.scr_d, &scr_i = C.scr_i;
+    const int32_t h_nsp = C.h_nsp, batch = C.batch;
+    const int blocks = C.blocks, threads = C.threads;
 
     FAIR_TRY(A.rowptr.grow(sizeof(int64_t) * (m + 1)));
     FAIR_TRY(scan_counts(counts.as<int32_t>(), m, A.rowptr.as<int64_t>(), s));
@@ -429,8 +462,8 @@ int build_geometry(const GeomTables &T, DevCSR &A, cudaStream_t s) {
     int h_err = 0;
     FAIR_CUDA(cudaMemcpyAsync(&h_err, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     FAIR_CUDA(cudaStreamSynchronize(s));
-    counts.release(); special.release(); nsp.release(); err.release();
-    scr_d.release(); scr_i.release();
+    C.release();
+    err.release();
     if (h_err) {
         set_detail(h_err & 1 ? "column index outside 1..N^2 while tracing a ray"
                              : "fill pass wrote a different count than the count pass");

@@ -142,8 +142,11 @@ __device__ __forceinline__ long long fx_warp_sum(long long F) {  // |F| < 2^55 p
     const int l2 = __reduce_add_sync(0xffffffffu, (int)(F >> 52));
     return (long long)l2 * (1LL << 52) + (long long)l1 * (1LL << 26) + (long long)l0;
 }
-// total * 2^(E - 1075) rounded to nearest even; ldexp when the result leaves
-// the normal range
+// total * 2^(E - 1075) rounded to nearest even, once. Below the normal range
+// the value is exact: the frame's unit 2^(E - 1075) (E >= 1) is a multiple of
+// the smallest subnormal 2^-1074, and such a total has fewer than 53 - E + 1
+// bits, so it is the subnormal significand shifted by E - 1. Above it the
+// rounded value overflows to infinity.
 __device__ __forceinline__ double fx_to_double(long long total, int E) {
     if (total == 0) return 0.0;
     const bool neg = total < 0;
@@ -163,8 +166,10 @@ __device__ __forceinline__ double fx_to_double(long long total, int E) {
         }
     }
     const int field = nb + E - 53;
-    if (field < 1 || field > 2046) return ldexp((double)total, E - 1075);
-    unsigned long long bits = ((unsigned long long)field << 52) | (mant & 0xFFFFFFFFFFFFFull);
+    unsigned long long bits;
+    if (field < 1) bits = a << (E - 1);  // nb <= 53 - E here: no rounding above, < 2^52
+    else if (field > 2046) bits = 0x7FF0000000000000ull;
+    else bits = ((unsigned long long)field << 52) | (mant & 0xFFFFFFFFFFFFFull);
     if (neg) bits |= 1ull << 63;
     return __longlong_as_double((long long)bits);
 }

@@ -16,17 +16,17 @@
 //   * n + m must not exceed FAIR_NOALLOC_MAX_ENTRIES (4,194,304 doubles,
 //     32 MiB); larger problems are rejected with FAIR_ERR_ARG.
 //   * The product is computed in FP64 whatever precision the handle is set to.
-//   * The first call on a device looks up the arrays' device addresses
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//   * Every call looks up the arrays' device addresses (cudaGetSymbolAddress)
+//     with the handle's device current, so an address is never reused after
+//     the device's context was reset and the module loaded again; the first
+//     call on a device also loads the arrays, so make it before any stream
+//     capture.
 //   * Every call shares the arrays and leaves its vectors in them: two calls
 //     whose work overlaps on the GPU (different streams or handles at once)
 //     race and corrupt each other's results. The counters are cleared by
 //     every call before the product runs.
 //   * Nothing here calls cudaMalloc, cudaFree or an allocating library routine;
 //     the matrix itself must already be on the GPU (built or uploaded earlier).
-#include <mutex>
-
 #include "fair_gpu_ext.h"
 #include "fair_internal.cuh"
 
@@ -37,33 +37,19 @@ __device__ __align__(256) double g_noalloc_vectors[FAIR_NOALLOC_MAX_ENTRIES];
 __device__ __align__(256) unsigned g_noalloc_sched[4];
 
 struct NoAllocAddrs {
-    bool ready = false;
     double *vectors = nullptr;
     unsigned *sched = nullptr;
 };
 
-std::mutex g_addr_mu;
-NoAllocAddrs g_addrs[128];
-
-// Device addresses of the two arrays on the current device (looked up once).
+// Device addresses of the two arrays on the current device, looked up on every
+// call (a cheap host query; a cached address would go stale after a context
+// reset reloads the module).
 int noalloc_addresses(NoAllocAddrs &out) {
-    int dev = 0;
-    FAIR_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 128) {
-        set_detail("device ordinal out of range");
-        return FAIR_ERR_ARG;
-    }
-    std::lock_guard<std::mutex> lk(g_addr_mu);
-    NoAllocAddrs &a = g_addrs[dev];
-    if (!a.ready) {
-        void *pv = nullptr, *ps = nullptr;
-        FAIR_CUDA(cudaGetSymbolAddress(&pv, g_noalloc_vectors));
-        FAIR_CUDA(cudaGetSymbolAddress(&ps, g_noalloc_sched));
-        a.vectors = static_cast<double *>(pv);
-        a.sched = static_cast<unsigned *>(ps);
-        a.ready = true;
-    }
-    out = a;
+    void *pv = nullptr, *ps = nullptr;
+    FAIR_CUDA(cudaGetSymbolAddress(&pv, g_noalloc_vectors));
+    FAIR_CUDA(cudaGetSymbolAddress(&ps, g_noalloc_sched));
+    out.vectors = static_cast<double *>(pv);
+    out.sched = static_cast<unsigned *>(ps);
     return FAIR_OK;
 }
 

@@ -6,7 +6,9 @@ the device synchronisation of cudaMalloc/cudaFree, a job held to a fixed
 memory budget on a shared GPU -- use this entry point instead of
 fair_matvecmul. It stages the vectors in a fixed device array of the library,
 so its result must equal fair_matvecmul's on consecutive calls (the array is
-reused), and problems larger than the array must be refused.
+reused), whatever value precision the handle is set to (the product is
+computed in FP64), with no change in the GPU's free memory; n + m up to the
+array's size must be accepted and larger problems refused.
 """
 import ctypes as C
 
@@ -66,3 +68,58 @@ def test_noalloc_size_errors(fair):
     st, _ = _call(f, big, np.ones(1))
     assert st == 4
     assert b"FAIR_NOALLOC_MAX_ENTRIES" in fair.lib().fair_last_error_detail()
+
+
+def test_noalloc_computes_fp64_on_a_reduced_precision_handle(fair, oracle):
+    """A handle set to q16 or f32 values still gets the FP64 product."""
+    f = _entry(fair)
+    n, nth, p = 40, 30, 58
+    th = np.pi * np.arange(nth) / nth
+    A = fair.paralleltomo(fair.Data(n=n, p=p, nth=nth, theta=th))
+    R = oracle.paralleltomo(n, nth, p, th)
+    v = np.random.default_rng(4).standard_normal(A.n)
+    ref = oracle.matvecmul(R, v)
+    scale = oracle.matvecmul(R, np.abs(v))
+    for prec in ("q16", "f32"):
+        A.set_precision(prec)
+        for _ in range(2):
+            st, w = _call(f, A, v)
+            assert st == 0
+            assert _close(w, ref, scale)
+    A.close()
+
+
+def test_noalloc_accepts_the_largest_problem(fair):
+    """n + m == FAIR_NOALLOC_MAX_ENTRIES exactly: accepted (an empty matrix
+    of LIMIT - 1 rows and one column: w = 0)."""
+    f = _entry(fair)
+    m = LIMIT - 1
+    edge = fair.CSRMatrix.construct(m, 1, np.zeros(0), np.zeros(m + 1, np.int32),
+                                    np.zeros(0, np.int32))
+    st, w = _call(f, edge, np.ones(1))
+    assert st == 0
+    assert not np.any(w)
+    edge.close()
+
+
+def test_noalloc_leaves_free_memory_unchanged(fair):
+    """Around a call on a fresh handle whose work buffers were never grown
+    (after one call elsewhere has loaded the kernels), the GPU's free memory
+    does not change."""
+    import torch
+    f = _entry(fair)
+    th = np.pi * np.arange(40) / 40
+    A = fair.paralleltomo(fair.Data(n=48, p=70, nth=40, theta=th))
+    assert _call(f, A, np.ones(A.n))[0] == 0  # warm: the product's kernels are loaded
+    B = fair.paralleltomo(fair.Data(n=56, p=80, nth=36, theta=np.pi * np.arange(36) / 36))
+    v = np.random.default_rng(2).standard_normal(B.n)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        st, w = _call(f, B, v)
+        assert st == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert np.allclose(w, B.matvecmul(v), rtol=1e-13, atol=1e-13)
+    A.close()
+    B.close()
