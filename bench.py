@@ -748,10 +748,11 @@ def run_mfree(args):
     """Matrix-free SIRT (a secondary line): parallel beam N=2048, 1440 angles
     over [0, pi), 2896 bins (7.7e9 nonzeros if stored: 92 GB in FP64 per
     copy), seeded 20-Gaussian phantom, 1% noise, SIRT (Cimmino) 50 iterations
-    in FP32 on the matrix-free projector pair (FP64 weights and iterate);
-    beside it, at the N=1024 problem (720 angles, 1448 bins) that the stored
-    form holds comfortably, the matrix-free and the stored (packed FP32,
-    autotuned) SIRT iterations."""
+    in FP32 on the matrix-free projector pair (FP64 weights and iterate), and
+    on the same matrix stored in FP32 only (A and A' as FP32 values with int64
+    row offsets, 123 GB, built by blocks of angles), each arm's iterate
+    compared with the other's; beside it, at the N=1024 problem (720 angles,
+    1448 bins), the matrix-free and the stored (FP32, autotuned) iterations."""
     import ctypes as C
 
     import torch
@@ -801,7 +802,15 @@ def run_mfree(args):
         res = {"iter_per_s": K / (ms / 1e3), "ms_per_iteration": ms / K,
                "project_ms": t1 / 5, "backproject_ms": t2 / 5, "nnz": nnz,
                "entries_per_s": 2 * nnz / (ms / K / 1e3), "clocks": clocks}
+        # the matrix-free iterate after K iterations from zero (error reference)
+        with torch.cuda.stream(stream):
+            d_x.zero_()
+        M.run_device(d_b.data_ptr(), d_x.data_ptr(), K)
+        stream.synchronize()
+        x_mf = d_x.cpu().numpy()
         M.close()
+        if n == 2048 and not args.no_stored:
+            res["stored_f32"] = stored_f32_arm(args, F, d, b, x_mf, K, stream, d_b, d_x)
         if n == 1024:  # the stored form, packed FP32, autotuned
             A = F.paralleltomo(d)
             A.set_stream(stream.cuda_stream)
@@ -841,6 +850,71 @@ def run_mfree(args):
     return 0
 
 
+def stored_f32_arm(args, F, d, b, x_mf, K, stream, d_b, d_x):
+    """The stored-CSR arm of the matrix-free comparison: the same geometry held
+    in FP32 only (fair_paralleltomo_f32: A and A' as FP32 values, int32
+    columns, int64 row offsets, built by blocks of angles), K Cimmino
+    iterations on the CSR layout, timed like the matrix-free ones; the two
+    iterates are compared with each other."""
+    import ctypes as C
+
+    import torch
+
+    from fortran_airtools_gb300._clib import check, lib
+    L = lib()
+    t0 = time.perf_counter()
+    H = F.paralleltomo_f32(d)
+    build_s = time.perf_counter() - t0
+    m, n, nnz = H.info()
+    H.set_stream(stream.cuda_stream)
+    opts = F.airms.options()
+    check(L.fair_sirt_prepare(H.handle, b"cimmino", C.byref(opts)))
+    out = {"build_s": build_s, "nnz": nnz, "row_offsets": "int64",
+           "device_bytes_matrix": int(nnz * 16 + (m + n + 2) * 8)}
+    for cfg in ((8, 8, 0, 0), (8, 8, 9, 9)):
+        # the CSR, then the tiled copies built beside it (another ~100 GB: if the
+        # GPU cannot hold them the line says so)
+        st = L.fair_sirt_set_lanes(H.handle, (C.c_int32 * 4)(*cfg))
+        if st == 0:
+            with torch.cuda.stream(stream):
+                d_x.zero_()
+            st = L.fair_sirt_run_device(H.handle, d_b.data_ptr(), d_x.data_ptr(), 1)
+            stream.synchronize()
+        if st != 0:
+            out[f"layout_{cfg[2]}_{cfg[3]}"] = {"unavailable": F.FairError(st).args[0]}
+            break
+        with torch.cuda.stream(stream):
+            d_x.zero_()
+        check(L.fair_sirt_run_device(H.handle, d_b.data_ptr(), d_x.data_ptr(), 3))  # warm-up
+        stream.synchronize()
+        with torch.cuda.stream(stream):
+            d_x.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        check(L.fair_sirt_run_device(H.handle, d_b.data_ptr(), d_x.data_ptr(), K))
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1)
+        x_st = d_x.cpu().numpy()
+        ms1, ms2 = C.c_float(), C.c_float()
+        with torch.cuda.stream(stream):
+            d_x.zero_()
+        check(L.fair_sirt_run_device_timed(H.handle, d_b.data_ptr(), d_x.data_ptr(), 3,
+                                           C.byref(ms1), C.byref(ms2)))
+        gb = 2 * nnz * 8 / 1e9
+        key = "csr" if cfg[2] == 0 else f"layout_{cfg[2]}_{cfg[3]}"
+        out[key] = {
+            "iter_per_s": K / (ms / 1e3), "ms_per_iteration": ms / K,
+            "pass1_ms": ms1.value / 3, "pass2_ms": ms2.value / 3,
+            "matrix_gbs": gb / (ms / K / 1e3), "pass_config": list(cfg),
+            "rel_err_vs_matrix_free": float(np.linalg.norm(x_st - x_mf) / np.linalg.norm(x_mf))}
+        if cfg[2] == 9:  # whether the tiled copies were built (else the passes read the CSR)
+            out[key]["tiled_built"] = [H.tiled_info()["has"], H.tiled_info(transposed=True)["has"]]
+    H.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -868,6 +942,8 @@ def main():
     ap.add_argument("--batch-prec", choices=["f64", "f32", "f16", "q16"], default="f32")
     ap.add_argument("--batch-layout", default="tiled,packed",
                     help="batch layouts timed, one line each (comma list of tiled, packed)")
+    ap.add_argument("--no-stored", action="store_true",
+                    help="mfree workload: skip the stored FP32 arm at N=2048")
     ap.add_argument("--mf-sizes", default="",
                     help="matrix-free cases to run, by N (comma list of 2048, 1024; default both)")
     args = ap.parse_args()

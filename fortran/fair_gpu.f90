@@ -348,6 +348,12 @@ module fair_gpu
        integer(c_int32_t), value :: which
        integer(c_int32_t), intent(out) :: shape(*)
      end function fair_csr_tiled_info
+     integer(c_int) function fair_paralleltomo_f32(dat, block_angles, h) bind(C, name="fair_paralleltomo_f32")
+       import :: c_int, c_ptr, c_int32_t, fair_data
+       type(fair_data), intent(in) :: dat
+       integer(c_int32_t), value :: block_angles
+       type(c_ptr), value :: h
+     end function fair_paralleltomo_f32
      integer(c_int) function fair_matvecmul_noalloc(h, v, size_v, w) bind(C, name="fair_matvecmul_noalloc")
        import :: c_int, c_ptr, c_int64_t, c_double
        type(c_ptr), value :: h

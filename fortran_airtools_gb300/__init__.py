@@ -16,8 +16,8 @@ from . import airms, batch, mfree, phantomgallery, sparse_matrices, system_gener
 from .batch import Batch  # noqa: F401
 from .mfree import MatrixFree  # noqa: F401
 from .sparse_matrices import CSRMatrix  # noqa: F401
-from .system_generation import Data, fanlineartomo, linspace, paralleltomo  # noqa: F401
+from .system_generation import Data, fanlineartomo, linspace, paralleltomo, paralleltomo_f32  # noqa: F401
 
 __all__ = ["FairError", "Opts", "lib", "airms", "batch", "mfree", "phantomgallery",
            "sparse_matrices", "system_generation", "Batch", "CSRMatrix", "Data", "MatrixFree",
-           "fanlineartomo", "linspace", "paralleltomo"]
+           "fanlineartomo", "linspace", "paralleltomo", "paralleltomo_f32"]

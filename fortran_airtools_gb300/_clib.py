@@ -126,6 +126,7 @@ def _declare(L):
         "fair_csr_packed_info": ([h, i32, P(i32), P(i64), P(i64), P(i32), P(i32)], C.c_int),
         "fair_csr_sliced_info": ([h, i32, P(i32), P(i64)], C.c_int),
         "fair_csr_tiled_info": ([h, i32, vp], C.c_int),
+        "fair_paralleltomo_f32": ([P(Data), i32, h], C.c_int),
         "fair_sirt_autotune": ([h, vp, vp, i32, vp], C.c_int),
         "fair_sirt_prepare": ([h, C.c_char_p, P(Opts)], C.c_int),
         "fair_sirt_run_device": ([h, vp, vp, i32], C.c_int),

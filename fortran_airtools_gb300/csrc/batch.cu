@@ -571,6 +571,10 @@ int fair_batch_add(fair_batch B, fair_csr h, int32_t take) {
         fair::set_detail("handle holds no matrix");
         return FAIR_ERR_STATE;
     }
+    if (h->A.f32_only) {  // the batch derives its forms and weights from FP64 values
+        fair::set_detail("the matrix is held in FP32 only (fair_paralleltomo_f32)");
+        return FAIR_ERR_STATE;
+    }
     std::lock_guard<std::mutex> lk(B->mu);
     FAIR_CUDA(cudaStreamSynchronize(h->stream));
     BatchProb *q = new (std::nothrow) BatchProb();

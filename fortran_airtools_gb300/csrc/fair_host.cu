@@ -97,6 +97,8 @@ void DevCSR::release() {
     dl[1].release();
     rowptr.release(); col.release(); v64.release(); v32.release(); v16.release(); vq.release();
     has32 = has16 = hasq = false;
+    rn1.release(); rn2.release();
+    f32_only = false;
     prow.release(); gidx.release(); gside.release();
     pv64.release(); pv32.release(); pv16.release(); pvq.release();
     pf16.release(); pfq.release();
@@ -171,7 +173,7 @@ static void scramble_host(int32_t n, int32_t *arr) {
 }
 
 // linspace, system_generation.f90:17-35
-static void linspace_host(double a, double b, int n, double *x) {
+void linspace_host(double a, double b, int n, double *x) {
     double c = (b - a) / (n - 1);
     double d = a - c;
     for (int i = 1; i <= n; ++i) x[i - 1] = c * i + d;
@@ -238,6 +240,16 @@ using namespace fair;
 #define NEED_MATRIX(h)                                                   \
     do {                                                                 \
         if ((h)->A.empty()) { set_detail("handle holds no matrix"); return FAIR_ERR_STATE; } \
+    } while (0)
+
+// Entry points that read FP64 values refuse a matrix held in FP32 only
+// (fair_paralleltomo_f32).
+#define NEED_F64(h)                                                                         \
+    do {                                                                                    \
+        if ((h)->A.f32_only) {                                                              \
+            set_detail("the matrix is held in FP32 only (fair_paralleltomo_f32): no FP64 values"); \
+            return FAIR_ERR_STATE;                                                          \
+        }                                                                                   \
     } while (0)
 
 extern "C" {
@@ -334,6 +346,10 @@ int fair_csr_set_precision(fair_csr h, int32_t prec) {
         set_detail("precision must be FAIR_PREC_F64, _F32, _F16 or _Q16");
         return FAIR_ERR_ARG;
     }
+    if (h->A.f32_only && prec != FAIR_PREC_F32) {
+        set_detail("the matrix is held in FP32 only (fair_paralleltomo_f32)");
+        return FAIR_ERR_STATE;
+    }
     h->prec = prec;
     return FAIR_OK;
 }
@@ -387,6 +403,7 @@ int fair_csr_download(fair_csr h, double *vA, int64_t *IA, int32_t *JA) {
     NEED_MATRIX(h);
     cudaStream_t s = h->stream;
     if (IA) FAIR_TRY(download<int64_t>(IA, h->A.rowptr.p, (size_t)h->A.m + 1, s));
+    if (vA) NEED_F64(h);
     if (vA) FAIR_TRY(download<double>(vA, h->A.v64.p, (size_t)h->A.nnz, s));
     if (JA) {
         FAIR_TRY(download<int32_t>(JA, h->A.col.p, (size_t)h->A.nnz, s));
@@ -567,6 +584,7 @@ int fair_transvecmul(fair_csr h, const double *v, int64_t size_v, double *w) {
 int fair_rowvecmult(fair_csr h, int32_t k, const double *v, int64_t size_v, double *f) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     if (!v || !f) return FAIR_ERR_NULL;
     if (k < 1 || k > h->A.m) { set_detail("row index outside 1..m"); return FAIR_ERR_ARG; }
     if (size_v != h->A.n) return FAIR_ERR_SIZE;
@@ -581,6 +599,7 @@ int fair_add_scalar_mult_row(fair_csr h, int32_t k, double c, double *w, int64_t
                              const double *lwrb, const double *upb) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     if (!w) return FAIR_ERR_NULL;
     if (k < 1 || k > h->A.m) { set_detail("row index outside 1..m"); return FAIR_ERR_ARG; }
     if (size_w != h->A.n) return FAIR_ERR_SIZE;
@@ -627,6 +646,7 @@ int fair_transpose(fair_csr h) {
 int fair_multiply_by_scalar(fair_csr h, double c) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     h->sirt_ready = false;
     FAIR_TRY(csr_scale(h->A, c, h->stream));
     if (h->at_valid) FAIR_TRY(csr_scale(h->AT, c, h->stream));
@@ -725,6 +745,7 @@ static int normest_dev(fair_csr h, double tol, int maxit, double *sigma) {
 int fair_normest(fair_csr h, const double *tolerance, const int32_t *max_its, double *sigma) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     if (!sigma) return FAIR_ERR_NULL;
     return normest_dev(h, tolerance ? *tolerance : 1e-5, max_its ? *max_its : 100, sigma);
 }
@@ -734,6 +755,7 @@ int fair_gradient_descent(double *xout, fair_csr h, const double *b, const int32
                           const fair_opts *options, int32_t *iters_done) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     if (!xout || !b) return FAIR_ERR_NULL;
     OptVals o = read_opts(options);
     int maxiter = max_iter ? *max_iter : 100;
@@ -904,6 +926,7 @@ int fair_art(double *Xout, const char *art_method, fair_csr h, const double *b,
              const int32_t *order, int32_t nord, const fair_opts *options) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     if (!Xout || !art_method || !b || !Kin) return FAIR_ERR_NULL;
     if (nK < 1) { set_detail("Kin is empty"); return FAIR_ERR_ARG; }
     OptVals o = read_opts(options);
@@ -954,6 +977,7 @@ int fair_twin_art(double *xout, int32_t *final_it, double *Xstore, double *Ystor
                   const int32_t *order, int32_t nord, int32_t slack, const fair_opts *options) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     if (!xout || !final_it || !Xstore || !Ystore || !EG || !art_method || !stoprule || !b || !Kin)
         return FAIR_ERR_NULL;
     if (nK < 1) { set_detail("Kin is empty"); return FAIR_ERR_ARG; }
@@ -1243,6 +1267,7 @@ int fair_sirt_adjoint(fair_csr h, const char *sirt_method, int32_t nrhs, const d
                       const double *gx, double *xK, double *gb, double *gx0, double *glam) {
     ENTER(h);
     NEED_MATRIX(h);
+    NEED_F64(h);
     if (!sirt_method || !b || !lambda || !gx || !gb || !gx0 || !glam) return FAIR_ERR_NULL;
     bool sart;
     if (!strcmp(sirt_method, "cimmino")) sart = false;

@@ -143,6 +143,11 @@ struct DevCSR {
     // slot, a word of four 7-bit steps beside the values (FP32, FP64 forms);
     // dl[1]: 6 entries per slot in one 16-byte record {six 5-bit steps, six
     // 2-byte values} (f16, q16).
+    // Matrices held in FP32 only (fair_paralleltomo_f32): no FP64 values; the
+    // rows' 1- and 2-norms, computed in FP64 from the traced FP64 values, are
+    // kept for the SIRT weights and the norm queries.
+    bool f32_only = false;
+    DevBuf rn1, rn2;   // double [m]
     struct Delta {
         int E = 4, bits = 7;      // entries per slot, bits per step code
         int S = 0, L = 7;         // step code: delta = lo + hi * S, lo the low L bits
@@ -175,6 +180,10 @@ struct GeomTables {
     void release();
 };
 int build_geometry(const GeomTables &G, DevCSR &A, cudaStream_t s);
+// Nonzeros the tables' rays produce (the count pass of build_geometry only).
+int geometry_nnz(const GeomTables &T, int64_t *nnz, cudaStream_t s);
+// linspace, system_generation.f90:17-35: x(i) = c*i + d (host).
+void linspace_host(double a, double b, int n, double *x);
 
 // ---- scans / sparse kernels (sparse.cu) -----------------------------------------
 // Exclusive scan of counts[0..m) into out[0..m] (out[m] = total).

@@ -66,6 +66,10 @@ extern "C" int fair_matvecmul_noalloc(fair_csr h, const double *v, int64_t size_
         set_detail("handle holds no matrix");
         return FAIR_ERR_STATE;
     }
+    if (h->A.f32_only) {  // the product here reads the FP64 values
+        set_detail("the matrix is held in FP32 only (fair_paralleltomo_f32)");
+        return FAIR_ERR_STATE;
+    }
     const int64_t m = h->A.m, n = h->A.n;
     if (size_v != n) return FAIR_ERR_SIZE;  // "Vector input size incorrect."
     if (n + m > (int64_t)FAIR_NOALLOC_MAX_ENTRIES) {

@@ -585,6 +585,16 @@ int csr_scale(DevCSR &A, double c, cudaStream_t s) {
 }
 
 int csr_row_norms(const DevCSR &A, int p, double *d_out, cudaStream_t s) {
+    if (A.f32_only) {  // no FP64 values: the norms kept from the FP64 build
+        if (p != 1 && p != 2) {
+            set_detail("a matrix held in FP32 only keeps its row 1- and 2-norms, no other p");
+            return FAIR_ERR_STATE;
+        }
+        if (A.m > 0)
+            FAIR_CUDA(cudaMemcpyAsync(d_out, (p == 1 ? A.rn1 : A.rn2).p, sizeof(double) * (size_t)A.m,
+                                      cudaMemcpyDeviceToDevice, s));
+        return FAIR_OK;
+    }
     if (A.m > 0) {
         const int g = grid_for(256, (int64_t)A.m * 32);
         const int64_t *rp = A.rowptr.as<int64_t>();

@@ -51,6 +51,16 @@ def paralleltomo(dat: Data) -> CSRMatrix:
     return A
 
 
+def paralleltomo_f32(dat: Data, block_angles: int = 0) -> CSRMatrix:
+    """paralleltomo held in FP32 only (A and A' as FP32 values, int32 columns,
+    int64 row offsets), built on the GPU by blocks of angles; for problems
+    whose FP64 matrix does not fit. The handle runs FP32 products and SIRT."""
+    A = CSRMatrix()
+    d = dat._c()
+    check(lib().fair_paralleltomo_f32(C.byref(d), int(block_angles), A.handle))
+    return A
+
+
 def fanlineartomo(dat: Data, geometry_fix: bool = False) -> CSRMatrix:
     """system_generation.f90:79-307, built on the GPU. geometry_fix=False keeps
     the reference's odd-p ray angles (system_generation.f90:122)."""
@@ -69,4 +79,4 @@ def add_white_noise(b, eta):
     return bt, e
 
 
-__all__ = ["Data", "linspace", "paralleltomo", "fanlineartomo", "add_white_noise", "pi"]
+__all__ = ["Data", "linspace", "paralleltomo", "paralleltomo_f32", "fanlineartomo", "add_white_noise", "pi"]

@@ -117,6 +117,21 @@ int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslot
  * tiles of A' times angle blocks)}; all zero when no copy is built. */
 int fair_csr_tiled_info(fair_csr h, int32_t which, int32_t *shape);
 
+/* paralleltomo (system_generation.f90:309-492) for the FP32 form only: the
+ * same rays, columns and values (traced in FP64, stored rounded to FP32), with
+ * A and A' held as FP32 values, int32 column indices and int64 row offsets
+ * (8 bytes per nonzero each), built by blocks of block_angles angles (0: blocks
+ * of about 2^28 nonzeros) so that the FP64 matrix is never held whole: the
+ * N=2048, 1440-angle, 2896-bin problem (7.69e9 nonzeros) needs 123 GB instead
+ * of the FP64 build's ~280 GB. The row and column 1- and 2-norms are kept from
+ * the FP64 values (SIRT weights). The handle's precision becomes FAIR_PREC_F32
+ * and stays so; fair_matvecmul, fair_transvecmul, the norms, fair_sirt and the
+ * device-resident SIRT entry points work on it (FP32 products, any FP32
+ * layout); entry points that read FP64 values (the Kaczmarz family, gradient
+ * descent, normest, the adjoint, row edits, FP64 downloads of vA, batches)
+ * return FAIR_ERR_STATE. No reference counterpart beyond paralleltomo. */
+int fair_paralleltomo_f32(const fair_data *dat, int32_t block_angles, fair_csr h);
+
 /* Capacity, in doubles, of the fixed device array behind
  * fair_matvecmul_noalloc (32 MiB): n + m of the matrix must fit in it. */
 #define FAIR_NOALLOC_MAX_ENTRIES 4194304
