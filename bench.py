@@ -6,12 +6,14 @@ A step is one SIRT (Cimmino) iteration: a residual pass over A and a
 backprojection/update pass over A'. ``value`` is iterations/s with the matrix
 and vectors resident in HBM (CUDA events on the launching stream); ``e2e`` is
 the same metric through the host C-ABI call fair_sirt (host b in, host x
-out, copies inside the timed region); ``forms`` gives the FP32 and
-FP16-stored forms with their error against the FP64 iterate; ``roofline`` is
-the dominant kernel's algorithmic bytes over its average launch time against
-the measured HBM copy bandwidth; ``cpu_baseline`` is the CPU oracle (a
-restatement of the reference's Fortran) on a bounded sample of the same
-iteration.
+out, copies inside the timed region); ``forms`` gives the FP64, FP32 and
+16-bit forms with their error against the oracle's FP64 iterate (and the GPU
+FP64 one); ``roofline`` is the dominant kernel's algorithmic bytes over its
+average launch time against the measured HBM copy bandwidth; ``cpu_baseline``
+is the CPU oracle (a restatement of the reference's Fortran) on a bounded
+sample of the same iteration, three ways; ``secondary`` holds the lines of
+the other workloads (Kaczmarz family, adjoint, batch, matrix-free and stored
+FP32 at N=2048), each run in its own process after the headline.
 
 --impl reference times the CPU restatement of the reference (oracle/, all
 host threads for the row-parallel product and for the transposed product, the
@@ -419,7 +421,7 @@ def run_ours(args):
     on_pk = bool(pk and pk[dom - 1])
     code = (head["pass_config"]["groups_per_lane"][dom - 1] if head.get("pass_config")
             else 0 if hp == "f64" else 1)  # the library's default layouts
-    kname = ("k_tl_partials" if dom == 1 and code in (9, 10, 14) and on_pk else
+    kname = ("k_tl_partials" if code in (9, 10, 14) and on_pk else
              {1: "k_sirt_resid", 2: "k_sirt_update"}[dom] + kernel_suffix(hp, code, on_pk))
     dom_bytes = b2 if dom == 2 else b1
     dom_ms = head["pass2_ms"] if dom == 2 else head["pass1_ms"]
@@ -506,11 +508,45 @@ def run_ours(args):
             "clocks": head["clocks"],
             "cpu_baseline": cpu,
         }
-        print(json.dumps(line))
     A.close()
+    if rank == 0:
+        if world == 1 and not args.no_secondary:
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            line["secondary"] = run_secondary(args)
+        print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+SECONDARY = [  # (name, extra arguments, time limit in s): the other workloads of the path
+    ("kaczmarz", ["--workload", "kaczmarz", "--no-cpu"], 300),
+    ("adjoint", ["--workload", "adjoint", "--no-cpu"], 300),
+    ("batch", ["--workload", "batch", "--batch-layout", "auto", "--no-cpu"], 600),
+    ("mfree", ["--workload", "mfree", "--mf-sizes", "2048"], 600),
+]
+
+
+def run_secondary(args):
+    """The secondary workloads (Kaczmarz family, adjoint, batch, matrix-free and
+    stored FP32 at N=2048), each in a process of its own after the headline
+    run has freed its GPU memory; their JSON lines are collected here so that
+    one bench run records every workload. CPU baselines of these lines are
+    skipped (the headline line carries the CPU comparison)."""
+    out = {}
+    for name, extra, limit in SECONDARY:
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + extra,
+                               capture_output=True, text=True, timeout=limit, cwd=ROOT)
+            lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+            out[name] = {"rc": r.returncode, "wall_s": time.perf_counter() - t0, "lines": lines}
+            if r.returncode != 0:
+                out[name]["stderr_tail"] = r.stderr[-600:]
+        except subprocess.TimeoutExpired:
+            out[name] = {"rc": None, "error": f"timed out after {limit} s"}
+    return out
 
 
 def run_kaczmarz(args):
@@ -665,6 +701,12 @@ def run_batch_layout(args, layout):
     build_s = time.perf_counter() - t0
     info = B.info()
     ball = np.concatenate(bs)
+    shapes = {}
+    for i in range(nprob):  # the layout each problem runs on
+        lay = B.problem_layout(i)
+        key = (f"tiled {lay['tile']}/{lay['pixel_tile']}x{lay['cells']}" if lay["tiled"]
+               else "packed")
+        shapes[key] = shapes.get(key, 0) + 1
     B.set_stream(stream.cuda_stream)
     opts = F.airms.options(lbound=0.0, ubound=1.0)
     B.prepare("sart", opts)
@@ -724,7 +766,7 @@ def run_batch_layout(args, layout):
                "iteration (3 minus 1), scaled by nonzeros to the whole batch"}
     line = {"metric": "batched SART iter/s (all problems per iteration)",
             "workload": f"{nprob} fan-beam problems, N 64..512, 90..720 angles, p = ceil(1.42N)",
-            "layout": layout,
+            "layout": layout, "problem_layouts": shapes,
             "value": K / (ms_b / 1e3), "unit": "batch iter/s", "ms_per_iteration": ms_b / K,
             "iterations": K, "dtype": args.batch_prec, "problems": nprob, "nnz": info["nnz"],
             "device_bytes": info["device_bytes"], "build_s": build_s,
@@ -940,8 +982,10 @@ def main():
                     help="sirt: the headline line; kaczmarz, adjoint, batch, mfree: secondary lines")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--batch-prec", choices=["f64", "f32", "f16", "q16"], default="f32")
-    ap.add_argument("--batch-layout", default="tiled,packed",
-                    help="batch layouts timed, one line each (comma list of tiled, packed)")
+    ap.add_argument("--batch-layout", default="auto,tiled,packed",
+                    help="batch layouts timed, one line each (comma list of auto, tiled, packed)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="headline only: skip the secondary workloads run after it")
     ap.add_argument("--no-stored", action="store_true",
                     help="mfree workload: skip the stored FP32 arm at N=2048")
     ap.add_argument("--mf-sizes", default="",

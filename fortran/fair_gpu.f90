@@ -342,6 +342,11 @@ module fair_gpu
        integer(c_int32_t), intent(out) :: has
        integer(c_int64_t), intent(out) :: nslots
      end function fair_csr_sliced_info
+     integer(c_int) function fair_sirt_set_tiles(h, shape) bind(C, name="fair_sirt_set_tiles")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: h
+       integer(c_int32_t), intent(in) :: shape(*)
+     end function fair_sirt_set_tiles
      integer(c_int) function fair_csr_tiled_info(h, which, shape) bind(C, name="fair_csr_tiled_info")
        import :: c_int, c_ptr, c_int32_t
        type(c_ptr), value :: h
@@ -386,6 +391,12 @@ module fair_gpu
        type(c_ptr), value :: b, h
        integer(c_int32_t), value :: take
      end function fair_batch_add
+     integer(c_int) function fair_batch_problem_layout(b, p, layout) bind(C, name="fair_batch_problem_layout")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: b
+       integer(c_int32_t), value :: p
+       integer(c_int32_t), intent(out) :: layout(*)
+     end function fair_batch_problem_layout
      integer(c_int) function fair_batch_info(b, nprob, rows, cols, nnz, device_bytes) &
           bind(C, name="fair_batch_info")
        import :: c_int, c_ptr, c_int32_t, c_int64_t

@@ -126,6 +126,7 @@ def _declare(L):
         "fair_csr_packed_info": ([h, i32, P(i32), P(i64), P(i64), P(i32), P(i32)], C.c_int),
         "fair_csr_sliced_info": ([h, i32, P(i32), P(i64)], C.c_int),
         "fair_csr_tiled_info": ([h, i32, vp], C.c_int),
+        "fair_sirt_set_tiles": ([h, vp], C.c_int),
         "fair_paralleltomo_f32": ([P(Data), i32, h], C.c_int),
         "fair_sirt_autotune": ([h, vp, vp, i32, vp], C.c_int),
         "fair_sirt_prepare": ([h, C.c_char_p, P(Opts)], C.c_int),
@@ -164,6 +165,7 @@ def _declare(L):
         "fair_batch_set_layout": ([h, i32], C.c_int),
         "fair_batch_add": ([h, h, i32], C.c_int),
         "fair_batch_info": ([h, P(i32), P(i64), P(i64), P(i64), P(i64)], C.c_int),
+        "fair_batch_problem_layout": ([h, i32, vp], C.c_int),
         "fair_batch_offsets": ([h, vp, vp], C.c_int),
         "fair_batch_pass_bytes": ([h, i32, P(i64), P(i64)], C.c_int),
         "fair_batch_sirt": ([h, C.c_char_p, vp, i32, vp, P(Opts), vp], C.c_int),

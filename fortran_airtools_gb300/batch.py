@@ -16,17 +16,21 @@ from .airms import options
 
 
 class Batch:
+    LAYOUTS = {"packed": 0, "tiled": 1, "auto": 2}
+
     def __init__(self, prec: str = "f32", layout: str = "packed"):
-        """layout 'packed' (the packed index streams; CSR in f64) or 'tiled'
-        (the tiled copies of A and A' for every problem on an N x N image)."""
-        if layout not in ("packed", "tiled"):
-            raise ValueError("layout must be 'packed' or 'tiled'")
+        """layout 'packed' (the packed index streams; CSR in f64), 'tiled'
+        (the tiled copies of A and A' for every problem on an N x N image) or
+        'auto' (per class of problems the faster of the two, timed on its
+        first problem, with the fastest tile shape)."""
+        if layout not in self.LAYOUTS:
+            raise ValueError("layout must be 'packed', 'tiled' or 'auto'")
         self._h = C.c_void_p()
         check(lib().fair_batch_create(C.byref(self._h), PREC[prec]))
         self.prec = prec
         self.layout = layout
-        if layout == "tiled":
-            check(lib().fair_batch_set_layout(self._h, 1))
+        if layout != "packed":
+            check(lib().fair_batch_set_layout(self._h, self.LAYOUTS[layout]))
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -56,6 +60,12 @@ class Batch:
                                     C.byref(by)))
         return {"problems": np_.value, "rows": m.value, "cols": n.value, "nnz": nnz.value,
                 "device_bytes": by.value}
+
+    def problem_layout(self, p: int) -> dict:
+        """The layout problem p runs on: {'tiled', 'tile', 'pixel_tile', 'cells'}."""
+        v = (C.c_int32 * 4)()
+        check(lib().fair_batch_problem_layout(self._h, int(p), v))
+        return {"tiled": bool(v[0]), "tile": v[1], "pixel_tile": v[2], "cells": v[3]}
 
     def pass_bytes(self, sart: bool = True):
         """Algorithmic bytes of the two passes of one iteration."""

@@ -175,6 +175,15 @@ void launch_f64(int G, bool dry, const BPass *P, const int64_t *c0, int np, cons
 
 }  // namespace
 
+// The layout the "auto" batch (layout 2) chose for a class of problems (the
+// same image side and bins per angle): tiled copies with their tile shape, or
+// the packed streams (the CSR in FP64), and the pass times that decided it.
+struct ClassChoice {
+    bool tiled = false;
+    int tile[3] = {0, 0, 0};  // A's tile side, A''s pixel-tile side and cells
+    float ms_tiled[2] = {-1.f, -1.f}, ms_packed[2] = {-1.f, -1.f};
+};
+
 // One problem of a batch.
 struct BatchProb {
     DevCSR A, AT;
@@ -202,7 +211,10 @@ struct fair_batch_s {
     std::vector<int64_t> row_off{0}, col_off{0};
     int64_t nnz = 0;
     int cfg[4] = {8, 8, 1, 1};  // lanes A, lanes A', groups A, groups A'
-    int layout = 0;             // 0: packed streams (CSR in FP64); 1: tiled copies where they build
+    int layout = 0;             // 0: packed streams (CSR in FP64); 1: tiled copies where they
+                                // build; 2: per class of problems, the faster of the two, the
+                                // tiled copies with the fastest tile shape
+    std::map<std::pair<int64_t, int64_t>, fair::ClassChoice> classes;  // layout 2, by (n, bins)
     int ntiled = 0;             // problems on their tiled copies
     fair::TlBatch tb1, tb2;     // device tables of the tiled problems' passes
     // prepared state
@@ -424,6 +436,121 @@ int copy_csr(const DevCSR &src, DevCSR &dst, cudaStream_t s) {
     return FAIR_OK;
 }
 
+// Layout 2: times one problem's passes (alone, on scratch vectors) on the
+// packed streams (the CSR in FP64) and on its tiled copies with each candidate
+// tile shape, and keeps the faster layout, with the fastest shape per pass.
+// The problem's weights and transpose are in place.
+int tune_class(fair_batch_s *B, BatchProb &q, ClassChoice &c) {
+    cudaStream_t s = B->stream;
+    const int prec = B->prec;
+    const bool red = prec != FAIR_PREC_F64;
+    const int64_t m = q.A.m, n = q.A.n;
+    TmpBuf b, x, x32, r, sched;
+    FAIR_TRY(b.grow(sizeof(double) * (size_t)(m + 1)));
+    FAIR_TRY(x.grow(sizeof(double) * (size_t)(n + 1)));
+    FAIR_TRY(x32.grow(sizeof(float) * (size_t)(n + 1)));
+    FAIR_TRY(r.grow(sizeof(double) * (size_t)(m + 1)));
+    FAIR_TRY(sched.grow(4 * sizeof(unsigned)));
+    FAIR_CUDA(cudaMemsetAsync(b.p, 0, sizeof(double) * (size_t)(m + 1), s));
+    FAIR_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * (size_t)(n + 1), s));
+    FAIR_CUDA(cudaMemsetAsync(x32.p, 0, sizeof(float) * (size_t)(n + 1), s));
+    FAIR_CUDA(cudaMemsetAsync(sched.p, 0, 4 * sizeof(unsigned), s));
+    SirtDev S;
+    S.prec = prec;
+    S.m = (int32_t)m;
+    S.n = (int32_t)n;
+    S.A = &q.A;
+    S.AT = &q.AT;
+    S.b = b.as<double>();
+    S.Minv = q.M_sart.as<double>();
+    S.D = q.D.as<double>();
+    S.x = x.as<double>();
+    S.x32 = x32.as<float>();
+    S.r = r.p;
+    S.sched = sched.as<unsigned>();
+    cudaEvent_t ev[2];
+    for (auto &e : ev) FAIR_CUDA(cudaEventCreate(&e));
+    struct EvScope {
+        cudaEvent_t *e;
+        ~EvScope() { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+    } evs{ev};
+    // time of one pass on the layout M is set to (best of two rounds of 5)
+    auto timed = [&](int pass, float *out) -> int {
+        *out = -1.f;
+        for (int round = 0; round < 2; ++round) {
+            sirt_pass(S, pass, s);  // warm-up
+            cudaEventRecord(ev[0], s);
+            for (int k = 0; k < 5; ++k) sirt_pass(S, pass, s);
+            cudaEventRecord(ev[1], s);
+            FAIR_CUDA(cudaEventSynchronize(ev[1]));
+            FAIR_CUDA(cudaGetLastError());  // a launch that failed times as nothing
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            ms /= 5;
+            *out = round == 0 ? ms : std::min(*out, ms);
+        }
+        return FAIR_OK;
+    };
+    DevCSR *mats[2] = {&q.A, &q.AT};
+    // the packed streams (reduced forms; groups of 4, 8 lanes) or the CSR (FP64)
+    bool pk = !red;
+    if (red) {
+        FAIR_TRY(sirt_make_forms(q.A, q.AT, prec, s, false, false));
+        pk = q.A.haspk && q.AT.haspk && !(prec == FAIR_PREC_Q16 && (q.A.qsigned || q.AT.qsigned));
+    }
+    if (pk)
+        for (int pass = 1; pass <= 2; ++pass) {
+            mats[pass - 1]->sirt_lanes[prec] = 8;
+            mats[pass - 1]->sirt_groups[prec] = red ? 1 : 0;
+            FAIR_TRY(timed(pass, &c.ms_packed[pass - 1]));
+        }
+    // the tiled copies, each candidate shape
+    static const int shapes[2][4][2] = {{{96, 0}, {64, 0}, {128, 0}, {0, 0}},
+                                        {{32, 13000}, {32, 6500}, {16, 6500}, {48, 13000}}};
+    bool tl_ok = true;
+    for (int pass = 1; pass <= 2 && tl_ok; ++pass) {
+        DevCSR &M = *mats[pass - 1];
+        float best = -1.f;
+        int bk = -1;
+        for (int k = 0; k < 4; ++k) {
+            if (shapes[pass - 1][k][0] == 0) continue;
+            M.tile_req[0] = shapes[pass - 1][k][0];
+            M.tile_req[1] = shapes[pass - 1][k][1];
+            FAIR_TRY(csr_make_tiled(M, prec, pass, s));
+            if (!tl_batch_ready(M, prec)) continue;
+            M.sirt_lanes[prec] = 8;
+            M.sirt_groups[prec] = 9;
+            float t = -1.f;
+            FAIR_TRY(timed(pass, &t));
+            if (best < 0.f || t < best) {
+                best = t;
+                bk = k;
+            }
+        }
+        if (bk < 0) {
+            tl_ok = false;
+            break;
+        }
+        M.tile_req[0] = shapes[pass - 1][bk][0];
+        M.tile_req[1] = shapes[pass - 1][bk][1];
+        c.ms_tiled[pass - 1] = best;
+    }
+    for (DevCSR *M : mats) {  // the batch sets the passes' layouts itself
+        M->sirt_lanes[prec] = 8;
+        M->sirt_groups[prec] = red ? 1 : 0;
+    }
+    c.tiled = tl_ok && (!pk || c.ms_tiled[0] + c.ms_tiled[1] < c.ms_packed[0] + c.ms_packed[1]);
+    c.tile[0] = q.A.tile_req[0];
+    c.tile[1] = q.AT.tile_req[0];
+    c.tile[2] = q.AT.tile_req[1];
+    if (!c.tiled) {
+        q.A.tl.release();
+        q.AT.tl.release();
+    }
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    return FAIR_OK;
+}
+
 // Weights, transpose and forms of a new problem whose A is in place.
 int finish_problem(fair_batch_s *B, BatchProb &q) {
     cudaStream_t s = B->stream;
@@ -433,7 +560,25 @@ int finish_problem(fair_batch_s *B, BatchProb &q) {
     FAIR_TRY(q.D.grow(sizeof(double) * ((size_t)q.A.n + 1)));
     FAIR_TRY(sirt_weights(q.A, q.AT, true, q.M_sart.as<double>(), q.D.as<double>(), s));
     FAIR_TRY(sirt_weights(q.A, q.AT, false, q.M_cim.as<double>(), nullptr, s));
-    if (B->layout == 1) {  // tiled copies of A (pass 1) and A' (pass 2) where both build
+    bool want_tiled = B->layout == 1;
+    if (B->layout == 2) {  // the class's choice, timed on its first problem
+        const std::pair<int64_t, int64_t> key{q.A.n, q.A.tstride_hint};
+        auto it = B->classes.find(key);
+        if (it == B->classes.end()) {
+            ClassChoice c;
+            FAIR_TRY(tune_class(B, q, c));
+            it = B->classes.emplace(key, c).first;
+        }
+        const ClassChoice &c = it->second;
+        want_tiled = c.tiled;
+        if (c.tiled) {
+            q.A.tile_req[0] = c.tile[0];
+            q.A.tile_req[1] = 0;
+            q.AT.tile_req[0] = c.tile[1];
+            q.AT.tile_req[1] = c.tile[2];
+        }
+    }
+    if (want_tiled) {  // tiled copies of A (pass 1) and A' (pass 2) where both build
         FAIR_TRY(csr_make_tiled(q.A, B->prec, 1, s));
         FAIR_TRY(csr_make_tiled(q.AT, B->prec, 2, s));
         FAIR_CUDA(cudaStreamSynchronize(s));
@@ -442,6 +587,9 @@ int finish_problem(fair_batch_s *B, BatchProb &q) {
             q.A.tl.release();
             q.AT.tl.release();
         }
+    } else {
+        q.A.tl.release();
+        q.AT.tl.release();
     }
     if (B->prec != FAIR_PREC_F64 && !q.tiled) {
         FAIR_TRY(sirt_make_forms(q.A, q.AT, B->prec, s, false, false));
@@ -547,8 +695,8 @@ int fair_batch_set_stream(fair_batch B, void *cuda_stream) {
 
 int fair_batch_set_layout(fair_batch B, int32_t layout) {
     BENTER(B);
-    if (layout != 0 && layout != 1) {
-        fair::set_detail("layout must be 0 (packed streams) or 1 (tiled copies)");
+    if (layout != 0 && layout != 1 && layout != 2) {
+        fair::set_detail("layout must be 0 (packed streams), 1 (tiled copies) or 2 (chosen per class)");
         return FAIR_ERR_ARG;
     }
     std::lock_guard<std::mutex> lk(B->mu);
@@ -603,6 +751,21 @@ int fair_batch_add(fair_batch B, fair_csr h, int32_t take) {
     B->nnz += q->A.nnz;
     B->ready = false;
     fair::drop_graph(B);
+    return FAIR_OK;
+}
+
+int fair_batch_problem_layout(fair_batch B, int32_t p, int32_t *layout) {
+    if (!B || !layout) return FAIR_ERR_NULL;
+    std::lock_guard<std::mutex> lk(B->mu);
+    if (p < 0 || p >= (int32_t)B->probs.size()) {
+        fair::set_detail("problem index outside 0..problems-1");
+        return FAIR_ERR_ARG;
+    }
+    const BatchProb &q = *B->probs[p];
+    layout[0] = q.tiled ? 1 : 0;
+    layout[1] = q.tiled ? q.A.tl.T : 0;
+    layout[2] = q.tiled ? q.AT.tl.T : 0;
+    layout[3] = q.tiled ? q.AT.tl.cells_cap : 0;
     return FAIR_OK;
 }
 

@@ -68,6 +68,7 @@ void DevCSR::Tiled::release() {
     v64.release(); v32.release(); r16.release(); rq.release(); part.release();
     sstart.release(); send.release(); bmin.release(); srow.release();
     kind = p = nth = W = 0;
+    cells_cap = 0;
     NA = nab = 1;
     soff6.release(); anc6.release(); code6.release(); side6.release(); r6_16.release(); r6_q.release();
     S6 = 0;
@@ -105,6 +106,7 @@ void DevCSR::release() {
     pk_tried = haspk = hasp64 = hasp32 = hasp16 = haspq = hasf16 = hasfq = false;
     for (int &g : sirt_lanes) g = 8;
     for (int &g : sirt_groups) g = 1;
+    tile_req[0] = tile_req[1] = 0;
     sirt_groups[FAIR_PREC_F64] = 0;
     ngroups = nesc = 0;
     stride_hint = tstride_hint = 0;
@@ -1319,6 +1321,24 @@ int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslot
     *has = ok ? 1 : 0;
     *nslots = ok ? M.nslots : 0;
     return FAIR_OK;
+}
+
+int fair_sirt_set_tiles(fair_csr h, const int32_t *shape) {
+    ENTER(h);
+    NEED_MATRIX(h);
+    if (!shape) return FAIR_ERR_NULL;
+    auto in = [](int32_t v, int lo, int hi) { return v == 0 || (v >= lo && v <= hi); };
+    if (!in(shape[0], 16, 128) || !in(shape[1], 8, 64) || !in(shape[2], 1024, 16384)) {
+        set_detail("tile shape: side of A's tiles 16-128, pixel tiles of A' 8-64, cells 1024-16384 (0: default)");
+        return FAIR_ERR_ARG;
+    }
+    FAIR_CUDA(cudaStreamSynchronize(h->stream));
+    h->A.tile_req[0] = shape[0];
+    h->A.tile_req[1] = 0;
+    FAIR_TRY(ensure_transpose(h));
+    h->AT.tile_req[0] = shape[1];
+    h->AT.tile_req[1] = shape[2];
+    return FAIR_OK;  // the tiled copies are rebuilt with these shapes when a pass next reads them
 }
 
 int fair_csr_tiled_info(fair_csr h, int32_t which, int32_t *shape) {

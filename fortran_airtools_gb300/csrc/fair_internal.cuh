@@ -66,6 +66,11 @@ struct DevCSR {
     // 5, 6 the sliced copy with 2 or 4 steps in flight; 7, 8 the same with
     // the gathers one step ahead
     int sirt_groups[4] = {0, 1, 1, 1};
+    // requested shape of the tiled copy (0: the defaults): [0] the tile side
+    // (A, pass 1: T x T pixels) or the pixel-tile side (A', pass 2); [1] (A')
+    // the most residual cells a tile's shared copy holds (angles per block x
+    // bins per angle)
+    int tile_req[2] = {0, 0};
     // allocate col and v64 for nnz entries plus the pad (pad zeroed)
     int alloc_entries(int64_t nnz_, cudaStream_t s);
     DevBuf rowptr;        // int64 [m+1]
@@ -112,6 +117,7 @@ struct DevCSR {
         // (A': pixels) times blocks of NA angles of the columns (rays a*p + b),
         // each with a window of W bins per angle starting at bmin
         int kind = 0, p = 0, nth = 0, NA = 1, nab = 1, W = 0;
+        int cells_cap = 0;  // kind 1: the residual cells per tile it was built for
         DevBuf bmin;      // int32 [ntr*ntr*nth] (kind 1)
         DevBuf srow;      // int32 [nseg] row of each segment (value fills)
         int64_t nseg = 0, nchunks = 0, nslots = 0;
@@ -247,6 +253,9 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s);
 // an N x N image and whose columns rays of p bins per angle (p = its stride
 // hint). Does nothing for other matrices.
 int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s);
+// The tile shape csr_make_tiled uses for M in `pass` (the request or the
+// default): tile side and (pass 2) residual cells per tile.
+void tiled_shape(const DevCSR &M, int pass, int *side, int *cells);
 // A SIRT pass on the tiled copy (layout codes 9, 10, 14; two kernels); false
 // when the matrix has no tiled copy of the form.
 bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cudaStream_t s);

@@ -340,11 +340,11 @@ static void lp_pass(const SirtDev &S, const DevCSR &M, int pass, const VT *vals,
         if (sirt_pass_tiled(S, M, pass, code, s)) return;
         code = 9;
     }
-    if (code >= 11) {
+    if (code >= 11 && code <= 13) {
         if (sirt_pass_delta(S, M, pass, code, s)) return;
         code = code == 11 ? 5 : 8;  // no delta copy: the sliced copy
     }
-    if (code >= 9) {
+    if (code == 9 || code == 10) {
         if (sirt_pass_tiled(S, M, pass, code, s)) return;
         code = 3;  // no tiled copy: the fused records (else the packed stream)
     }
@@ -410,8 +410,8 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
                            M.pk_L};
             const double *pv = M.pv64.as<double>();
             if (NG == 14) NG = 9;  // step records: 2-byte forms only
-            if (NG >= 11 && sirt_pass_delta(S, M, pass, NG, s)) return;
-            if (NG >= 9 && NG <= 10 && sirt_pass_tiled(S, M, pass, NG, s)) return;
+            if (NG >= 11 && NG <= 13 && sirt_pass_delta(S, M, pass, NG, s)) return;
+            if ((NG == 9 || NG == 10) && sirt_pass_tiled(S, M, pass, NG, s)) return;
             if (NG >= 5 && NG <= 8 && sirt_pass_sliced(S, M, pass, NG, s)) return;
             if (NG >= 9) NG = 1;
             if (NG > 2) NG = 2 - (NG & 1);  // 3, 5 -> 1 group per lane; 4, 6 -> 2
@@ -583,6 +583,7 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
                 for (int r = 0; r < reps; ++r) sirt_pass(S, pass, s);
                 cudaEventRecord(ev[1], s);
                 cudaError_t e = cudaEventSynchronize(ev[1]);
+                if (e == cudaSuccess) e = cudaGetLastError();  // a launch that failed times as nothing
                 if (e != cudaSuccess) { st = cuda_fail(e, "autotune", __FILE__, __LINE__); break; }
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, ev[0], ev[1]);
@@ -596,6 +597,46 @@ int sirt_autotune(const SirtDev &S, DevCSR &A, DevCSR &AT, int reps, cudaStream_
             }
         M.sirt_lanes[S.prec] = best_g;
         M.sirt_groups[S.prec] = best_code;
+        // a tiled pass: try other tile shapes (the copy is rebuilt for each)
+        // unless the caller asked for one
+        if (st == FAIR_OK && (best_code == 9 || best_code == 10 || best_code == 14) &&
+            M.tile_req[0] == 0 && M.tile_req[1] == 0) {
+            static const int shapes[2][4][2] = {{{96, 0}, {64, 0}, {128, 0}, {0, 0}},
+                                                {{32, 13000}, {32, 6500}, {16, 6500}, {48, 13000}}};
+            int best_shape = 0;
+            float best_t = best_ms;
+            for (int k = 1; k < 4 && st == FAIR_OK; ++k) {
+                if (shapes[pass - 1][k][0] == 0) continue;
+                M.tile_req[0] = shapes[pass - 1][k][0];
+                M.tile_req[1] = shapes[pass - 1][k][1];
+                st = csr_make_tiled(M, S.prec, pass, s);
+                if (st != FAIR_OK) break;
+                if (!M.tl.built() || (best_code == 14 && !M.tl.built6)) continue;
+                float tk = -1.f;
+                for (int round = 0; round < 2 && st == FAIR_OK; ++round) {
+                    sirt_pass(S, pass, s);  // warm-up
+                    cudaEventRecord(ev[0], s);
+                    for (int r = 0; r < reps; ++r) sirt_pass(S, pass, s);
+                    cudaEventRecord(ev[1], s);
+                    cudaError_t e = cudaEventSynchronize(ev[1]);
+                    if (e == cudaSuccess) e = cudaGetLastError();
+                    if (e != cudaSuccess) { st = cuda_fail(e, "autotune", __FILE__, __LINE__); break; }
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+                    ms /= reps;
+                    tk = round == 0 ? ms : std::min(tk, ms);
+                }
+                if (st == FAIR_OK && tk >= 0.f && tk < best_t) {
+                    best_t = tk;
+                    best_shape = k;
+                }
+            }
+            // keep the best shape; the default is recorded as no request
+            M.tile_req[0] = best_shape ? shapes[pass - 1][best_shape][0] : 0;
+            M.tile_req[1] = best_shape ? shapes[pass - 1][best_shape][1] : 0;
+            if (st == FAIR_OK) st = csr_make_tiled(M, S.prec, pass, s);
+            best_ms = best_t;
+        }
         if (st == FAIR_OK && best_code >= 5 && best_code <= 8) st = csr_make_sliced(M, S.prec, best_g, s);
         if (!uses_sliced(M)) M.drop_sliced();  // free the copies no pass reads
         if (!uses_tiled(M)) M.tl.release();

@@ -591,6 +591,93 @@ __device__ __forceinline__ ACC chain_sum(const ACC (&a)[K]) {
     return k[0];
 }
 
+// The partial sums of warp `wid`'s chunks of work unit U, W warps sharing the
+// unit (D = 2 slots in flight), the tile's copy of the gathered vector in xs.
+template <class LD, typename XT, typename ACC>
+__device__ __forceinline__ void tl_stream_chunks(const TlArgs &P, const LD &ldr, int4 U,
+                                                 const XT *__restrict__ xs, ACC *__restrict__ part,
+                                                 int W, int wid) {
+    constexpr int E = LD::E;
+    // independent sums: one per ring slot in the FP32 forms, one in FP64
+    constexpr int KC = sizeof(ACC) == 8 ? 1 : 2;
+    const int lane = threadIdx.x & 31;
+    // the warp's chunks of the unit, one per group of W consecutive
+    // chunks, in snake order (w in even groups, W - 1 - w in odd ones:
+    // the chunks of a tile are sorted longest first, so the warps' sums
+    // of lengths balance), as one stream of slots: the loads of the
+    // next chunks' first slots start during the current chunk. With 2
+    // slots in flight the window reaches at most one slot past the
+    // current chunk: into the next chunk, or, when that chunk has a
+    // single slot, into the first slot of the chunk after it (every
+    // chunk has at least one slot).
+    struct Meta {
+        int64_t s0;
+        int len, ps;
+        typename LD::State st;
+    };
+    auto meta = [&](int c) -> Meta {
+        Meta r{0, 0, -1, typename LD::State{}};
+        if (c < U.z) {
+            const int64_t o0 = __ldg(P.soff + c);
+            r.s0 = o0 + lane;
+            r.len = (int)((__ldg(P.soff + c + 1) - o0) >> 5);
+            r.ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
+            r.st = ldr.init((int64_t)c * 32 + lane);
+        }
+        return r;
+    };
+    // chunk of group g (past the unit's end once one is: later groups
+    // start after every chunk of group g)
+    auto chunk_of = [&](int g) { return U.y + W * g + ((g & 1) ? W - 1 - wid : wid); };
+    int g = 0, c = chunk_of(0);
+    Meta cur = meta(c), nxt = meta(chunk_of(1));
+    // slot q of the stream that starts at chunk c = chunk_of(g) (q <=
+    // cur.len + 1); the chunk after nxt is looked up only when the
+    // window reaches it (a 1-slot nxt: the tiles' shortest segments)
+    auto fetch = [&](int q) {
+        if (q < cur.len) return ldr.load(cur.s0 + 32 * (int64_t)q);
+        q -= cur.len;
+        if (q < nxt.len) return ldr.load(nxt.s0 + 32 * (int64_t)q);
+        const int c2 = chunk_of(g + 2);
+        return q == nxt.len && c2 < U.z ? ldr.load(__ldg(P.soff + c2) + lane) : LD::none();
+    };
+    typename LD::Raw ring[2] = {fetch(0), fetch(1)};
+    while (c < U.z) {
+        ACC acc[KC] = {};
+        int t = 0;
+        for (; t + 2 <= cur.len; t += 2) {  // slot pairs: both slots' work interleaves
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const typename LD::Raw r = ring[k];
+                ring[k] = fetch(t + k + 2);
+                uint32_t li[E];
+                ACC v[E];
+                ldr.open(r, cur.st, li, v);
+#pragma unroll
+                for (int q = 0; q < E; ++q) acc[k % KC] += (ACC)xs[li[q]] * v[q];
+            }
+        }
+        if (t < cur.len) {  // an odd last slot, in ring[0]
+            const typename LD::Raw r = ring[0];
+            ring[0] = fetch(t + 2);
+            uint32_t li[E];
+            ACC v[E];
+            ldr.open(r, cur.st, li, v);
+#pragma unroll
+            for (int q = 0; q < E; ++q) acc[0] += (ACC)xs[li[q]] * v[q];
+            // the next chunk's slot 0 now sits in ring[1]
+            const typename LD::Raw tmp = ring[0];
+            ring[0] = ring[1];
+            ring[1] = tmp;
+        }
+        if (cur.ps >= 0) part[cur.ps] = chain_sum<ACC, KC>(acc);
+        ++g;
+        c = chunk_of(g);
+        cur = nxt;
+        nxt = meta(chunk_of(g + 1));
+    }
+}
+
 // Partial sums of all segments. Persistent CTAs take work units through
 // ctr[0] (reset by the last CTA through ctr[1] for the next launch).
 // One work unit U (a tile and a range of its chunks) by the whole CTA: the
@@ -604,7 +691,6 @@ __device__ __forceinline__ void tl_unit(const TlArgs &P, const LD &ldr, const XT
     // independent sums: one per ring slot in the FP32 forms, one in FP64 (whose
     // pass is bound by the FP64 pipe and keeps its registers for a second CTA
     // per SM)
-    constexpr int KC = sizeof(ACC) == 8 ? 1 : 2;
     constexpr int KD = sizeof(ACC) == 8 ? 1 : D;
     const int lane = threadIdx.x & 31;
     {
@@ -612,84 +698,8 @@ __device__ __forceinline__ void tl_unit(const TlArgs &P, const LD &ldr, const XT
         if (threadIdx.x == 0) s_chunk = U.y;
         __syncthreads();
         if constexpr (CONT) {
-            // the warp's chunks of the unit, one per group of W consecutive
-            // chunks, in snake order (w in even groups, W - 1 - w in odd ones:
-            // the chunks of a tile are sorted longest first, so the warps' sums
-            // of lengths balance), as one stream of slots: the loads of the
-            // next chunks' first slots start during the current chunk. With 2
-            // slots in flight the window reaches at most one slot past the
-            // current chunk: into the next chunk, or, when that chunk has a
-            // single slot, into the first slot of the chunk after it (every
-            // chunk has at least one slot).
             static_assert(D == 2, "the continuous stream keeps 2 slots in flight");
-            const int W = blockDim.x >> 5;
-            struct Meta {
-                int64_t s0;
-                int len, ps;
-                typename LD::State st;
-            };
-            auto meta = [&](int c) -> Meta {
-                Meta r{0, 0, -1, typename LD::State{}};
-                if (c < U.z) {
-                    const int64_t o0 = __ldg(P.soff + c);
-                    r.s0 = o0 + lane;
-                    r.len = (int)((__ldg(P.soff + c + 1) - o0) >> 5);
-                    r.ps = __ldg(P.pslot + (int64_t)c * 32 + lane);
-                    r.st = ldr.init((int64_t)c * 32 + lane);
-                }
-                return r;
-            };
-            const int wid = (int)(threadIdx.x >> 5);
-            // chunk of group g (past the unit's end once one is: later groups
-            // start after every chunk of group g)
-            auto chunk_of = [&](int g) { return U.y + W * g + ((g & 1) ? W - 1 - wid : wid); };
-            int g = 0, c = chunk_of(0);
-            Meta cur = meta(c), nxt = meta(chunk_of(1));
-            // slot q of the stream that starts at chunk c = chunk_of(g) (q <=
-            // cur.len + 1); the chunk after nxt is looked up only when the
-            // window reaches it (a 1-slot nxt: the tiles' shortest segments)
-            auto fetch = [&](int q) {
-                if (q < cur.len) return ldr.load(cur.s0 + 32 * (int64_t)q);
-                q -= cur.len;
-                if (q < nxt.len) return ldr.load(nxt.s0 + 32 * (int64_t)q);
-                const int c2 = chunk_of(g + 2);
-                return q == nxt.len && c2 < U.z ? ldr.load(__ldg(P.soff + c2) + lane) : LD::none();
-            };
-            typename LD::Raw ring[2] = {fetch(0), fetch(1)};
-            while (c < U.z) {
-                ACC acc[KC] = {};
-                int t = 0;
-                for (; t + 2 <= cur.len; t += 2) {  // slot pairs: both slots' work interleaves
-#pragma unroll
-                    for (int k = 0; k < 2; ++k) {
-                        const typename LD::Raw r = ring[k];
-                        ring[k] = fetch(t + k + 2);
-                        uint32_t li[E];
-                        ACC v[E];
-                        ldr.open(r, cur.st, li, v);
-#pragma unroll
-                        for (int q = 0; q < E; ++q) acc[k % KC] += (ACC)xs[li[q]] * v[q];
-                    }
-                }
-                if (t < cur.len) {  // an odd last slot, in ring[0]
-                    const typename LD::Raw r = ring[0];
-                    ring[0] = fetch(t + 2);
-                    uint32_t li[E];
-                    ACC v[E];
-                    ldr.open(r, cur.st, li, v);
-#pragma unroll
-                    for (int q = 0; q < E; ++q) acc[0] += (ACC)xs[li[q]] * v[q];
-                    // the next chunk's slot 0 now sits in ring[1]
-                    const typename LD::Raw tmp = ring[0];
-                    ring[0] = ring[1];
-                    ring[1] = tmp;
-                }
-                if (cur.ps >= 0) part[cur.ps] = chain_sum<ACC, KC>(acc);
-                ++g;
-                c = chunk_of(g);
-                cur = nxt;
-                nxt = meta(chunk_of(g + 1));
-            }
+            tl_stream_chunks<LD, XT, ACC>(P, ldr, U, xs, part, blockDim.x >> 5, (int)(threadIdx.x >> 5));
         } else {
             for (;;) {
                 int c = 0;
@@ -887,11 +897,20 @@ int t6_build(DevCSR &A, cudaStream_t s) {
 
 }  // namespace
 
+void tiled_shape(const DevCSR &M, int pass, int *side, int *cells) {
+    const int dflt = pass == 1 ? kTile : kPixTile;
+    *side = M.tile_req[0] > 0 ? M.tile_req[0] : dflt;
+    *cells = pass == 1 ? 0 : (M.tile_req[1] > 0 ? M.tile_req[1] : kPixCells);
+}
+
 int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s) {
     if (A.m == 0 || A.nnz == 0) return FAIR_OK;
     DevCSR::Tiled &tl = A.tl;
     const int kind = pass == 1 ? 0 : 1;
-    if (tl.built() && tl.kind != kind) tl.release();
+    int want_T = 0, want_cells = 0;
+    tiled_shape(A, pass, &want_T, &want_cells);
+    if (tl.built() && (tl.kind != kind || tl.T != want_T || (kind == 1 && tl.cells_cap != want_cells)))
+        tl.release();
     if (!tl.built()) {
         TlGeo G;
         G.kind = kind;
@@ -899,16 +918,16 @@ int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s) {
             const int64_t N = isqrt_exact(A.n);
             if (N <= 0) return FAIR_OK;  // the columns are not an image of N x N pixels
             G.N = (int)N;
-            G.T = kTile;
-            G.ntr = (int)((N + kTile - 1) / kTile);
+            G.T = want_T;
+            G.ntr = (int)((N + want_T - 1) / want_T);
         } else {
             const int64_t N = isqrt_exact(A.m);
             const int p = A.stride_hint;
             // the rows are not an N x N image, or the columns not rays of p bins per angle
             if (N <= 0 || p <= 0 || A.n % p != 0) return FAIR_OK;
             G.N = (int)N;
-            G.T = kPixTile;
-            G.ntr = (int)((N + kPixTile - 1) / kPixTile);
+            G.T = want_T;
+            G.ntr = (int)((N + want_T - 1) / want_T);
             G.p = p;
             G.nth = A.n / p;
             // the bins each pixel tile sees at each angle
@@ -931,11 +950,11 @@ int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s) {
                 if (hi[i] < 0) lo[i] = 0;  // no ray of the tile at this angle
                 else W = std::max(W, hi[i] - lo[i] + 1);
             }
-            if (W <= 0 || W > kPixCells) { tl.release(); return FAIR_OK; }
+            if (W <= 0 || W > want_cells) { tl.release(); return FAIR_OK; }
             FAIR_CUDA(cudaMemcpyAsync(tl.bmin.p, lo.data(), sizeof(int32_t) * nb, cudaMemcpyHostToDevice, s));
             FAIR_CUDA(cudaStreamSynchronize(s));
             G.W = W;
-            G.NA = std::max(1, std::min(G.nth, kPixCells / W));
+            G.NA = std::max(1, std::min(G.nth, want_cells / W));
             G.nab = (G.nth + G.NA - 1) / G.NA;
             G.bmin = tl.bmin.as<int32_t>();
         }
@@ -1054,6 +1073,7 @@ int csr_make_tiled(DevCSR &A, int prec, int pass, cudaStream_t s) {
         tl.NA = G.NA;
         tl.nab = G.nab;
         tl.W = G.W;
+        tl.cells_cap = want_cells;
         tl.nseg = S;
         tl.nchunks = nch;
         tl.nslots = nslots;

@@ -38,8 +38,20 @@ int fair_batch_set_stream(fair_batch b, void *cuda_stream);
  * whose columns form an N x N image and whose rays are p bins per angle;
  * other problems keep the packed layout. A tiled pass is two launches
  * (partial sums per ray segment, then row sums in row order), each covering
- * every tiled problem; the results equal fair_sirt with layout code 9. */
+ * every tiled problem; the results equal fair_sirt with layout code 9.
+ * 2 chooses per class of problems (the same image side and bins per angle):
+ * the first problem of a class is timed alone on the packed streams (the CSR
+ * in FAIR_PREC_F64) and on its tiled copies with each candidate tile shape
+ * (A's tiles 96, 64, 128; A''s pixel tiles x residual cells 32 x 13000,
+ * 32 x 6500, 16 x 6500, 48 x 13000), and the class takes the faster layout
+ * with the fastest shape per pass (fair_batch_problem_layout reports it);
+ * the results equal fair_sirt on that layout and shape. */
 int fair_batch_set_layout(fair_batch b, int32_t layout);
+
+/* The layout problem p (0-based, in the order added) runs on: layout[0] = 1
+ * for the tiled copies (0: packed streams / CSR), then A's tile side, A''s
+ * pixel-tile side and residual cells per tile (0 when not tiled). */
+int fair_batch_problem_layout(fair_batch b, int32_t p, int32_t *layout);
 
 /* Appends the matrix of handle h as the next problem. take = 1 moves the
  * matrix out of h (h is left holding no matrix, as after fair_csr_create);

@@ -109,6 +109,15 @@ int fair_csr_packed_info(fair_csr h, int32_t which, int32_t *has, int64_t *ngrou
  * the padding of each chunk of 32 rows to its longest row). */
 int fair_csr_sliced_info(fair_csr h, int32_t which, int32_t *has, int64_t *nslots);
 
+/* Tile shape of the tiled copies (layout codes 9, 10, 14; no reference
+ * counterpart): shape = {side of A's T x T image tiles (16-128), side of A''s
+ * pixel tiles (8-64), residual cells a tile of A' holds, i.e. angles per block
+ * x bins per angle (1024-16384)}, 0 for the default of each (96, 32, 13000).
+ * The copies are rebuilt with the new shape when a pass next reads them.
+ * fair_sirt_autotune tries other shapes for a tiled pass unless one was set
+ * here; fair_csr_tiled_info reports the shape in use. */
+int fair_sirt_set_tiles(fair_csr h, const int32_t *shape);
+
 /* Shape of the tiled copy of A (which = 0) or A' (which = 1), built when a
  * SIRT pass is set to layout 9, 10 or 14 or by the autotuner (no reference
  * counterpart). shape receives 8 values: {built (0/1), tile side T, tiles per

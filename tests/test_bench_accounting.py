@@ -45,3 +45,4 @@ def test_kernel_names():
     assert bench.kernel_suffix("f32", 4, True) == "_pk"
     assert bench.kernel_suffix("f64", 6, True) == "_sl"
     assert bench.kernel_suffix("q16", 12, True) == "_dl"
+

@@ -156,6 +156,38 @@ def test_tiled_batch_equals_single(problems, fair, oracle, prec, method):
     B.close()
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32", "q16"])
+def test_auto_layout(problems, fair, oracle, prec):
+    """layout 'auto': per class of problems the faster of the packed streams
+    and the tiled copies, with the fastest tile shape, timed on the class's
+    first problem; a tiled problem equals fair_sirt on its tiled copies with
+    the reported shape, bit for bit, and every problem meets its bar against
+    the oracle."""
+    from fortran_airtools_gb300._clib import check, lib
+    B = fair.Batch(prec, layout="auto")
+    for A, _, _ in problems:
+        B.add(A)
+    o = fair.airms.options(lbound=0.0, ubound=1.0)
+    ball = np.concatenate([b for _, _, b in problems])
+    X = B.sirt("sart", ball, 20, opts=o)
+    _, co = B.offsets()
+    tol = {"f64": 1e-10, "f32": 1e-5, "q16": 1e-4}[prec]
+    for p, (A, R, b) in enumerate(problems):
+        lay = B.problem_layout(p)
+        if lay["tiled"]:
+            assert lay["tile"] in (64, 96, 128) and lay["pixel_tile"] in (16, 32, 48)
+            check(lib().fair_sirt_set_tiles(A.handle, (C.c_int32 * 3)(lay["tile"], lay["pixel_tile"],
+                                                                       lay["cells"])))
+            try:
+                xs = single_code9(fair, A, b, prec, "sart", 20, o)
+            finally:
+                check(lib().fair_sirt_set_tiles(A.handle, (C.c_int32 * 3)(0, 0, 0)))
+            assert np.array_equal(X[co[p]:co[p + 1]], xs)
+        xr = oracle.sirt("sart", R, b, 20, opts=oracle.options(lbound=0.0, ubound=1.0))
+        assert rel_err(X[co[p]:co[p + 1]], xr) < tol
+    B.close()
+
+
 def test_tiled_batch_mixed_and_device_api(problems, fair, oracle):
     """A problem whose columns are not an N x N image keeps the packed layout
     beside the tiled ones (three launches per pass); the device-resident
@@ -217,7 +249,7 @@ def test_batch_errors(fair, oracle):
     with pytest.raises(ValueError):
         fair.Batch("f32", layout="rows")
     B = fair.Batch("f32")
-    assert lib().fair_batch_set_layout(B.handle, 2) == 4  # FAIR_ERR_ARG
+    assert lib().fair_batch_set_layout(B.handle, 3) == 4  # FAIR_ERR_ARG
     Bt = fair.Batch("f64")
     At, _ = build(fair, oracle, "par", 16, 12, 24)
     Bt.add(At)

@@ -138,3 +138,32 @@ def test_tiled_many_chunks_per_unit(par200, fair, oracle, prec, codes):
     xc = run(fair, A, b, prec, (8, 8, 0, 0), "cimmino", 5, fair.airms.options())
     assert rel_err(xt, xc) < TOL_SAME[prec]
     assert rel_err(xt, oracle.sirt("cimmino", R, b, 5, nthreads=8)) < (1e-10 if prec == "f64" else 1e-5)
+
+
+@pytest.mark.parametrize("shape", [(64, 16, 6500), (128, 48, 13000), (40, 8, 2048)])
+def test_tile_shapes(par200, fair, oracle, shape):
+    """fair_sirt_set_tiles: other tile sides for A, pixel-tile sides and residual
+    cells for A' (more angle blocks): the same iterates as the CSR layout."""
+    from fortran_airtools_gb300._clib import check, lib
+    A, R, b = par200
+    L = lib()
+    check(L.fair_sirt_set_tiles(A.handle, (C.c_int32 * 3)(*shape)))
+    try:
+        for prec, codes in (("f64", (9, 10)), ("q16", (14, 14))):
+            A.set_precision(prec)
+            check(L.fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, *codes)))
+            xt = fair.airms.sirt("cimmino", A, b, 5)
+            ia, iat = A.tiled_info(), A.tiled_info(transposed=True)
+            assert ia["has"] and ia["tile"] == shape[0]
+            assert iat["has"] and iat["tile"] == shape[1]
+            assert iat["angles_per_block"] * iat["window"] <= shape[2]
+            check(L.fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, 0, 0)))
+            xc = fair.airms.sirt("cimmino", A, b, 5)
+            assert rel_err(xt, xc) < TOL_SAME[prec]
+    finally:
+        check(L.fair_sirt_set_tiles(A.handle, (C.c_int32 * 3)(0, 0, 0)))
+        check(L.fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, 1, 1)))
+        A.set_precision("f64")
+        check(L.fair_sirt_set_lanes(A.handle, (C.c_int32 * 4)(8, 8, 0, 0)))
+    with pytest.raises(fair.FairError):
+        check(L.fair_sirt_set_tiles(A.handle, (C.c_int32 * 3)(200, 0, 0)))
