@@ -10,6 +10,7 @@
 // This file is compiled with -ffp-contract=off for the host compiler so that
 // the geometry tables round every product separately, like the reference.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -314,6 +315,7 @@ int fair_csr_destroy(fair_csr h) {
                       &h->w_D, &h->w_xn, &h->w_tmp, &h->w_part, &h->w_flag, &h->w_ord,
                       &h->w_cumul, &h->w_nrA, &h->w_y, &h->s_M, &h->s_D, &h->s_r, &h->s_x32, &h->w_sched};
     for (DevBuf *b : bufs) b->release();
+    h->w_sweep.release();
     if (h->own_stream) cudaStreamDestroy(h->stream);
     delete h;
     return FAIR_OK;
@@ -804,7 +806,13 @@ struct ArtState {
     std::vector<int32_t> Kuse;
     int32_t nord = 0;
     bool isrand = false, issym = false;
+    uint64_t order_key = 0;  // changes whenever ord changes (sweep schedules are cached by it)
 };
+
+uint64_t new_order_key() {
+    static std::atomic<uint64_t> next{1};
+    return next++;
+}
 
 // AIRMs.f90:217-312 (art) / :525-628 (twin_art)
 int art_setup(fair_csr h, const char *method, const int32_t *Kin, int32_t nK,
@@ -868,6 +876,7 @@ int art_setup(fair_csr h, const char *method, const int32_t *Kin, int32_t nK,
             for (int32_t i = st.nord; i < m; ++i) st.cumul[i] = 1.0;
         }
     }
+    st.order_key = new_order_key();
     FAIR_TRY(upload(h->w_nrA, st.nrA.data(), (size_t)m, s));
     FAIR_TRY(upload(h->w_cumul, st.cumul.data(), (size_t)m, s));
     FAIR_TRY(upload(h->w_ord, st.ord.data(), (size_t)std::max<int32_t>(st.nord, 1), s));
@@ -877,6 +886,7 @@ int art_setup(fair_csr h, const char *method, const int32_t *Kin, int32_t nK,
 int sweep(fair_csr h, const ArtState &st, const OptVals &o, const double *d_b, double *d_x,
           int dir) {
     SweepDev S;
+    S.work = &h->w_sweep;
     S.A = &h->A;
     S.b = d_b;
     S.nrA = h->w_nrA.as<double>();
@@ -885,6 +895,8 @@ int sweep(fair_csr h, const ArtState &st, const OptVals &o, const double *d_b, d
     S.ord = h->w_ord.as<int32_t>();
     S.nord = st.nord;
     S.rand_rowprob = st.isrand && o.rowprob;
+    // random orders are drawn anew in every sweep: no level schedule is kept
+    S.order_key = st.isrand ? 0 : st.order_key;
     S.omg = o.omg;
     S.bmode = o.bmode();
     S.lb = o.lb;
@@ -897,11 +909,19 @@ int sweep(fair_csr h, const ArtState &st, const OptVals &o, const double *d_b, d
     return kaczmarz_sweep(S, dir, h->stream);
 }
 
+// Releases the sweep buffers when a Kaczmarz call returns (on every path):
+// the windowed sweep's reordered entries are of the size of the matrix.
+struct SweepRelease {
+    SweepWork &w;
+    ~SweepRelease() { w.release(); }
+};
+
 int rescramble(fair_csr h, ArtState &st) {
     {
         std::lock_guard<std::mutex> lk(g_rng_mu);
         scramble_host(st.nord, st.ord.data());
     }
+    st.order_key = new_order_key();
     return upload(h->w_ord, st.ord.data(), (size_t)std::max<int32_t>(st.nord, 1), h->stream);
 }
 
@@ -933,6 +953,7 @@ int fair_art(double *Xout, const char *art_method, fair_csr h, const double *b,
     if (nK < 1) { set_detail("Kin is empty"); return FAIR_ERR_ARG; }
     OptVals o = read_opts(options);
     ArtState st;
+    SweepRelease sweep_guard{h->w_sweep};
     FAIR_TRY(art_setup(h, art_method, Kin, nK, order, nord, o, st));
     const int32_t m = h->A.m, n = h->A.n;
     cudaStream_t s = h->stream;
@@ -986,6 +1007,7 @@ int fair_twin_art(double *xout, int32_t *final_it, double *Xstore, double *Ystor
     bool eg = !strcmp(stoprule, "errorgauge"), ms = !strcmp(stoprule, "mutualstep");
     OptVals o = read_opts(options);
     ArtState st;
+    SweepRelease sweep_guard{h->w_sweep};
     FAIR_TRY(art_setup(h, art_method, Kin, nK, order, nord, o, st));
     if (!eg && !ms) {  // AIRMs.f90:584
         set_detail("Unknown stopping rule. Use errorgauge or mutualstep.");

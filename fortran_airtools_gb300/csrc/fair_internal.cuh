@@ -331,7 +331,34 @@ int sirt_adjoint(fair_csr h, bool sart, int nrhs, const double *b, const double 
                  double *xK, double *gb, double *gx0, double *glam);
 
 // Kaczmarz sweep (kaczmarz.cu).
+// Buffers of the Kaczmarz sweeps (kaczmarz.cu), kept by the handle between the
+// sweeps of one call and released at its end.
+struct SweepWork {
+    DevBuf steps;                      // schedule of one sweep
+    // level set-up: step lengths and entry offsets, grouped columns, window
+    // rows, longest paths within the windows, levels, per-level counts, the
+    // column level table (large images), the fallback flag, the blocks' stamp
+    // tables
+    DevBuf lens, eoff, idx, rec, dpath, lvl, cnt, lvtab, err, tabs;
+    int32_t tab_n = 0, tab_blocks = 0;
+    uint64_t uid = 0;                  // next window stamp (the tables hold older ones)
+    bool err_valid = false;            // err holds the set-up's repeated-column flag
+    // level schedules of the last order per direction (forward, backward)
+    struct Levels {
+        uint64_t key = 0;              // the order they were built for (0: none)
+        int32_t nord = 0, nlev = 0;    // steps, levels
+        int64_t entries = 0;           // entries of all steps
+        bool use = false;              // enough steps per level to run the levels
+        DevBuf sched, lptr, dnlev;     // steps in level order, level pointers, level count
+    } lev[2];
+    void release();
+};
+
 struct SweepDev {
+    SweepWork *work = nullptr;
+    // identifies the step order of a sweep (the same key: the same rows in the
+    // same order); 0 for orders drawn anew in each sweep
+    uint64_t order_key = 0;
     const DevCSR *A = nullptr;
     const double *b = nullptr, *nrA = nullptr, *cumul = nullptr;
     double *x = nullptr;
@@ -410,6 +437,7 @@ struct fair_csr_s {
     fair::DevBuf w_in, w_out, w_b, w_x, w_x32, w_r, w_M, w_D, w_xn, w_tmp, w_part, w_flag;
     fair::DevBuf w_ord, w_cumul, w_nrA, w_y;
     fair::DevBuf w_sched;  // two zeroed counters for dynamic chunk scheduling
+    fair::SweepWork w_sweep;  // Kaczmarz sweep buffers (released after each call)
     // state of fair_sirt_prepare (device-resident SIRT)
     bool sirt_ready = false, sirt_sart = false;
     int sirt_prec = FAIR_PREC_F64;

@@ -211,14 +211,21 @@ __device__ __forceinline__ double fx_total(const FxPart *part) {
     return fx_to_double(t, E);
 }
 
+// dup: when given and set, some row repeats a column (found by the level
+// set-up); thread 0 then applies each row's updates one entry after the other,
+// so that a repeated column takes both updates in order as in add_mult_row.
+// only_if_dup: the level sweep ran; this kernel runs only for such a matrix.
 template <int W, int CACHE, bool SMEM_X>
 __global__ void __launch_bounds__(32 * W) k_sweep(const RowStep *__restrict__ steps, int32_t nord,
                                                   const int32_t *__restrict__ col,
                                                   const double *__restrict__ val, double *xg,
-                                                  int32_t n, Box box) {
+                                                  int32_t n, Box box, const int *dup,
+                                                  int only_if_dup) {
     constexpr int T = 32 * W;
     extern __shared__ double xs[];
     __shared__ FxPart part_s[W];
+    const bool serial_update = dup && *dup;
+    if (only_if_dup && !serial_update) return;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     double *x = SMEM_X ? xs : xg;
     if (SMEM_X) {
@@ -282,15 +289,25 @@ __global__ void __launch_bounds__(32 * W) k_sweep(const RowStep *__restrict__ st
             resid = fx_total<1>(&mine);
         }
         const double coeff = __dmul_rn(-resid, cur.w);
+        if (serial_update) {
+            // every thread's reads of x for this row are done (the barrier above,
+            // or the warp's reductions)
+            if (tid == 0)
+                for (int k = 0; k < cur.len; ++k) {
+                    const int32_t c = __ldg(col + cur.s + k);
+                    x[c] = box.apply(fma(coeff, __ldg(val + cur.s + k), x[c]));
+                }
+        } else {
 #pragma unroll
-        for (int q = 0; q < CACHE; ++q) {
-            if (q >= nq) break;
-            int k = tid + q * T;
-            if (k < cur.len) x[cc[q]] = box.apply(fma(coeff, vv[q], xo[q]));
-        }
-        for (int k = tid + CACHE * T; k < cur.len; k += T) {
-            int32_t c = __ldg(col + cur.s + k);
-            x[c] = box.apply(fma(coeff, __ldg(val + cur.s + k), x[c]));
+            for (int q = 0; q < CACHE; ++q) {
+                if (q >= nq) break;
+                int k = tid + q * T;
+                if (k < cur.len) x[cc[q]] = box.apply(fma(coeff, vv[q], xo[q]));
+            }
+            for (int k = tid + CACHE * T; k < cur.len; k += T) {
+                int32_t c = __ldg(col + cur.s + k);
+                x[c] = box.apply(fma(coeff, __ldg(val + cur.s + k), x[c]));
+            }
         }
         if (W > 1) __syncthreads(); else __syncwarp();
         cur = nxt;
@@ -307,17 +324,18 @@ __global__ void __launch_bounds__(32 * W) k_sweep(const RowStep *__restrict__ st
 
 template <int W, int CACHE>
 int launch(const SweepDev &S, const RowStep *steps, bool smem, size_t smem_bytes, const Box &box,
-           cudaStream_t s) {
+           const int *dup, int only_if_dup, cudaStream_t s) {
     const DevCSR &A = *S.A;
     if (smem) {
         auto kern = k_sweep<W, CACHE, true>;
         FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem_bytes));
         kern<<<1, 32 * W, smem_bytes, s>>>(steps, S.nord, A.col.as<int32_t>(), A.v64.as<double>(),
-                                          S.x, A.n, box);
+                                          S.x, A.n, box, dup, only_if_dup);
     } else {
         k_sweep<W, CACHE, false><<<1, 32 * W, 0, s>>>(steps, S.nord, A.col.as<int32_t>(),
-                                                     A.v64.as<double>(), S.x, A.n, box);
+                                                     A.v64.as<double>(), S.x, A.n, box, dup,
+                                                     only_if_dup);
     }
     FAIR_CUDA(cudaGetLastError());
     return FAIR_OK;
@@ -343,13 +361,995 @@ int sweep_warps() {
     return 4;
 }
 
+// ---- level-scheduled sweep ------------------------------------------------------
+// Two steps of a sweep commute when their rows share no column: neither reads
+// what the other writes. Give step k the level 1 + max(level of every earlier
+// step sharing a column with it); then every step's reads come after all
+// earlier steps that write those columns and before all later ones, so running
+// the levels in order, the steps of one level in parallel, gives exactly the
+// sequence of bounded projections of basic_sweep (AIRMs.f90:813-858): the
+// same row sums (exact fixed-point sums of the lanes' FP64 partials, rounded
+// once) and the same updates in the same order per column. For a ray order
+// that walks the bins of one angle and then the next, the levels form a
+// wavefront: a ray waits for its neighbour bin and for the few rays of the
+// previous angle that cross its pixels, so about 30 (fan beam N=128) to 80
+// (N=512) steps share a level.
+//
+// The levels are exact, computed per sweep order in windows of 32 steps:
+//   k_lvl_setup (every SM, windows in parallel): each entry swaps a stamp
+//     into its column's cell of the block's table; a stamp of an earlier step
+//     of the window makes the entry "shared" and sets that step's bit in this
+//     step's predecessor mask; the step's entries are written in groups
+//     [first touch in the window and last | first, not last | shared, not
+//     last | shared and last];
+//   k_lvl_levels (one block, windows in order): a step's level is the larger
+//     of 1 + the table's level over its first-touch columns and 1 + the level
+//     of each predecessor in its mask (a 32-lane recurrence); the last touches
+//     write the step's level into the table;
+//   counting sort of the steps by level (level pointers, steps in level order).
+// The sweep (k_lvl_sweep) runs on one thread-block cluster: a warp per step,
+// the steps of a level spread over the cluster's warps, a cluster barrier
+// between levels; x stays in global memory (L2), read past L1.
+
+struct WinRow {
+    int64_t off;              // first entry of the step in the grouped column array
+    int32_t len, c1, c2, c3;  // entries; groups [0,c1) [c1,c2) [c2,c3) [c3,len)
+};
+static_assert(sizeof(WinRow) == 24, "WinRow layout");
+
+constexpr int kWinRows = 32;      // steps per window (one predecessor bit each)
+constexpr int kMinStepsPerLevel = 4;
+constexpr int kSetupThreads = 512;
+constexpr int kSetupWarps = kSetupThreads / 32;
+// Window stamps of the set-up's column tables: window id (36 bits), step in
+// the window (8 bits), entry position in the window (20 bits). All ones marks
+// an empty cell.
+constexpr int kStampPosBits = 20;
+constexpr unsigned long long kStampIdLimit = (1ull << 36) - 1ull;
+
+__device__ __forceinline__ unsigned long long win_stamp(unsigned long long id, int r, int pos) {
+    return (id << 28) | ((unsigned long long)r << kStampPosBits) | (unsigned long long)pos;
+}
+// group of an entry from its flags (bit 0: a later step has the column; bit 1: an earlier one)
+__device__ __forceinline__ int win_group(unsigned f) {
+    return (f & 2u) ? ((f & 1u) ? 2 : 3) : (int)f;
+}
+
+// total * 2^(E - 1075), rounded once: the integer converted to double (round
+// to nearest even) and rescaled by its exponent field when the result is a
+// normal number; otherwise fx_to_double.
+__device__ __forceinline__ double fx_to_double_fast(long long total, int E) {
+    if (total == 0) return 0.0;
+    const long long bits = __double_as_longlong(__ll2double_rn(total));
+    const int field = (int)((bits >> 52) & 0x7FF) + E - 1075;
+    if (field >= 1 && field <= 2046)
+        return __longlong_as_double(bits + ((long long)(E - 1075) << 52));
+    return fx_to_double(total, E);
+}
+__device__ __forceinline__ double fx_part_double(const FxPart &p) {
+    return p.e >= 0x7FF ? p.d : fx_to_double_fast(p.s, p.e);
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Exclusive scan of n counts (n from *n_dev when given) into out[0..n], one
+// block.
+__global__ void __launch_bounds__(1024) k_scan_excl(const int32_t *__restrict__ in, int64_t n_host,
+                                                   const int *__restrict__ n_dev,
+                                                   int64_t *__restrict__ out) {
+    __shared__ int64_t wsum[32];
+    __shared__ int64_t carry;
+    const int64_t n = n_dev ? (int64_t)*n_dev : n_host;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int64_t b = 0; b < n; b += 1024) {
+        const int64_t i = b + tid;
+        int64_t v = i < n ? in[i] : 0, inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) wsum[wid] = inc;
+        __syncthreads();
+        if (wid == 0) {
+            int64_t w = wsum[lane], wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
+            wsum[lane] = wi - w;
+        }
+        __syncthreads();
+        const int64_t c = carry;
+        if (i < n) out[i] = c + wsum[wid] + inc - v;
+        __syncthreads();
+        if (tid == 1023) carry = c + wsum[31] + inc;
+        __syncthreads();
+    }
+    if (tid == 0) out[n] = carry;
+}
+
+__global__ void k_step_lengths(const RowStep *__restrict__ steps, int32_t nord,
+                               int32_t *__restrict__ lens) {
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nord; k += gridDim.x * blockDim.x)
+        lens[k] = steps[k].len;
+}
+
+// Set-up of the windows (one block per window at a time, a table per block).
+// The steps of a window are taken in order; each entry swaps its stamp into
+// its column's cell, and the stamp it finds tells whether an earlier step of
+// the window has the column (this entry is then shared, that one not last,
+// and that step a predecessor of this one). A stamp of the same step means the
+// row repeats a column: *err is set and the single-block kernel applies the
+// sweep's updates in order instead. From the predecessors, the longest path
+// between every two steps of the window (dpath: 32 bytes per step).
+__global__ void __launch_bounds__(kSetupThreads) k_lvl_setup(
+        const RowStep *__restrict__ steps, const int64_t *__restrict__ eoff, int32_t nord,
+        const int32_t *__restrict__ col, unsigned long long *__restrict__ tabs, int32_t n,
+        unsigned long long id0, int32_t *__restrict__ oidx, WinRow *__restrict__ rec,
+        signed char *__restrict__ dpath, int *err) {
+    extern __shared__ __align__(16) unsigned char fl[];  // [entries of a window]
+    __shared__ int rb[kWinRows + 1];
+    __shared__ uint32_t msk[kWinRows];              // predecessor steps in the window
+    __shared__ signed char dps[kWinRows][kWinRows];  // longest path a -> r, -1: none
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    unsigned long long *tab = tabs + (size_t)blockIdx.x * (size_t)n;
+    const int nwin = (nord + kWinRows - 1) / kWinRows;
+    for (int q = blockIdx.x; q < nwin; q += gridDim.x) {
+        const int k0 = q * kWinRows, nr = min(kWinRows, nord - k0);
+        const int64_t wbase = eoff[k0];
+        if (tid < kWinRows) {
+            rb[tid + 1] = tid < nr ? (int)(eoff[k0 + tid + 1] - wbase) : 0;
+            msk[tid] = 0;
+            if (tid == 0) rb[0] = 0;
+        }
+        __syncthreads();
+        const unsigned long long id = id0 + (unsigned long long)q;
+        for (int r = 0; r < nr; ++r) {
+            const int64_t s0 = steps[k0 + r].s;
+            const int base = rb[r], len = rb[r + 1] - base;
+            for (int e = tid; e < len; e += kSetupThreads) {
+                const int32_t c = col[s0 + e];
+                const int pos = base + e;
+                const unsigned long long old = atomicExch(tab + c, win_stamp(id, r, pos));
+                unsigned char f = 0;
+                if ((old >> 28) == id) {
+                    const int orow = (int)((old >> kStampPosBits) & 0xFFull);
+                    if (orow == r) {
+                        atomicExch(err, 1);
+                    } else {
+                        f = 2;
+                        fl[old & ((1ull << kStampPosBits) - 1ull)] |= 1;  // its one writer
+                        atomicOr(&msk[r], 1u << orow);
+                    }
+                }
+                fl[pos] = f;
+            }
+            __syncthreads();
+        }
+        if (wid == 0) {  // longest paths within the window (rows in order)
+            for (int r = 0; r < nr; ++r) {
+                int v = lane == r ? 0 : -1;
+                for (uint32_t bits = msk[r]; bits; bits &= bits - 1u) {
+                    const int d = dps[__ffs(bits) - 1][lane];
+                    if (d >= 0) v = max(v, d + 1);
+                }
+                dps[r][lane] = (signed char)v;
+                __syncwarp();
+            }
+            for (int r = 0; r < nr; ++r) dpath[(size_t)(k0 + r) * kWinRows + lane] = dps[r][lane];
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        for (int r = wid; r < nr; r += kSetupWarps) {
+            const int64_t s0 = steps[k0 + r].s;
+            const int base = rb[r], len = rb[r + 1] - base;
+            int n0 = 0, n1 = 0, n2 = 0;
+            for (int e0 = 0; e0 < len; e0 += 32) {
+                const int e = e0 + lane;
+                const int g = e < len ? win_group(fl[base + e]) : -1;
+                n0 += __popc(__ballot_sync(0xffffffffu, g == 0));
+                n1 += __popc(__ballot_sync(0xffffffffu, g == 1));
+                n2 += __popc(__ballot_sync(0xffffffffu, g == 2));
+            }
+            int o0 = 0, o1 = n0, o2 = n0 + n1, o3 = n0 + n1 + n2;
+            const int64_t ro = wbase + base;
+            for (int e0 = 0; e0 < len; e0 += 32) {
+                const int e = e0 + lane;
+                const int g = e < len ? win_group(fl[base + e]) : -1;
+                const unsigned b0 = __ballot_sync(0xffffffffu, g == 0);
+                const unsigned b1 = __ballot_sync(0xffffffffu, g == 1);
+                const unsigned b2 = __ballot_sync(0xffffffffu, g == 2);
+                const unsigned b3 = __ballot_sync(0xffffffffu, g == 3);
+                if (g >= 0) {
+                    const int d = g == 0 ? o0 + __popc(b0 & lt)
+                                : g == 1 ? o1 + __popc(b1 & lt)
+                                : g == 2 ? o2 + __popc(b2 & lt)
+                                         : o3 + __popc(b3 & lt);
+                    oidx[ro + d] = col[s0 + e];
+                }
+                o0 += __popc(b0);
+                o1 += __popc(b1);
+                o2 += __popc(b2);
+                o3 += __popc(b3);
+            }
+            if (lane == 0) rec[k0 + r] = WinRow{ro, len, n0, n0 + n1, n0 + n1 + n2};
+        }
+        __syncthreads();  // fl, rb, msk and dps belong to the next window
+    }
+}
+
+// The steps' levels, windows in order (one block of 1024 threads). lv: the
+// last level written into each column (shared memory when it fits, else
+// global memory, zeroed by the caller). A step's level is the largest, over
+// the steps a of its window with a path to it, of base(a) + the path's length,
+// where base(a) = 1 + the table's level over a's first-touch columns. The next
+// window's records are loaded while a window runs.
+template <bool SMEM>
+__global__ void __launch_bounds__(1024, 1) k_lvl_levels(
+        const WinRow *__restrict__ rec, const signed char *__restrict__ dpath,
+        const int32_t *__restrict__ oidx, int32_t nord, int32_t *lvg, int32_t n,
+        int32_t *__restrict__ lvl, int *__restrict__ nlev) {
+    extern __shared__ int32_t lvs[];
+    __shared__ int32_t base[kWinRows], lvw[kWinRows];
+    int32_t *lv = SMEM ? lvs : lvg;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (SMEM)
+        for (int32_t j = tid; j < n; j += 1024) lvs[j] = 0;
+    const WinRow none{0, 0, 0, 0, 0};
+    const int nwin = (nord + kWinRows - 1) / kWinRows;
+    int nr1 = min(kWinRows, nord);
+    WinRow wn = wid < nr1 ? rec[wid] : none;
+    uint4 dn0 = make_uint4(0, 0, 0, 0), dn1 = dn0;
+    if (wid == 0 && lane < nr1) {
+        const uint4 *d = reinterpret_cast<const uint4 *>(dpath + (size_t)lane * kWinRows);
+        dn0 = d[0];
+        dn1 = d[1];
+    }
+    __syncthreads();
+    int top = 0;
+    for (int q = 0; q < nwin; ++q) {
+        const int k0 = q * kWinRows, nr = nr1;
+        const WinRow w = wn;
+        const uint4 d0 = dn0, d1 = dn1;
+        if (q + 1 < nwin) {
+            nr1 = min(kWinRows, nord - k0 - kWinRows);
+            wn = wid < nr1 ? rec[k0 + kWinRows + wid] : none;
+            if (wid == 0 && lane < nr1) {
+                const uint4 *d = reinterpret_cast<const uint4 *>(
+                    dpath + (size_t)(k0 + kWinRows + lane) * kWinRows);
+                dn0 = d[0];
+                dn1 = d[1];
+            }
+        }
+        if (wid < nr) {  // 1 + the table's level over the step's first-touch columns
+            int m = 0;
+            for (int e0 = lane; e0 < w.c2; e0 += 32 * 8) {  // 8 independent loads per lane
+                int32_t j[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) j[t] = e0 + 32 * t < w.c2 ? oidx[w.off + e0 + 32 * t] : -1;
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    if (j[t] >= 0) m = max(m, SMEM ? lvs[j[t]] : __ldcg(lvg + j[t]));
+            }
+            m = (int)__reduce_max_sync(0xffffffffu, (unsigned)m);
+            if (lane == 0) base[wid] = m + 1;
+        }
+        __syncthreads();
+        if (wid == 0) {  // the longest paths within the window
+            const uint32_t dw[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+            int L = 0;
+#pragma unroll
+            for (int a = 0; a < kWinRows; ++a) {
+                const int dv = (int)(signed char)(dw[a >> 2] >> (8 * (a & 3)));
+                if (a < nr && dv >= 0) L = max(L, base[a] + dv);
+            }
+            if (lane < nr) {
+                lvw[lane] = L;
+                lvl[k0 + lane] = L;
+            }
+            top = max(top, (int)__reduce_max_sync(0xffffffffu, lane < nr ? (unsigned)L : 0u));
+        }
+        __syncthreads();
+        if (wid < nr) {  // the last touches of the window write the step's level
+            const int L = lvw[wid];
+            for (int e0 = lane; e0 < w.len; e0 += 32 * 8) {
+                int32_t j[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const int e = e0 + 32 * t;
+                    j[t] = e < w.len && (e < w.c1 || e >= w.c3) ? oidx[w.off + e] : -1;
+                }
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    if (j[t] >= 0) lv[j[t]] = L;
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) *nlev = top;
+}
+
+// The same on a cluster of CS blocks (512 threads each), for a level table
+// in global memory: block c takes the steps c, c + CS, ... of every window
+// (16 * CS / 32 warps per step), so the scattered table reads and writes are
+// spread over CS SMs. The steps' bases meet in distributed shared memory; a
+// cluster barrier after the bases and one after the table writes keep the
+// windows in order. *nlev must be zero at the start.
+template <int CS>
+__global__ void __launch_bounds__(512, 1) k_lvl_levels_cluster(
+        const WinRow *__restrict__ rec, const signed char *__restrict__ dpath,
+        const int32_t *__restrict__ oidx, int32_t nord, int32_t *lv, int32_t *__restrict__ lvl,
+        int *__restrict__ nlev) {
+    constexpr int RW = (kWinRows + CS - 1) / CS;  // steps per block and window
+    constexpr int WPR = 16 / RW;                  // warps per step
+    static_assert(WPR >= 1 && RW * WPR <= 16, "cluster shape");
+    __shared__ int32_t base[RW], lvw[RW];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int rank = (int)cluster_rank();
+    const int i = wid / WPR, sw = wid - i * WPR;  // the warp's step slot, warp in the step
+    const WinRow none{0, 0, 0, 0, 0};
+    const int nwin = (nord + kWinRows - 1) / kWinRows;
+    int top = 0;
+    // distributed shared memory address of the base of step `lane` of a window
+    uint32_t lane_base;
+    {
+        const uint32_t a = (uint32_t)__cvta_generic_to_shared(base);
+        asm("mapa.shared::cluster.u32 %0, %1, %2;"
+            : "=r"(lane_base)
+            : "r"(a + 4u * (uint32_t)(lane / CS)), "r"((uint32_t)(lane % CS)));
+    }
+    for (int q = 0; q < nwin; ++q) {
+        const int k0 = q * kWinRows, nr = min(kWinRows, nord - k0);
+        const int r = rank + CS * i;  // this warp's step in the window
+        const bool mine = i < RW && r < nr;
+        const WinRow w = mine ? rec[k0 + r] : none;
+        if (sw == 0 && lane == 0 && i < RW) base[i] = 0;
+        if (q + 1 < nwin && mine) {  // the next window's step of this warp: its columns into L2
+            const int r1 = r;
+            if (k0 + kWinRows + r1 < nord) {
+                const WinRow wn = rec[k0 + kWinRows + r1];
+                const char *c0 = reinterpret_cast<const char *>(oidx + wn.off);
+                const int nl = (wn.len * 4 + 127) >> 7;
+                for (int l = sw * 32 + lane; l < nl; l += 32 * WPR)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(c0 + ((size_t)l << 7)));
+            }
+        }
+        __syncthreads();
+        if (mine) {  // 1 + the table's level over the step's first-touch columns
+            int m = 0;
+            for (int e0 = sw * 32 + lane; e0 < w.c2; e0 += 32 * WPR * 4) {
+                int32_t j[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int e = e0 + 32 * WPR * t;
+                    j[t] = e < w.c2 ? oidx[w.off + e] : -1;
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (j[t] >= 0) m = max(m, __ldcg(lv + j[t]));
+            }
+            m = (int)__reduce_max_sync(0xffffffffu, (unsigned)m);
+            if (lane == 0) atomicMax(&base[i], m + 1);
+        }
+        cluster_barrier();
+        if (mine && sw == 0) {  // the longest paths within the window
+            const uint4 *dp = reinterpret_cast<const uint4 *>(dpath + (size_t)(k0 + r) * kWinRows);
+            const uint4 d0 = dp[0], d1 = dp[1];
+            const uint32_t dw[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+            int dv = 0;
+#pragma unroll
+            for (int a = 0; a < kWinRows; ++a)
+                if (a == lane) dv = (int)(signed char)(dw[a >> 2] >> (8 * (a & 3)));
+            int bv = 0;
+            if (lane < nr && dv >= 0)
+                asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(bv) : "r"(lane_base));
+            const int L = (int)__reduce_max_sync(0xffffffffu, (lane < nr && dv >= 0) ? (unsigned)(bv + dv) : 0u);
+            if (lane == 0) {
+                lvw[i] = L;
+                lvl[k0 + r] = L;
+            }
+            top = max(top, L);
+        }
+        __syncthreads();
+        if (mine) {  // the last touches of the window write the step's level
+            const int L = lvw[i];
+            for (int e0 = sw * 32 + lane; e0 < w.len; e0 += 32 * WPR * 4) {
+                int32_t j[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int e = e0 + 32 * WPR * t;
+                    j[t] = e < w.len && (e < w.c1 || e >= w.c3) ? oidx[w.off + e] : -1;
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (j[t] >= 0) lv[j[t]] = L;
+            }
+        }
+        cluster_barrier();
+    }
+    if (lane == 0 && top > 0) atomicMax(nlev, top);
+}
+
+__global__ void k_lvl_count(const int32_t *__restrict__ lvl, int32_t nord, int32_t *cnt) {
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nord; k += gridDim.x * blockDim.x)
+        atomicAdd(cnt + lvl[k] - 1, 1);
+}
+// steps in level order (any order within a level: its steps share no column)
+__global__ void k_lvl_scatter(const RowStep *__restrict__ steps, const int32_t *__restrict__ lvl,
+                              int32_t nord, const int64_t *__restrict__ lptr, int32_t *cnt,
+                              RowStep *__restrict__ sched) {
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nord; k += gridDim.x * blockDim.x) {
+        const int l = lvl[k] - 1;
+        sched[lptr[l] + atomicSub(cnt + l, 1) - 1] = steps[k];
+    }
+}
+
+
+// Where the level sweep keeps x: global memory read past L1 (XG), the
+// block's shared memory (XS, one block), or the cluster's distributed shared
+// memory (XD: block r holds x[r * 2^cb, (r + 1) * 2^cb)). XS and XD address x
+// by 32-bit shared-window addresses.
+enum { XG = 0, XS = 1, XD = 2 };
+template <int XM> struct XAcc;
+template <> struct XAcc<XG> {
+    double *x;
+    using R = double *;
+    __device__ __forceinline__ R ref(int32_t j) const { return x + j; }
+    __device__ __forceinline__ double ld(R p) const { return __ldcg(p); }
+    __device__ __forceinline__ void st(R p, double v) const { *p = v; }
+};
+template <> struct XAcc<XS> {
+    uint32_t base;  // shared-window address of x
+    using R = uint32_t;
+    __device__ __forceinline__ R ref(int32_t j) const { return base + ((uint32_t)j << 3); }
+    __device__ __forceinline__ double ld(R a) const {
+        double v;
+        asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(a));
+        return v;
+    }
+    __device__ __forceinline__ void st(R a, double v) const {
+        asm volatile("st.shared.f64 [%0], %1;" ::"r"(a), "d"(v));
+    }
+};
+template <> struct XAcc<XD> {
+    uint32_t base;  // shared-window address of this block's part
+    int cb;         // log2 of the part's length
+    using R = uint32_t;
+    __device__ __forceinline__ R ref(int32_t j) const {  // an address, no memory access
+        const uint32_t a = base + (((uint32_t)j & ((1u << cb) - 1u)) << 3);
+        uint32_t r;
+        asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"((uint32_t)j >> cb));
+        return r;
+    }
+    // volatile keeps these in program order among themselves and against the
+    // barriers (also volatile asm), the only ordering the sweep needs
+    __device__ __forceinline__ double ld(R a) const {
+        double v;
+        asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a));
+        return v;
+    }
+    __device__ __forceinline__ void st(R a, double v) const {
+        asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v));
+    }
+};
+
+// One step by a group of G warps: the row's chunks of 32 entries are dealt
+// to the group's warps in turn (chunk q to warp q mod G), CACHE chunks per
+// warp held in registers and the rest loaded in batches of four. Each warp's
+// part of a.x - b is an exact fixed-point sum (fx_warp_part); the G parts meet
+// in shared memory behind the group's named barrier, are added exactly and
+// rounded once; then the coefficient (b - a.x) * (omega / nrA) and the bounded
+// updates.
+template <int XM, int CACHE>
+__device__ __forceinline__ void lvl_row(const RowStep &st, const int32_t *__restrict__ col,
+                                        const double *__restrict__ val, const XAcc<XM> &X,
+                                        const Box &box, int lane, int G, int wg, FxPart *parts,
+                                        int bar) {
+    using R = typename XAcc<XM>::R;
+    constexpr int B = 4;  // chunks per batch beyond the cached ones
+    R cr[CACHE];
+    double vv[CACHE], xo[CACHE];
+    const int nq = (st.len + 31) >> 5;                      // chunks of the row
+    const int nmine = nq > wg ? (nq - wg + G - 1) / G : 0;  // this warp's chunks
+    int32_t cj[CACHE];
+#pragma unroll
+    for (int i = 0; i < CACHE; ++i) {
+        if (i >= nmine) break;
+        const int e = (wg + G * i) * 32 + lane;
+        const bool h = e < st.len;
+        cj[i] = h ? __ldg(col + st.s + e) : 0;
+        vv[i] = h ? __ldg(val + st.s + e) : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < CACHE; ++i) {
+        if (i >= nmine) break;
+        cr[i] = X.ref(cj[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < CACHE; ++i) {
+        if (i >= nmine) break;
+        xo[i] = (wg + G * i) * 32 + lane < st.len ? X.ld(cr[i]) : 0.0;
+    }
+    double p0 = 0.0, p1 = 0.0;
+#pragma unroll
+    for (int i = 0; i < CACHE; ++i) {
+        if (i >= nmine) break;
+        if (i & 1) p1 = fma(xo[i], vv[i], p1);
+        else p0 = fma(xo[i], vv[i], p0);
+    }
+    for (int i0 = CACHE; i0 < nmine; i0 += B) {
+        R tr[B];
+        bool th[B];
+        double tv[B], tx[B];
+        int32_t tj[B];
+#pragma unroll
+        for (int t = 0; t < B; ++t) {
+            const int e = (wg + G * (i0 + t)) * 32 + lane;
+            th[t] = i0 + t < nmine && e < st.len;
+            tj[t] = th[t] ? __ldg(col + st.s + e) : 0;
+            tv[t] = th[t] ? __ldg(val + st.s + e) : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < B; ++t) tr[t] = X.ref(tj[t]);
+#pragma unroll
+        for (int t = 0; t < B; ++t) tx[t] = th[t] ? X.ld(tr[t]) : 0.0;
+#pragma unroll
+        for (int t = 0; t < B; ++t) {
+            if (t & 1) p1 = fma(tx[t], tv[t], p1);
+            else p0 = fma(tx[t], tv[t], p0);
+        }
+    }
+    const FxPart part = fx_warp_part(p0, p1, (wg == 0 && lane == 0) ? -st.b : 0.0);
+    double resid;
+    if (G > 1) {
+        if (lane == 0) parts[wg] = part;
+        asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(32 * G) : "memory");
+        int E = 0;
+        for (int w = 0; w < G; ++w) E = max(E, parts[w].e);
+        if (E >= 0x7FF) {
+            resid = 0.0;
+            for (int w = 0; w < G; ++w)
+                if (parts[w].e >= 0x7FF) resid += parts[w].d;
+        } else {
+            long long t = 0;
+            for (int w = 0; w < G; ++w) {
+                const int sh = E - parts[w].e;
+                if (sh < 64) t += parts[w].s >> sh;
+            }
+            resid = fx_to_double_fast(t, E);
+        }
+    } else {
+        resid = fx_part_double(part);
+    }
+    const double c = __dmul_rn(-resid, st.w);
+#pragma unroll
+    for (int i = 0; i < CACHE; ++i) {
+        if (i >= nmine) break;
+        if ((wg + G * i) * 32 + lane < st.len) X.st(cr[i], box.apply(fma(c, vv[i], xo[i])));
+    }
+    for (int i0 = CACHE; i0 < nmine; i0 += B) {
+        R tr[B];
+        bool th[B];
+        double tv[B], tx[B];
+        int32_t tj[B];
+#pragma unroll
+        for (int t = 0; t < B; ++t) {
+            const int e = (wg + G * (i0 + t)) * 32 + lane;
+            th[t] = i0 + t < nmine && e < st.len;
+            tj[t] = th[t] ? __ldg(col + st.s + e) : 0;
+            tv[t] = th[t] ? __ldg(val + st.s + e) : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < B; ++t) tr[t] = X.ref(tj[t]);
+#pragma unroll
+        for (int t = 0; t < B; ++t) tx[t] = th[t] ? X.ld(tr[t]) : 0.0;
+#pragma unroll
+        for (int t = 0; t < B; ++t)
+            if (th[t]) X.st(tr[t], box.apply(fma(c, tv[t], tx[t])));
+    }
+}
+
+
+// The levels in order on one cluster of gridDim.x blocks (CLUSTER) or one
+// block. Groups of G consecutive warps take the steps of a level in turn; the
+// bounds of the next level and each group's first step in it are loaded one
+// level ahead, and that step's entries are prefetched into L2. With x in
+// (distributed) shared memory (XM = XS or XD, cb = log2 of a block's part), x
+// is loaded at the start and written back at the end.
+template <bool CLUSTER, int XM, int CACHE, int NT>
+__global__ void __launch_bounds__(NT, 1) k_lvl_sweep(
+        const RowStep *__restrict__ sched, const int64_t *__restrict__ lptr,
+        const int *__restrict__ nlevp, const int32_t *__restrict__ col,
+        const double *__restrict__ val, double *x, int32_t n, int cb, Box box, int G,
+        const int *__restrict__ err) {
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) double xsm[];
+    __shared__ FxPart parts[2][NW];  // per group: two rows' parts (by parity), G each
+    if (*err) return;
+    const int nlev = *nlevp;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    XAcc<XM> X;
+    int64_t part0 = 0, plen = 0;  // this block's part of x (XS: all of it)
+    if constexpr (XM == XG) {
+        X.x = x;
+    } else {
+        X.base = (uint32_t)__cvta_generic_to_shared(xsm);
+        if constexpr (XM == XD) {
+            X.cb = cb;
+            part0 = (int64_t)cluster_rank() << cb;
+            plen = (int64_t)1 << cb;
+        } else {
+            plen = n;
+        }
+        for (int64_t i = threadIdx.x; i < plen; i += NT)
+            xsm[i] = part0 + i < n ? x[part0 + i] : 0.0;
+    }
+    if (CLUSTER) cluster_barrier();
+    else __syncthreads();
+    const int gl = wid / G, wg = wid - gl * G;  // group in the block, warp in the group
+    const int64_t grp = (int64_t)blockIdx.x * (NW / G) + gl;
+    const int64_t NG = (int64_t)gridDim.x * (NW / G);
+    const int bar = 1 + gl;
+    const RowStep none{0, 0, 0, 0.0, 0.0};
+    int64_t a0 = 0, a1 = nlev > 0 ? lptr[1] : 0;
+    RowStep nxt = grp < a1 ? sched[grp] : none;
+    for (int l = 0; l < nlev; ++l) {
+        const int64_t b1 = l + 1 < nlev ? lptr[l + 2] : a1;
+        const RowStep cur = nxt;
+        nxt = a1 + grp < b1 ? sched[a1 + grp] : none;
+        int par = 0;
+        for (int64_t k = a0 + grp; k < a1; k += NG, par ^= 1)
+            lvl_row<XM, CACHE>(k == a0 + grp ? cur : sched[k], col, val, X, box, lane, G, wg,
+                               parts[par] + gl * G, bar);
+        if (nxt.len > 0) {  // the next level's first step of this group: into L2
+            const char *c0 = reinterpret_cast<const char *>(col + nxt.s);
+            const char *v0 = reinterpret_cast<const char *>(val + nxt.s);
+            const int nc = (nxt.len * 4 + 127) >> 7, nv = (nxt.len * 8 + 127) >> 7;
+            for (int i = wg * 32 + lane; i < nc + nv; i += 32 * G) {
+                const char *p = i < nc ? c0 + ((size_t)i << 7) : v0 + ((size_t)(i - nc) << 7);
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+            }
+        }
+        if (CLUSTER) cluster_barrier();
+        else __syncthreads();
+        a0 = a1;
+        a1 = b1;
+    }
+    if constexpr (XM != XG) {
+        for (int64_t i = threadIdx.x; i < plen; i += NT)
+            if (part0 + i < n) x[part0 + i] = xsm[i];
+    }
+}
+
+int env_int(const char *name, int dflt) {
+    const char *v = getenv(name);
+    return v && *v ? atoi(v) : dflt;
+}
+
+// log2 of the power-of-two part of x per block when cs blocks hold n entries
+int part_log2(int cs, int32_t n) {
+    int cb = 0;
+    while (((int64_t)cs << cb) < (int64_t)n) ++cb;
+    return cb;
+}
+
+// The cluster shape of the level sweep: the largest of 16, 8, 4, 2 blocks
+// (at most `want`) that the device can co-schedule, each with its part of x
+// in shared memory (XD: 8 << part_log2 bytes, at most `room`) or none (XG);
+// 1 if none can be had.
+template <int XM, int CACHE, int NT>
+int lvl_cluster_size(int want, int32_t n, size_t room) {
+    auto kern = k_lvl_sweep<true, XM, CACHE, NT>;
+    for (int cs = 16; cs >= 2; cs >>= 1) {
+        if (cs > want) continue;
+        const size_t smem = XM == XD ? (size_t)8 << part_log2(cs, n) : 0;
+        if (XM == XD && smem > room) continue;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            (cs > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, kern, &cfg) == cudaSuccess && nc >= 1) return cs;
+        cudaGetLastError();
+    }
+    return 1;
+}
+
+template <int XM, int CACHE, int NT>
+int lvl_launch_cluster(int cs, size_t smem, const RowStep *sched, const int64_t *lptr,
+                       const int *nlev, const int32_t *col, const double *val, double *x,
+                       int32_t n, int cb, const Box &box, int G, const int *err, cudaStream_t s) {
+    auto kern = k_lvl_sweep<true, XM, CACHE, NT>;
+    FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (cs > 8) FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    FAIR_CUDA(cudaLaunchKernelEx(&cfg, kern, sched, lptr, nlev, col, val, x, n, cb, box, G, err));
+    return FAIR_OK;
+}
+
+// Launches the level sweep: x in the distributed shared memory of a cluster
+// when its parts (a power of two per block) fit, else in global memory; one
+// block with x in its shared memory when no cluster can be had.
+// FAIR_SWEEP_CLUSTER caps the cluster size (1: one block), FAIR_SWEEP_XMEM
+// picks x's place (0: global, 1: shared/distributed).
+template <int CACHE, int NT>
+int lvl_launch(const SweepDev &S, const RowStep *sched, const int64_t *lptr, const int *nlev,
+               const Box &box, int G, const int *err, cudaStream_t s) {
+    // cluster sizes found per device, x placement and image size
+    static struct { int32_t n = -1; int want = 0, cs = 0; } cache[128][2];
+    int dev = 0, optin = 0;
+    FAIR_CUDA(cudaGetDevice(&dev));
+    FAIR_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int want = std::max(1, env_int("FAIR_SWEEP_CLUSTER", 16));
+    const bool xmem = env_int("FAIR_SWEEP_XMEM", 1) != 0;
+    const int32_t n = S.A->n;
+    const int32_t *col = S.A->col.as<int32_t>();
+    const double *val = S.A->v64.as<double>();
+    const size_t room = (size_t)optin - 8192;  // beside the static parts
+    auto cluster = [&](int xd) {
+        auto &c = cache[dev & 127][xd];
+        if (c.n != n || c.want != want) {
+            c.cs = xd ? lvl_cluster_size<XD, CACHE, NT>(want, n, room)
+                      : lvl_cluster_size<XG, CACHE, NT>(want, n, room);
+            c.n = n;
+            c.want = want;
+        }
+        return c.cs;
+    };
+    if (xmem) {
+        const int cs = cluster(1);
+        if (cs >= 2) {
+            const int cb = part_log2(cs, n);
+            return lvl_launch_cluster<XD, CACHE, NT>(cs, (size_t)8 << cb, sched, lptr, nlev, col, val,
+                                                     S.x, n, cb, box, G, err, s);
+        }
+        if ((size_t)8 * n <= room) {
+            auto kern = k_lvl_sweep<false, XS, CACHE, NT>;
+            FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(8 * (size_t)n)));
+            kern<<<1, NT, 8 * (size_t)n, s>>>(sched, lptr, nlev, col, val, S.x, n, 0, box, G, err);
+            FAIR_CUDA(cudaGetLastError());
+            return FAIR_OK;
+        }
+    }
+    const int cs = cluster(0);
+    if (cs <= 1) {
+        k_lvl_sweep<false, XG, CACHE, NT><<<1, NT, 0, s>>>(sched, lptr, nlev, col, val, S.x, n, 0,
+                                                          box, G, err);
+        FAIR_CUDA(cudaGetLastError());
+        return FAIR_OK;
+    }
+    return lvl_launch_cluster<XG, CACHE, NT>(cs, 0, sched, lptr, nlev, col, val, S.x, n, 0, box, G,
+                                             err, s);
+}
+
+// The levels on a 16-block cluster (the level table in global memory);
+// false when no such cluster can be had (FAIR_SWEEP_CLUSTER below 16 also
+// keeps the single block).
+bool lvl_levels_cluster(SweepWork &W, int32_t nord, int *nlev, cudaStream_t s) {
+    if (env_int("FAIR_SWEEP_CLUSTER", 16) < 16) return false;
+    auto kern = k_lvl_levels_cluster<16>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(512);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, kern, &cfg) != cudaSuccess || nc < 1) {
+        cudaGetLastError();
+        return false;
+    }
+    if (cudaMemsetAsync(nlev, 0, sizeof(int), s) != cudaSuccess ||
+        cudaLaunchKernelEx(&cfg, kern, (const WinRow *)W.rec.as<WinRow>(),
+                           (const signed char *)W.dpath.as<signed char>(),
+                           (const int32_t *)W.idx.as<int32_t>(), nord, W.lvtab.as<int32_t>(),
+                           W.lvl.as<int32_t>(), nlev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
+// Builds (or takes from the cache of this sweep order) the level schedule and
+// launches the level sweep. Returns FAIR_OK with *done = false (nothing
+// launched) when its buffers cannot be had; the caller then runs the
+// single-block kernel alone.
+int lvl_sweep(const SweepDev &S, int dir, const RowStep *steps, const Box &box, bool *done,
+              cudaStream_t s) {
+    *done = false;
+    SweepWork &W = *S.work;
+    const DevCSR &A = *S.A;
+    const int slot = dir > 0 ? 0 : 1;
+    SweepWork::Levels &C = W.lev[slot];
+    const bool cached = S.order_key != 0 && C.key == S.order_key && C.nord == S.nord;
+    // orders drawn anew in every sweep get no levels, only (once per call) the
+    // set-up's check for rows that repeat a column
+    const bool want = S.order_key != 0 || env_int("FAIR_SWEEP_LEVELS_ALWAYS", 0);
+    if (!want && W.err_valid) return FAIR_OK;
+    if (!cached) {
+        C.key = 0;
+        const int32_t nord = S.nord;
+        const int nwin = (nord + kWinRows - 1) / kWinRows;
+        const size_t tab_row = (size_t)std::max<int32_t>(A.n, 1) * sizeof(unsigned long long);
+        int blocks = std::min(nwin, 2 * sm_count());
+        blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)blocks, ((size_t)2 << 30) / tab_row));
+        const int64_t max_win = (int64_t)kWinRows * std::max(A.max_row, 1);
+        if (max_win >= (1 << kStampPosBits)) return FAIR_OK;
+        // the entries of this sweep: an upper bound from the longest row
+        const size_t ent = (size_t)nord * (size_t)std::max(A.max_row, 1);
+        if (W.lens.grow(4 * ((size_t)nord + 1)) || W.eoff.grow(8 * ((size_t)nord + 1)) ||
+            W.idx.grow(4 * ent) || W.rec.grow(sizeof(WinRow) * (size_t)nord) ||
+            W.dpath.grow((size_t)kWinRows * ((size_t)nord + kWinRows)) || W.lvl.grow(4 * (size_t)nord) ||
+            W.cnt.grow(4 * ((size_t)nord + 1)) || W.err.grow(sizeof(int)) ||
+            C.sched.grow(sizeof(RowStep) * (size_t)nord) || C.lptr.grow(8 * ((size_t)nord + 2)) ||
+            C.dnlev.grow(sizeof(int))) {
+            W.release();
+            return FAIR_OK;
+        }
+        if (W.tab_n != A.n || W.tab_blocks < blocks || W.uid + (uint64_t)nwin >= kStampIdLimit) {
+            W.tabs.release();
+            W.tab_n = 0;
+            W.tab_blocks = 0;
+            if (W.tabs.grow(tab_row * (size_t)blocks)) return FAIR_OK;
+            FAIR_CUDA(cudaMemsetAsync(W.tabs.p, 0xFF, tab_row * (size_t)blocks, s));
+            W.tab_n = A.n;
+            W.tab_blocks = blocks;
+            W.uid = 0;
+        }
+        int dev = 0, optin = 0;
+        FAIR_CUDA(cudaGetDevice(&dev));
+        FAIR_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const int g = (int)std::min<int64_t>((nord + 255) / 256, (int64_t)sm_count() * 4);
+        k_step_lengths<<<g, 256, 0, s>>>(steps, nord, W.lens.as<int32_t>());
+        k_scan_excl<<<1, 1024, 0, s>>>(W.lens.as<int32_t>(), nord, nullptr, W.eoff.as<int64_t>());
+        FAIR_CUDA(cudaMemsetAsync(W.err.p, 0, sizeof(int), s));
+        const size_t setup_smem = (size_t)max_win;
+        if (setup_smem + 1024 > (size_t)optin) return FAIR_OK;
+        FAIR_CUDA(cudaFuncSetAttribute(k_lvl_setup, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)setup_smem));
+        k_lvl_setup<<<blocks, kSetupThreads, setup_smem, s>>>(
+            steps, W.eoff.as<int64_t>(), nord, A.col.as<int32_t>(), W.tabs.as<unsigned long long>(),
+            A.n, W.uid, W.idx.as<int32_t>(), W.rec.as<WinRow>(), W.dpath.as<signed char>(),
+            W.err.as<int>());
+        FAIR_CUDA(cudaGetLastError());
+        W.err_valid = true;
+        W.uid += (uint64_t)nwin;
+        if (!want) return FAIR_OK;
+        const size_t lv_bytes = 4 * (size_t)std::max<int32_t>(A.n, 1);
+        if (lv_bytes + 2048 <= (size_t)optin) {
+            FAIR_CUDA(cudaFuncSetAttribute(k_lvl_levels<true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lv_bytes));
+            k_lvl_levels<true><<<1, 1024, lv_bytes, s>>>(W.rec.as<WinRow>(), W.dpath.as<signed char>(),
+                                                        W.idx.as<int32_t>(), nord, nullptr, A.n,
+                                                        W.lvl.as<int32_t>(), C.dnlev.as<int>());
+        } else {
+            if (W.lvtab.grow(lv_bytes)) {
+                W.release();
+                return FAIR_OK;
+            }
+            FAIR_CUDA(cudaMemsetAsync(W.lvtab.p, 0, lv_bytes, s));
+            if (!lvl_levels_cluster(W, nord, C.dnlev.as<int>(), s))
+                k_lvl_levels<false><<<1, 1024, 0, s>>>(W.rec.as<WinRow>(), W.dpath.as<signed char>(),
+                                                      W.idx.as<int32_t>(), nord,
+                                                      W.lvtab.as<int32_t>(), A.n,
+                                                      W.lvl.as<int32_t>(), C.dnlev.as<int>());
+        }
+        FAIR_CUDA(cudaGetLastError());
+        FAIR_CUDA(cudaMemsetAsync(W.cnt.p, 0, 4 * ((size_t)nord + 1), s));
+        k_lvl_count<<<g, 256, 0, s>>>(W.lvl.as<int32_t>(), nord, W.cnt.as<int32_t>());
+        k_scan_excl<<<1, 1024, 0, s>>>(W.cnt.as<int32_t>(), 0, C.dnlev.as<int>(), C.lptr.as<int64_t>());
+        k_lvl_scatter<<<g, 256, 0, s>>>(steps, W.lvl.as<int32_t>(), nord, C.lptr.as<int64_t>(),
+                                        W.cnt.as<int32_t>(), C.sched.as<RowStep>());
+        FAIR_CUDA(cudaGetLastError());
+        // levels pay when they hold several steps each (the ray orders: 30-80);
+        // an order whose steps nearly all depend on the one before runs on the
+        // single-block kernel
+        FAIR_CUDA(cudaMemcpyAsync(&C.nlev, C.dnlev.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FAIR_CUDA(cudaMemcpyAsync(&C.entries, W.eoff.as<int64_t>() + nord, sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, s));
+        FAIR_CUDA(cudaStreamSynchronize(s));
+        C.use = (int64_t)nord >= (int64_t)kMinStepsPerLevel * std::max(C.nlev, 1) ||
+                env_int("FAIR_SWEEP_LEVELS_ALWAYS", 0);
+        C.key = S.order_key;
+        C.nord = nord;
+    }
+    if (!C.use) return FAIR_OK;
+    const RowStep *sched = C.sched.as<RowStep>();
+    const int64_t *lptr = C.lptr.as<int64_t>();
+    const int *nlev = C.dnlev.as<int>();
+    const int *err = W.err.as<int>();
+    // warps per step: the average row in the registers of the group (4 chunks
+    // of 32 entries per warp); FAIR_SWEEP_GROUP overrides (1, 2, 4 or 8)
+    const double avg = S.nord > 0 ? (double)C.entries / S.nord : 0.0;
+    int G = 1;
+    while (G < 8 && 128.0 * G < std::min(2.0 * avg, (double)A.max_row)) G *= 2;
+    const int Ge = env_int("FAIR_SWEEP_GROUP", 0);
+    if (Ge == 1 || Ge == 2 || Ge == 4 || Ge == 8) G = Ge;
+    FAIR_TRY((lvl_launch<4, 512>(S, sched, lptr, nlev, box, G, err, s)));
+    *done = true;
+    return FAIR_OK;
+}
+
 }  // namespace
+
+void SweepWork::release() {
+    steps.release();
+    lens.release();
+    eoff.release();
+    idx.release();
+    rec.release();
+    dpath.release();
+    lvl.release();
+    cnt.release();
+    lvtab.release();
+    err.release();
+    tabs.release();
+    for (Levels &L : lev) {
+        L.sched.release();
+        L.lptr.release();
+        L.dnlev.release();
+        L.key = 0;
+        L.nord = L.nlev = 0;
+        L.entries = 0;
+        L.use = false;
+    }
+    tab_n = tab_blocks = 0;
+    uid = 0;
+    err_valid = false;
+}
 
 int kaczmarz_sweep(const SweepDev &S, int dir, cudaStream_t s) {
     if (S.nord <= 0) return FAIR_OK;
-    static thread_local DevBuf stepbuf;  // schedule of one sweep (grown on demand)
-    FAIR_TRY(stepbuf.grow(sizeof(RowStep) * (size_t)S.nord));
-    RowStep *steps = stepbuf.as<RowStep>();
+    SweepWork local;
+    SweepWork &W = S.work ? *S.work : local;
+    SweepDev SW = S;
+    SW.work = &W;
+    FAIR_TRY(W.steps.grow(sizeof(RowStep) * (size_t)S.nord));
+    RowStep *steps = W.steps.as<RowStep>();
     const DevCSR &A = *S.A;
     int grid = (int)std::min<int64_t>(((int64_t)S.nord + 255) / 256, (int64_t)sm_count() * 8);
     k_sweep_schedule<<<grid, 256, 0, s>>>(S.ord, S.nord, dir, S.rand_rowprob ? 1 : 0, S.cumul, A.m,
@@ -365,24 +1365,43 @@ int kaczmarz_sweep(const SweepDev &S, int dir, cudaStream_t s) {
     box.ub = S.ub;
     box.klb = host_key(S.lb);
     box.kub = host_key(S.ub);
+    // the level sweep, and the single-block kernel behind it for a matrix
+    // whose rows repeat a column (it runs only if the set-up said so);
+    // FAIR_SWEEP_LEGACY=1 runs the single-block kernel alone
+    bool leveled = false;
+    const int *dup = nullptr;
+    if (!env_int("FAIR_SWEEP_LEGACY", 0)) {
+        FAIR_TRY(lvl_sweep(SW, dir, steps, box, &leveled, s));
+        if (W.err_valid) dup = W.err.as<int>();
+    }
     int dev = 0, optin = 0;
     FAIR_CUDA(cudaGetDevice(&dev));
     FAIR_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const size_t need = sizeof(double) * (size_t)A.n;
     const bool smem = need + 4096 <= (size_t)optin;
-    const int W = sweep_warps();
+    const int Wl = sweep_warps();
+    const int oid = leveled ? 1 : 0;
     // entries per lane held in registers (longer rows finish in a loop)
-    const int per_lane = (A.max_row + 32 * W - 1) / (32 * W);
-    switch (W) {
-    case 1: return per_lane <= 8 ? launch<1, 8>(S, steps, smem, need, box, s)
-                                 : launch<1, 16>(S, steps, smem, need, box, s);
-    case 2: return per_lane <= 8 ? launch<2, 8>(S, steps, smem, need, box, s)
-                                 : launch<2, 16>(S, steps, smem, need, box, s);
-    case 4: return per_lane <= 4 ? launch<4, 4>(S, steps, smem, need, box, s)
-                                 : launch<4, 8>(S, steps, smem, need, box, s);
-    default: return per_lane <= 2 ? launch<8, 2>(S, steps, smem, need, box, s)
-                                  : launch<8, 4>(S, steps, smem, need, box, s);
+    const int per_lane = (A.max_row + 32 * Wl - 1) / (32 * Wl);
+    int st;
+    switch (Wl) {
+    case 1: st = per_lane <= 8 ? launch<1, 8>(SW, steps, smem, need, box, dup, oid, s)
+                               : launch<1, 16>(SW, steps, smem, need, box, dup, oid, s);
+        break;
+    case 2: st = per_lane <= 8 ? launch<2, 8>(SW, steps, smem, need, box, dup, oid, s)
+                               : launch<2, 16>(SW, steps, smem, need, box, dup, oid, s);
+        break;
+    case 4: st = per_lane <= 4 ? launch<4, 4>(SW, steps, smem, need, box, dup, oid, s)
+                               : launch<4, 8>(SW, steps, smem, need, box, dup, oid, s);
+        break;
+    default: st = per_lane <= 2 ? launch<8, 2>(SW, steps, smem, need, box, dup, oid, s)
+                                : launch<8, 4>(SW, steps, smem, need, box, dup, oid, s);
     }
+    if (!S.work) {
+        cudaStreamSynchronize(s);
+        local.release();
+    }
+    return st;
 }
 
 }  // namespace fair

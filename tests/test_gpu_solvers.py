@@ -161,8 +161,10 @@ def test_art_order_damp_xref(par, fair, oracle):
 
 @pytest.mark.parametrize("warps", ["1", "2", "4", "8"])
 def test_art_sweep_warps(par, fair, oracle, monkeypatch, warps):
-    """Every warps-per-row choice of the sweep: the row sums of 1 to 8 warps
-    (exact integer sums of the lanes' FP64 partials) against the oracle."""
+    """Every warps-per-row choice of the single-block sweep: the row sums of 1
+    to 8 warps (exact integer sums of the lanes' FP64 partials) against the
+    oracle."""
+    monkeypatch.setenv("FAIR_SWEEP_LEGACY", "1")
     monkeypatch.setenv("FAIR_SWEEP_WARPS", warps)
     A, R, _, b = par
     o = fair.airms.options(relaxpar=0.25, lbound=0.0, ubound=1.0)
@@ -172,11 +174,14 @@ def test_art_sweep_warps(par, fair, oracle, monkeypatch, warps):
     assert rel_err(X, Xr) < TOL64
 
 
-@pytest.mark.parametrize("warps", ["2", "8"])
+@pytest.mark.parametrize("warps", ["window", "2", "8"])
 def test_art_iterate_in_global_memory(fair, oracle, monkeypatch, warps):
-    """N=192 (36,864 unknowns: more than one block's shared memory holds), so the
+    """N=192 (36,864 unknowns: more than one block's shared memory holds): the
+    windowed sweep keeps each window's columns in slots, the single-block
     sweep gathers the iterate from global memory."""
-    monkeypatch.setenv("FAIR_SWEEP_WARPS", warps)
+    if warps != "window":
+        monkeypatch.setenv("FAIR_SWEEP_LEGACY", "1")
+        monkeypatch.setenv("FAIR_SWEEP_WARPS", warps)
     n, nth, p = 192, 24, 272
     th = oracle.linspace(0.0, np.pi, nth)
     A = fair.paralleltomo(fair.Data(n=n, p=p, nth=nth, theta=th))
