@@ -524,7 +524,7 @@ SECONDARY = [  # (name, extra arguments, time limit in s): the other workloads o
     ("kaczmarz", ["--workload", "kaczmarz", "--no-cpu"], 300),
     ("adjoint", ["--workload", "adjoint", "--no-cpu"], 300),
     ("batch", ["--workload", "batch", "--batch-layout", "auto", "--no-cpu"], 600),
-    ("mfree", ["--workload", "mfree", "--mf-sizes", "2048"], 600),
+    ("mfree", ["--workload", "mfree", "--mf-sizes", "2048,fan"], 600),
 ]
 
 
@@ -552,18 +552,21 @@ def run_secondary(args):
 def run_kaczmarz(args):
     """Kaczmarz family (a secondary measurement, one JSON line per case):
     fan beam N=512, 720 angles over [0, 2pi), 725 unit bins, R = 2N, three-phase
-    phantom, bounds [0,1], FP64: random Kaczmarz with row-norm probabilities
-    and symmetric Kaczmarz; and fan beam N=128, 360 angles, 181 bins, 10
-    natural-order sweeps with relaxation 0.25. Rows/s and sweeps/s through the
-    host C-ABI call (b in, x out), beside the oracle's serial sweep on one core
-    (the reference's sweep is serial)."""
+    phantom, bounds [0,1], FP64, 20 sweeps: random Kaczmarz with row-norm
+    probabilities and symmetric Kaczmarz; and fan beam N=128, 360 angles, 181
+    bins, 10 natural-order sweeps with relaxation 0.25. Rows/s and sweeps/s
+    through the host C-ABI call (b in, x out; the call's level schedules are
+    built inside it), beside the oracle's serial sweep on one core (the
+    reference's sweep is serial)."""
     import fortran_airtools_gb300 as F
     from oracle import oracle as O
     cases = [
-        ("randkaczmarz", dict(n=512, nth=720, p=725), dict(rowprobability=True, lbound=0.0, ubound=1.0), 2),
-        ("symkaczmarz", dict(n=512, nth=720, p=725), dict(lbound=0.0, ubound=1.0), 2),
+        ("randkaczmarz", dict(n=512, nth=720, p=725), dict(rowprobability=True, lbound=0.0, ubound=1.0), 20),
+        ("symkaczmarz", dict(n=512, nth=720, p=725), dict(lbound=0.0, ubound=1.0), 20),
         ("kaczmarz", dict(n=128, nth=360, p=181), dict(relaxpar=0.25), 10),
     ]
+    if args.kacz_cases:
+        cases = [c for c in cases if c[0] in args.kacz_cases.split(",")]
     for method, g, o, sweeps in cases:
         th = 2 * np.pi * np.arange(g["nth"]) / g["nth"]
         d = F.Data(n=g["n"], p=g["p"], nth=g["nth"], r=2.0, dw=g["p"] / g["n"], sd=2.0, theta=th)
@@ -878,6 +881,8 @@ def run_mfree(args):
             A.close()
         res["geometry"] = f"parallel beam N={n}, {nth} angles over [0,pi), {p} bins"
         out[f"N={n}"] = res
+    if not args.mf_sizes or "fan" in args.mf_sizes.split(","):
+        out["fan N=512"] = mfree_fan_case(F, K, stream)
     big = out.get("N=2048") or next(iter(out.values()))
     line = {"metric": "matrix-free SIRT iter/s (Cimmino, FP32)",
             "workload": big["geometry"],
@@ -890,6 +895,66 @@ def run_mfree(args):
             "gpu_launches": 1 + 2 * K}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def mfree_fan_case(F, K, stream):
+    """The fan-beam pair on the Kaczmarz workload's geometry (fan N=512, 720
+    angles over [0, 2pi), 725 bins, R = 2N): K FP32 Cimmino iterations on the
+    matrix-free pair and on the stored matrix (FP32, autotuned), the iterates
+    compared with each other."""
+    import ctypes as C
+
+    import torch
+
+    from fortran_airtools_gb300._clib import check, lib
+    n, nth, p = 512, 720, 725
+    th = 2 * np.pi * np.arange(nth) / nth
+    d = F.Data(n=n, p=p, nth=nth, r=2.0, dw=p / n, sd=2.0, theta=th)
+    M = F.MatrixFree(d, "f32", beam="fan")
+    b = noisy(M.project(F.phantomgallery.shepplogan(n)))
+    M.set_stream(stream.cuda_stream)
+    opts = F.airms.options()
+    M.prepare("cimmino", opts)
+    d_b = torch.from_numpy(b).cuda()
+    d_x = torch.zeros(M.n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    M.run_device(d_b.data_ptr(), d_x.data_ptr(), 3)  # warm-up
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(run):
+        with torch.cuda.stream(stream):
+            d_x.zero_()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run(K)
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1), d_x.cpu().numpy()
+
+    ms_mf, x_mf = timed(lambda k: M.run_device(d_b.data_ptr(), d_x.data_ptr(), k))
+    with torch.cuda.stream(stream):
+        d_x.zero_()
+    stream.synchronize()
+    t1, t2 = M.run_device_timed(d_b.data_ptr(), d_x.data_ptr(), 3)
+    nnz = M.nnz()
+    M.close()
+    A = F.fanlineartomo(d)
+    A.set_stream(stream.cuda_stream)
+    A.set_precision("f32")
+    L = lib()
+    check(L.fair_sirt_prepare(A.handle, b"cimmino", C.byref(opts)))
+    cfg = (C.c_int32 * 4)()
+    check(L.fair_sirt_autotune(A.handle, d_b.data_ptr(), d_x.data_ptr(), 3, cfg))
+    ms_st, x_st = timed(lambda k: check(L.fair_sirt_run_device(A.handle, d_b.data_ptr(),
+                                                                 d_x.data_ptr(), k)))
+    A.close()
+    return {"geometry": f"fan beam N={n}, {nth} angles over [0,2pi), {p} bins, R=2N",
+            "iter_per_s": K / (ms_mf / 1e3), "ms_per_iteration": ms_mf / K,
+            "project_ms": t1 / 3, "backproject_ms": t2 / 3, "nnz": nnz,
+            "stored_f32": {"iter_per_s": K / (ms_st / 1e3), "ms_per_iteration": ms_st / K,
+                           "pass_config": list(cfg)},
+            "rel_err_vs_stored": float(np.linalg.norm(x_mf - x_st) / np.linalg.norm(x_st))}
 
 
 def stored_f32_arm(args, F, d, b, x_mf, K, stream, d_b, d_x):
@@ -986,10 +1051,13 @@ def main():
                     help="batch layouts timed, one line each (comma list of auto, tiled, packed)")
     ap.add_argument("--no-secondary", action="store_true",
                     help="headline only: skip the secondary workloads run after it")
+    ap.add_argument("--kacz-cases", default="",
+                    help="kaczmarz workload: cases to run (comma list of randkaczmarz, "
+                         "symkaczmarz, kaczmarz; default all)")
     ap.add_argument("--no-stored", action="store_true",
                     help="mfree workload: skip the stored FP32 arm at N=2048")
     ap.add_argument("--mf-sizes", default="",
-                    help="matrix-free cases to run, by N (comma list of 2048, 1024; default both)")
+                    help="matrix-free cases to run (comma list of 2048, 1024, fan; default all)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

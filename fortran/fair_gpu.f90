@@ -460,13 +460,19 @@ module fair_gpu
        integer(c_int32_t), intent(in) :: config(*)
      end function fair_batch_set_config
 
-     ! ---- fair_mf.h: matrix-free parallel-beam operator ---------------------
+     ! ---- fair_mf.h: matrix-free parallel- and fan-beam operators -----------
      integer(c_int) function fair_mf_create_parallel(out, dat, prec) bind(C, name="fair_mf_create_parallel")
        import :: c_int, c_ptr, c_int32_t, fair_data
        type(c_ptr), intent(out) :: out
        type(fair_data), intent(in) :: dat
        integer(c_int32_t), value :: prec
      end function fair_mf_create_parallel
+     integer(c_int) function fair_mf_create_fan(out, dat, geometry_fix, prec) bind(C, name="fair_mf_create_fan")
+       import :: c_int, c_ptr, c_int32_t, fair_data
+       type(c_ptr), intent(out) :: out
+       type(fair_data), intent(in) :: dat
+       integer(c_int32_t), value :: geometry_fix, prec
+     end function fair_mf_create_fan
      integer(c_int) function fair_mf_destroy(A) bind(C, name="fair_mf_destroy")
        import :: c_int, c_ptr
        type(c_ptr), value :: A

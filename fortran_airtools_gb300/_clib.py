@@ -149,6 +149,7 @@ def _declare(L):
         "fair_phantom_device": ([C.c_char_p, i32, vp, vp], C.c_int),
         "fair_add_white_noise_device": ([vp, vp, vp, i64, d, vp], C.c_int),
         "fair_mf_create_parallel": ([P(h), P(Data), i32], C.c_int),
+        "fair_mf_create_fan": ([P(h), P(Data), i32, i32], C.c_int),
         "fair_mf_destroy": ([h], C.c_int),
         "fair_mf_set_stream": ([h, vp], C.c_int),
         "fair_mf_info": ([h, P(i32), P(i32)], C.c_int),

@@ -187,7 +187,7 @@ struct ClassChoice {
 // One problem of a batch.
 struct BatchProb {
     DevCSR A, AT;
-    DevBuf M_sart, M_cim, D;  // FP64 weights: row 1-norms, m*|a_i|^2, column 1-norms
+    DevBuf M_sart, M_cim, D;  // FP64 reciprocal weights: 1/row 1-norms, 1/(m*|a_i|^2), 1/column 1-norms
     bool tiled = false;       // passes on the tiled copies of A and A' (else packed / CSR)
     void release() {
         A.release(); AT.release();
@@ -558,8 +558,8 @@ int finish_problem(fair_batch_s *B, BatchProb &q) {
     FAIR_TRY(q.M_sart.grow(sizeof(double) * ((size_t)q.A.m + 1)));
     FAIR_TRY(q.M_cim.grow(sizeof(double) * ((size_t)q.A.m + 1)));
     FAIR_TRY(q.D.grow(sizeof(double) * ((size_t)q.A.n + 1)));
-    FAIR_TRY(sirt_weights(q.A, q.AT, true, q.M_sart.as<double>(), q.D.as<double>(), s));
-    FAIR_TRY(sirt_weights(q.A, q.AT, false, q.M_cim.as<double>(), nullptr, s));
+    FAIR_TRY(sirt_weights_recip(q.A, q.AT, true, q.M_sart.as<double>(), q.D.as<double>(), s));
+    FAIR_TRY(sirt_weights_recip(q.A, q.AT, false, q.M_cim.as<double>(), nullptr, s));
     bool want_tiled = B->layout == 1;
     if (B->layout == 2) {  // the class's choice, timed on its first problem
         const std::pair<int64_t, int64_t> key{q.A.n, q.A.tstride_hint};

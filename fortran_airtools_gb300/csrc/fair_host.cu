@@ -704,7 +704,7 @@ int fair_sirt(double *xout, const char *sirt_method, fair_csr h, const double *b
     FAIR_TRY(h->w_D.grow(sizeof(double) * ((size_t)n + 1)));
     FAIR_TRY(h->w_r.grow(sizeof(double) * ((size_t)m + 1)));
     FAIR_TRY(h->w_x32.grow(sizeof(float) * ((size_t)n + 1)));
-    FAIR_TRY(sirt_weights(h->A, h->AT, sart, h->w_M.as<double>(), h->w_D.as<double>(), s));
+    FAIR_TRY(sirt_weights_recip(h->A, h->AT, sart, h->w_M.as<double>(), h->w_D.as<double>(), s));
     SirtDev S;
     S.prec = h->prec;
     S.m = m; S.n = n;
@@ -1193,7 +1193,7 @@ int fair_sirt_prepare(fair_csr h, const char *sirt_method, const fair_opts *opti
     FAIR_TRY(h->s_D.grow(sizeof(double) * ((size_t)n + 1)));
     FAIR_TRY(h->s_r.grow(sizeof(double) * ((size_t)m + 1)));
     FAIR_TRY(h->s_x32.grow(sizeof(float) * ((size_t)n + 1)));
-    FAIR_TRY(sirt_weights(h->A, h->AT, sart, h->s_M.as<double>(), h->s_D.as<double>(), s));
+    FAIR_TRY(sirt_weights_recip(h->A, h->AT, sart, h->s_M.as<double>(), h->s_D.as<double>(), s));
     FAIR_TRY(sirt_make_forms(h->A, h->AT, h->prec, s));
     FAIR_CUDA(cudaStreamSynchronize(s));
     h->sirt_sart = sart;

@@ -232,8 +232,8 @@ struct SirtDev {
     int32_t m = 0, n = 0;
     const DevCSR *A = nullptr, *AT = nullptr;
     const double *b = nullptr;   // m
-    const double *Minv = nullptr;  // m: M diag (weights, FP64)
-    const double *D = nullptr;   // n: D diag (FP64; nullptr = 1)
+    const double *Minv = nullptr;  // m: 1/M, reciprocal row weights (FP64)
+    const double *D = nullptr;   // n: 1/D, reciprocal column weights (FP64; nullptr: D = 1)
     double *x = nullptr;         // n, FP64 master iterate
     float *x32 = nullptr;        // n, FP32 shadow (F32/F16)
     void *r = nullptr;           // m residual (double or float)
@@ -244,6 +244,12 @@ struct SirtDev {
 };
 int sirt_weights(const DevCSR &A, const DevCSR &AT, bool sart, double *d_M, double *d_D,
                  cudaStream_t s);
+// The same weights stored as reciprocals 1/M, 1/D: what the SIRT epilogues
+// (sirt_epi.cuh) multiply by.
+int sirt_weights_recip(const DevCSR &A, const DevCSR &AT, bool sart, double *d_Mi, double *d_Di,
+                       cudaStream_t s);
+// v = 1/v elementwise (IEEE: 1/0 = Inf, 1/Inf = 0).
+int vec_reciprocal(double *v, int64_t n, cudaStream_t s);
 int sirt_iterations(const SirtDev &S, int K, cudaStream_t s);
 // One SIRT pass (1: residual over A, 2: update over A') with the forms
 // already made; enqueues one kernel.
@@ -267,9 +273,9 @@ bool sirt_pass_tiled(const SirtDev &S, const DevCSR &M, int pass, int code, cuda
 struct TlBatchProb {
     const DevCSR *M;          // A (pass 1) or A' (pass 2), its tiled copy built
     const void *xin;          // the gathered vector: x32 or x (pass 1), r (pass 2)
-    const double *b, *Minv;   // pass 1: r = (b - A x) / M
+    const double *b, *Minv;   // pass 1: r = (b - A x) / M, Minv = 1/M
     void *r;
-    const double *D;          // pass 2: x = P(x + omega A'r / D); null: D = 1
+    const double *D;          // pass 2: x = P(x + omega A'r / D), D here 1/D; null: D = 1
     double *x;
     float *x32;
 };

@@ -1,5 +1,5 @@
-// mfree.cu -- matrix-free parallel-beam projector / backprojector pair and
-// SIRT on it (include/fair_mf.h).
+// mfree.cu -- matrix-free projector / backprojector pairs (parallel beam and
+// fan beam) and SIRT on them (include/fair_mf.h).
 //
 // Geometry of paralleltomo (system_generation.f90:309-492): ray (angle i,
 // bin j) is the line with unit normal n_i = (cos th_i, sin th_i) at offset
@@ -29,6 +29,18 @@
 // thread per pixel and, per angle, the 1-3 rays whose offsets bracket the
 // pixel's. Both keep only pairs with L > 0, so they sum the same entries: an
 // exact adjoint pair, deterministic, without atomics.
+//
+// Fan beam (fanlineartomo, system_generation.f90:79-307): ray (i, j) is the
+// line through the rotated source P_i with direction u_ij = R(omega_j) u0_i,
+// computed on the host exactly as the reference does (cos/sin of the bin
+// angles, the same products and sums). Its unit normal n = (b, -a)/|u| and
+// K_ij = n . ((1/2 - N/2, 1/2 - N/2) - P_i) give d = ix*n_x + iy*n_y + K_ij,
+// the same fixed-point form, one record per ray. The projector walks each ray
+// as above; the backprojector finds, per pixel and angle, the rays whose bin
+// angle omega_j lies within asin(0.7072/|c - P_i|) (+ 2e-4) of the angle of
+// the pixel centre c seen from the source (a binary search over the bin
+// angles, sorted once: the reference's odd-p angles are not monotone in j),
+// and tests them with the exact distance.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -117,7 +129,9 @@ struct EpiCimminoW {  // M = m * sum_j a_ij^2 (the sum arrives in acc)
 
 // Per ray r: MODE 0 sums a_rj * x_j, MODE 1 sums a_rj, MODE 2 sums a_rj^2,
 // MODE 3 counts the pixels with a_rj > 0 (x unused for MODE 1-3).
-template <typename XT, typename ACC, int MODE, class Epi>
+// FAN: ang holds one record per ray (K its own offset), else one per angle
+// (ray j of angle i at offset K - j).
+template <typename XT, typename ACC, int MODE, bool FAN, class Epi>
 __global__ void __launch_bounds__(128) k_mf_project(const MfAngle *__restrict__ ang, int nth,
                                                     int p, int N, const XT *__restrict__ x,
                                                     Epi epi) {
@@ -125,9 +139,9 @@ __global__ void __launch_bounds__(128) k_mf_project(const MfAngle *__restrict__ 
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m;
          r += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(r / p), j = (int)(r - (int64_t)i * p);
-        const MfAngle A = ang[i];
-        const long long K = A.K - ((long long)j << kFix);
-        const float Kf = A.Kf - (float)j;
+        const MfAngle A = ang[FAN ? r : i];
+        const long long K = FAN ? A.K : A.K - ((long long)j << kFix);
+        const float Kf = FAN ? A.Kf : A.Kf - (float)j;
         ACC acc = 0;
         // walk the faster axis: d = t*F + u*Q + K with t the walked index
         const long long F = A.by_column ? A.C : A.S, Q = A.by_column ? A.S : A.C;
@@ -202,6 +216,70 @@ __global__ void __launch_bounds__(128) k_mf_backproject(const MfAngle *__restric
     }
 }
 
+// Per angle of a fan: the source P and the unit direction u0 towards the
+// origin (floats, for the candidate search only).
+struct MfFanAngle {
+    float px, py, ux, uy;
+};
+
+// The rays of angle i through pixel (ix, iy): bin angles within the pixel's
+// angular half-width of its centre's angle from the source (oms sorted, omj
+// their bins), each tested with the exact fixed-point distance.
+template <typename YT, typename ACC, int MODE>
+__device__ __forceinline__ void bp_fan_rays(const MfAngle *__restrict__ rays, const MfFanAngle &F,
+                                            const float *__restrict__ oms,
+                                            const int *__restrict__ omj, int i, int p, int ix,
+                                            int iy, float cx, float cy, const YT *__restrict__ y,
+                                            ACC &acc) {
+    const float vx = cx - F.px, vy = cy - F.py;
+    const float al = atan2f(fmaf(F.ux, vy, -F.uy * vx), fmaf(F.ux, vx, F.uy * vy));
+    const float de = asinf(fminf(1.f, 0.7072f * rsqrtf(fmaf(vx, vx, vy * vy)))) + 2e-4f;
+    const float lo = al - de, hi = al + de;
+    int a = 0, b = p;  // first k with oms[k] >= lo
+    while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (__ldg(oms + mid) < lo) a = mid + 1;
+        else b = mid;
+    }
+    for (int k = a; k < p && __ldg(oms + k) <= hi; ++k) {
+        const int j = __ldg(omj + k);
+        const int64_t r = (int64_t)i * p + j;
+        const MfAngle &A = rays[r];
+        const long long d = (long long)ix * A.C + (long long)iy * A.S + A.K;
+        const ACC w = Chord<ACC>::of(A, d);
+        if (w > (ACC)0) {
+            if (MODE == 0) acc += w * (ACC)__ldg(y + r);
+            else acc += w;
+        }
+    }
+}
+
+template <typename YT, typename ACC, int MODE, class Epi>
+__global__ void __launch_bounds__(128) k_mf_backproject_fan(
+        const MfAngle *__restrict__ rays, const MfFanAngle *__restrict__ fa,
+        const float *__restrict__ oms, const int *__restrict__ omj, int nth, int p, int N,
+        const YT *__restrict__ y, Epi epi) {
+    const int half = (N + 1) / 2;  // pixel pairs per image column
+    const int64_t npairs = (int64_t)N * half;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < npairs;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(t / half), k = (int)(t - (int64_t)ix * half);
+        const int iy0 = N - 1 - 2 * k;  // pixel q0 = ix*N + 2k
+        const bool two = iy0 >= 1;      // and q0 + 1 (iy0 - 1) when it exists
+        const float cx = (float)ix + 0.5f - 0.5f * (float)N;
+        const float cy0 = (float)iy0 + 0.5f - 0.5f * (float)N;
+        ACC acc0 = 0, acc1 = 0;
+        for (int i = 0; i < nth; ++i) {
+            const MfFanAngle F = fa[i];
+            bp_fan_rays<YT, ACC, MODE>(rays, F, oms, omj, i, p, ix, iy0, cx, cy0, y, acc0);
+            if (two) bp_fan_rays<YT, ACC, MODE>(rays, F, oms, omj, i, p, ix, iy0 - 1, cx, cy0 - 1.f, y, acc1);
+        }
+        const int64_t q0 = (int64_t)ix * N + 2 * k;
+        epi(q0, acc0);
+        if (two) epi(q0 + 1, acc1);
+    }
+}
+
 int grid_for(int64_t items, int threads) {
     int64_t b = (items + threads - 1) / threads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm_count() * 32));
@@ -216,7 +294,9 @@ struct fair_mf_s {
     bool own_stream = false;
     int prec = FAIR_PREC_F32;
     int N = 0, p = 0, nth = 0;
-    fair::DevBuf ang;                  // MfAngle [nth]
+    int kind = 0;                      // 0: parallel beam, 1: fan beam
+    fair::DevBuf ang;                  // MfAngle [nth] (parallel) or [nth*p] (fan: per ray)
+    fair::DevBuf fang, oms, omj;       // fan: MfFanAngle [nth], sorted bin angles, their bins
     fair::DevBuf w_in, w_out;          // host-call staging (FP64)
     fair::DevBuf v_a, v_b;             // reduced-precision staging
     // SIRT state
@@ -232,27 +312,49 @@ struct fair_mf_s {
 namespace fair {
 namespace {
 
+// Projector / backprojector launches of either geometry.
+template <typename XT, typename ACC, int MODE, class Epi>
+void mf_project(fair_mf A, const XT *x, Epi epi, cudaStream_t s) {
+    const int64_t m = (int64_t)A->nth * A->p;
+    const MfAngle *ang = A->ang.as<MfAngle>();
+    if (A->kind == 1)
+        k_mf_project<XT, ACC, MODE, true><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N, x, epi);
+    else
+        k_mf_project<XT, ACC, MODE, false><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N, x, epi);
+}
+template <typename YT, typename ACC, int MODE, class Epi>
+void mf_backproject(fair_mf A, const YT *y, Epi epi, cudaStream_t s) {
+    const int64_t n = (int64_t)A->N * A->N;
+    const MfAngle *ang = A->ang.as<MfAngle>();
+    if (A->kind == 1)
+        k_mf_backproject_fan<YT, ACC, MODE><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
+            ang, A->fang.as<MfFanAngle>(), A->oms.as<float>(), A->omj.as<int>(), A->nth, A->p,
+            A->N, y, epi);
+    else
+        k_mf_backproject<YT, ACC, MODE><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(ang, A->nth, A->p,
+                                                                               A->N, y, epi);
+}
+
 int mf_weights(fair_mf A, bool sart, cudaStream_t s) {
     const int64_t m = (int64_t)A->nth * A->p, n = (int64_t)A->N * A->N;
-    const MfAngle *ang = A->ang.as<MfAngle>();
     if (sart && !A->have_sart) {
         FAIR_TRY(A->M_sart.grow(sizeof(double) * (m + 1)));
         FAIR_TRY(A->D.grow(sizeof(double) * (n + 1)));
         EpiStore<double> e1{A->M_sart.as<double>()};
-        k_mf_project<double, double, 1><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N,
-                                                                          nullptr, e1);
+        mf_project<double, double, 1>(A, (const double *)nullptr, e1, s);
         EpiStore<double> e2{A->D.as<double>()};
-        k_mf_backproject<double, double, 1><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
-            ang, A->nth, A->p, A->N, nullptr, e2);
+        mf_backproject<double, double, 1>(A, (const double *)nullptr, e2, s);
         FAIR_CUDA(cudaGetLastError());
+        FAIR_TRY(vec_reciprocal(A->M_sart.as<double>(), m, s));  // the epilogues multiply
+        FAIR_TRY(vec_reciprocal(A->D.as<double>(), n, s));
         A->have_sart = true;
     }
     if (!sart && !A->have_cim) {
         FAIR_TRY(A->M_cim.grow(sizeof(double) * (m + 1)));
         EpiCimminoW e{A->M_cim.as<double>(), (double)m};
-        k_mf_project<double, double, 2><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N,
-                                                                          nullptr, e);
+        mf_project<double, double, 2>(A, (const double *)nullptr, e, s);
         FAIR_CUDA(cudaGetLastError());
+        FAIR_TRY(vec_reciprocal(A->M_cim.as<double>(), m, s));
         A->have_cim = true;
     }
     return FAIR_OK;
@@ -260,29 +362,23 @@ int mf_weights(fair_mf A, bool sart, cudaStream_t s) {
 
 // One projector / backprojector pass of a SIRT iteration.
 void mf_pass(fair_mf A, int pass, const double *d_b, double *d_x, cudaStream_t s) {
-    const int64_t m = (int64_t)A->nth * A->p, n = (int64_t)A->N * A->N;
-    const MfAngle *ang = A->ang.as<MfAngle>();
     const double *M = A->sart ? A->M_sart.as<double>() : A->M_cim.as<double>();
     const double *D = A->sart ? A->D.as<double>() : nullptr;
     if (A->prec == FAIR_PREC_F64) {
         if (pass == 1) {
             EpiResidF64 e{d_b, M, A->r.as<double>()};
-            k_mf_project<double, double, 0><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p,
-                                                                              A->N, d_x, e);
+            mf_project<double, double, 0>(A, (const double *)d_x, e, s);
         } else {
             EpiUpdateF64 e{D, d_x, A->omg, A->lb, A->ub, A->bmode};
-            k_mf_backproject<double, double, 0><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
-                ang, A->nth, A->p, A->N, A->r.as<double>(), e);
+            mf_backproject<double, double, 0>(A, (const double *)A->r.as<double>(), e, s);
         }
     } else {
         if (pass == 1) {
             EpiResidLP e{d_b, M, A->r.as<float>(), 1.0};
-            k_mf_project<float, float, 0><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N,
-                                                                            A->x32.as<float>(), e);
+            mf_project<float, float, 0>(A, (const float *)A->x32.as<float>(), e, s);
         } else {
             EpiUpdateLP e{D, d_x, A->x32.as<float>(), A->omg, A->lb, A->ub, A->bmode, 1.0};
-            k_mf_backproject<float, float, 0><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
-                ang, A->nth, A->p, A->N, A->r.as<float>(), e);
+            mf_backproject<float, float, 0>(A, (const float *)A->r.as<float>(), e, s);
         }
     }
 }
@@ -298,24 +394,62 @@ void mf_pass(fair_mf A, int pass, const double *d_b, double *d_x, cudaStream_t s
 
 extern "C" {
 
-int fair_mf_create_parallel(fair_mf *out, const fair_data *dat, int32_t prec) {
+}  // extern "C"
+
+namespace fair {
+namespace {
+
+// The constants of the line with unit normal (C, S) and d = ix*C + iy*S + K
+// for pixel (ix, iy): fixed-point terms, chord thresholds, walk axis, floats.
+void mf_line(double C, double S, double K, MfAngle &a) {
+    const double c = std::max(fabs(C), fabs(S)), s = std::min(fabs(C), fabs(S));
+    a.C = llround(C * kOne);
+    a.S = llround(S * kOne);
+    a.K = llround(K * kOne);
+    a.H1 = llround(0.5 * (c - s) * kOne);
+    a.H2 = llround(0.5 * (c + s) * kOne);
+    a.Cf = (float)C;
+    a.Sf = (float)S;
+    a.Kf = (float)K;
+    a.by_column = fabs(S) >= fabs(C) ? 1 : 0;
+    a.inv_fast = (float)(1.0 / (a.by_column ? S : C));
+    a.inv_c = (float)(1.0 / c);
+    a.inv_c64 = 1.0 / c;
+    a.scale_ramp = s > 0 ? (float)(2.0 / (kOne * c * s)) : 0.f;
+    a.scale_ramp64 = s > 0 ? 1.0 / (kOne * c * s) : 0.0;
+    a.tie = 0;
+    if (a.S == 0) a.tie = C > 0 ? 1 : -1;        // vertical ray, normal (+-1, 0)
+    else if (a.C == 0) a.tie = S > 0 ? 1 : -1;   // horizontal ray, normal (0, +-1)
+    if (a.tie != 0) a.H1 = a.H2;                 // s = 0: no ramp
+    // segments of 1e-10 or less are dropped, as the ray tracer does
+    // (system_generation.f90:393-394)
+    a.Hcut = a.tie != 0 ? a.H2 : a.H2 - (long long)floor(1e-10 * c * s * kOne);
+    a.H1s = (int)(a.H1 >> 16);
+    a.H2s = (int)(a.H2 >> 16);
+    a.Hcuts = (int)(a.Hcut >> 16);
+    if (a.tie == 0 && a.Hcuts >= a.H2s) a.Hcuts = a.H2s;  // s > 0: the ramp ends at H2s
+    a.scale_ramp30 = s > 0 ? (float)(1.0 / (1073741824.0 * c * s)) : 0.f;
+}
+
+// A new operator handle with its own stream, or a status.
+int mf_new(fair_mf *out, const fair_data *dat, int32_t prec, int kind) {
     if (!out || !dat || !dat->theta) return FAIR_ERR_NULL;
     *out = nullptr;
     if (prec != FAIR_PREC_F64 && prec != FAIR_PREC_F32) {
-        fair::set_detail("the matrix-free operator runs in FP64 or FP32");
+        set_detail("the matrix-free operator runs in FP64 or FP32");
         return FAIR_ERR_ARG;
     }
     const int N = dat->n, p = dat->p, nth = dat->nth;
-    if (N < 1 || p < 2 || nth < 1) { fair::set_detail("n >= 1, p >= 2, nth >= 1 required"); return FAIR_ERR_ARG; }
+    if (N < 1 || p < 2 || nth < 1) { set_detail("n >= 1, p >= 2, nth >= 1 required"); return FAIR_ERR_ARG; }
     if ((int64_t)nth * p > INT32_MAX || N > 8192 || p > 16384) {
-        fair::set_detail("the matrix-free operator needs n <= 8192, p <= 16384, nth*p < 2^31");
+        set_detail("the matrix-free operator needs n <= 8192, p <= 16384, nth*p < 2^31");
         return FAIR_ERR_ARG;
     }
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) {
         cudaGetLastError();
-        fair::set_detail(e != cudaSuccess ? cudaGetErrorString(e) : "no CUDA device");
+        set_detail(e != cudaSuccess ? cudaGetErrorString(e) : "no CUDA device");
         return FAIR_ERR_NOGPU;
     }
     fair_mf A = new (std::nothrow) fair_mf_s();
@@ -325,53 +459,111 @@ int fair_mf_create_parallel(fair_mf *out, const fair_data *dat, int32_t prec) {
     A->N = N;
     A->p = p;
     A->nth = nth;
+    A->kind = kind;
     e = cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete A;
-        return fair::cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+        return cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
     }
     A->own_stream = true;
+    *out = A;
+    return FAIR_OK;
+}
+
+template <typename T>
+int mf_upload(DevBuf &d, const std::vector<T> &v) {
+    if (d.grow(sizeof(T) * std::max<size_t>(v.size(), 1)) != FAIR_OK) return FAIR_ERR_ALLOC;
+    if (cudaMemcpy(d.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        return FAIR_ERR_ALLOC;
+    }
+    return FAIR_OK;
+}
+
+}  // namespace
+}  // namespace fair
+
+extern "C" {
+
+int fair_mf_create_parallel(fair_mf *out, const fair_data *dat, int32_t prec) {
+    FAIR_TRY(fair::mf_new(out, dat, prec, 0));
+    fair_mf A = *out;
+    const int N = dat->n, p = dat->p, nth = dat->nth;
     // per-angle constants (cos/sin from the host libm, as paralleltomo)
     std::vector<fair::MfAngle> t(nth);
     for (int i = 0; i < nth; ++i) {
         const double C = cos(dat->theta[i]), S = sin(dat->theta[i]);
         const double K = (0.5 - 0.5 * N) * (C + S) + 0.5 * (p - 1);
-        const double c = std::max(fabs(C), fabs(S)), s = std::min(fabs(C), fabs(S));
-        fair::MfAngle &a = t[i];
-        a.C = llround(C * fair::kOne);
-        a.S = llround(S * fair::kOne);
-        a.K = llround(K * fair::kOne);
-        a.H1 = llround(0.5 * (c - s) * fair::kOne);
-        a.H2 = llround(0.5 * (c + s) * fair::kOne);
-        a.Cf = (float)C;
-        a.Sf = (float)S;
-        a.Kf = (float)K;
-        a.by_column = fabs(S) >= fabs(C) ? 1 : 0;
-        a.inv_fast = (float)(1.0 / (a.by_column ? S : C));
-        a.inv_c = (float)(1.0 / c);
-        a.inv_c64 = 1.0 / c;
-        a.scale_ramp = s > 0 ? (float)(2.0 / (fair::kOne * c * s)) : 0.f;
-        a.scale_ramp64 = s > 0 ? 1.0 / (fair::kOne * c * s) : 0.0;
-        a.tie = 0;
-        if (a.S == 0) a.tie = C > 0 ? 1 : -1;        // vertical ray, normal (+-1, 0)
-        else if (a.C == 0) a.tie = S > 0 ? 1 : -1;   // horizontal ray, normal (0, +-1)
-        if (a.tie != 0) a.H1 = a.H2;                 // s = 0: no ramp
-        // segments of 1e-10 or less are dropped, as the ray tracer does
-        // (system_generation.f90:393-394)
-        a.Hcut = a.tie != 0 ? a.H2 : a.H2 - (long long)floor(1e-10 * c * s * fair::kOne);
-        a.H1s = (int)(a.H1 >> 16);
-        a.H2s = (int)(a.H2 >> 16);
-        a.Hcuts = (int)(a.Hcut >> 16);
-        if (a.tie == 0 && a.Hcuts >= a.H2s) a.Hcuts = a.H2s;  // s > 0: the ramp ends at H2s
-        a.scale_ramp30 = s > 0 ? (float)(1.0 / (1073741824.0 * c * s)) : 0.f;
+        fair::mf_line(C, S, K, t[i]);
     }
-    if (A->ang.grow(sizeof(fair::MfAngle) * nth) != FAIR_OK ||
-        cudaMemcpy(A->ang.p, t.data(), sizeof(fair::MfAngle) * nth, cudaMemcpyHostToDevice) !=
-            cudaSuccess) {
+    if (fair::mf_upload(A->ang, t) != FAIR_OK) {
         fair_mf_destroy(A);
+        *out = nullptr;
         return FAIR_ERR_ALLOC;
     }
-    *out = A;
+    return FAIR_OK;
+}
+
+int fair_mf_create_fan(fair_mf *out, const fair_data *dat, int32_t geometry_fix, int32_t prec) {
+    FAIR_TRY(fair::mf_new(out, dat, prec, 1));
+    fair_mf A = *out;
+    const int N = dat->n, p = dat->p, nth = dat->nth;
+    const double pi = 3.141592653589793;  // 4*atan(1d0), system_generation.f90:4
+    // the bin angles and the rotated source and central direction, as
+    // fanlineartomo computes them (system_generation.f90:98-157)
+    const double R = dat->r * N, dwn = dat->dw * N, sdn = dat->sd * N;
+    const double dew = dwn / p;
+    std::vector<double> omega(p), com(p), som(p);
+    if (p % 2 == 1) {
+        const int hh = (p - 1) / 2;
+        for (int i = 1; i <= hh; ++i) {
+            const double dep = i * dew;
+            omega[hh - i] = atan(sdn / dep) - (geometry_fix ? .5 * pi : .5);  // :122
+            omega[hh + i] = .5 * pi - atan(sdn / dep);
+        }
+        omega[hh] = 0.0;
+    } else {
+        const int hh = p / 2;
+        for (int i = 1; i <= hh; ++i) {
+            const double dep = (i - .5) * dew;
+            omega[hh - i] = atan(sdn / dep) - .5 * pi;  // :129
+            omega[hh + i - 1] = .5 * pi - atan(sdn / dep);
+        }
+    }
+    for (int j = 0; j < p; ++j) {
+        com[j] = cos(omega[j]);
+        som[j] = sin(omega[j]);
+    }
+    std::vector<fair::MfAngle> rays((size_t)nth * p);
+    std::vector<fair::MfFanAngle> fa(nth);
+    for (int i = 0; i < nth; ++i) {
+        const double c = cos(dat->theta[i]), s = sin(dat->theta[i]);
+        const double x0th = c * 0.0 - s * R, y0th = s * 0.0 + c * R;
+        const double ath = -x0th / R, bth = -y0th / R;
+        fa[i] = fair::MfFanAngle{(float)x0th, (float)y0th, (float)ath, (float)bth};
+        for (int j = 0; j < p; ++j) {
+            // the ray direction of the reference's tracer (:163-166)
+            const double a = com[j] * ath - som[j] * bth;
+            const double b = som[j] * ath + com[j] * bth;
+            const double nu = sqrt(a * a + b * b);
+            const double C = b / nu, S = -a / nu;  // unit normal
+            const double K = C * (0.5 - 0.5 * N - x0th) + S * (0.5 - 0.5 * N - y0th);
+            fair::mf_line(C, S, K, rays[(size_t)i * p + j]);
+        }
+    }
+    // the bin angles sorted (the odd-p angles of :122 are not monotone in j)
+    std::vector<int> order(p);
+    for (int j = 0; j < p; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int u, int v) { return (float)omega[u] < (float)omega[v]; });
+    std::vector<float> oms(p);
+    for (int k = 0; k < p; ++k) oms[k] = (float)omega[order[k]];
+    if (fair::mf_upload(A->ang, rays) != FAIR_OK || fair::mf_upload(A->fang, fa) != FAIR_OK ||
+        fair::mf_upload(A->oms, oms) != FAIR_OK || fair::mf_upload(A->omj, order) != FAIR_OK) {
+        fair_mf_destroy(A);
+        *out = nullptr;
+        return FAIR_ERR_ALLOC;
+    }
     return FAIR_OK;
 }
 
@@ -379,8 +571,9 @@ int fair_mf_destroy(fair_mf A) {
     if (!A) return FAIR_OK;
     cudaSetDevice(A->device);
     cudaStreamSynchronize(A->stream);
-    for (fair::DevBuf *d : {&A->ang, &A->w_in, &A->w_out, &A->v_a, &A->v_b, &A->M_sart,
-                            &A->M_cim, &A->D, &A->x32, &A->r, &A->w_b, &A->w_x})
+    for (fair::DevBuf *d : {&A->ang, &A->fang, &A->oms, &A->omj, &A->w_in, &A->w_out, &A->v_a,
+                            &A->v_b, &A->M_sart, &A->M_cim, &A->D, &A->x32, &A->r, &A->w_b,
+                            &A->w_x})
         d->release();
     if (A->own_stream) cudaStreamDestroy(A->stream);
     delete A;
@@ -419,27 +612,20 @@ static int mf_apply(fair_mf A, bool back, const double *in, double *out) {
     FAIR_TRY(A->w_in.grow(sizeof(double) * (nin + 1)));
     FAIR_TRY(A->w_out.grow(sizeof(double) * (nout + 1)));
     FAIR_CUDA(cudaMemcpyAsync(A->w_in.p, in, sizeof(double) * nin, cudaMemcpyHostToDevice, s));
-    const fair::MfAngle *ang = A->ang.as<fair::MfAngle>();
     if (A->prec == FAIR_PREC_F64) {
         fair::EpiStore<double> e{A->w_out.as<double>()};
-        if (back)
-            fair::k_mf_backproject<double, double, 0><<<fair::grid_for(n / 2 + 1, 128), 128, 0, s>>>(
-                ang, A->nth, A->p, A->N, A->w_in.as<double>(), e);
-        else
-            fair::k_mf_project<double, double, 0><<<fair::grid_for(m, 128), 128, 0, s>>>(
-                ang, A->nth, A->p, A->N, A->w_in.as<double>(), e);
+        const double *vin = A->w_in.as<double>();
+        if (back) fair::mf_backproject<double, double, 0>(A, vin, e, s);
+        else fair::mf_project<double, double, 0>(A, vin, e, s);
         FAIR_CUDA(cudaGetLastError());
     } else {
         FAIR_TRY(A->v_a.grow(sizeof(float) * (nin + 1)));
         FAIR_TRY(A->v_b.grow(sizeof(float) * (nout + 1)));
         FAIR_TRY(fair::vec_to_f32(A->w_in.as<double>(), nin, A->v_a.as<float>(), s));
         fair::EpiStore<float> e{A->v_b.as<float>()};
-        if (back)
-            fair::k_mf_backproject<float, float, 0><<<fair::grid_for(n / 2 + 1, 128), 128, 0, s>>>(
-                ang, A->nth, A->p, A->N, A->v_a.as<float>(), e);
-        else
-            fair::k_mf_project<float, float, 0><<<fair::grid_for(m, 128), 128, 0, s>>>(
-                ang, A->nth, A->p, A->N, A->v_a.as<float>(), e);
+        const float *vin = A->v_a.as<float>();
+        if (back) fair::mf_backproject<float, float, 0>(A, vin, e, s);
+        else fair::mf_project<float, float, 0>(A, vin, e, s);
         FAIR_CUDA(cudaGetLastError());
         FAIR_TRY(fair::vec_to_f64(A->v_b.as<float>(), nout, A->w_out.as<double>(), s));
     }
@@ -456,8 +642,7 @@ int fair_mf_nnz(fair_mf A, int64_t *nnz) {
     cudaStream_t s = A->stream;
     FAIR_TRY(A->w_out.grow(sizeof(double) * (m + 1)));
     fair::EpiStore<double> e{A->w_out.as<double>()};
-    fair::k_mf_project<double, double, 3><<<fair::grid_for(m, 128), 128, 0, s>>>(
-        A->ang.as<fair::MfAngle>(), A->nth, A->p, A->N, nullptr, e);
+    fair::mf_project<double, double, 3>(A, (const double *)nullptr, e, s);
     FAIR_CUDA(cudaGetLastError());
     std::vector<double> c(m);
     FAIR_CUDA(cudaMemcpyAsync(c.data(), A->w_out.p, sizeof(double) * m, cudaMemcpyDeviceToHost, s));

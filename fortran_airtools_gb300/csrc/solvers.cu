@@ -318,6 +318,27 @@ int sirt_weights(const DevCSR &A, const DevCSR &AT, bool sart, double *d_M, doub
     return FAIR_OK;
 }
 
+__global__ void k_reciprocal(double *v, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = __ddiv_rn(1.0, v[i]);
+}
+
+int vec_reciprocal(double *v, int64_t n, cudaStream_t s) {
+    if (n <= 0) return FAIR_OK;
+    k_reciprocal<<<elem_grid(n), 256, 0, s>>>(v, n);
+    FAIR_CUDA(cudaGetLastError());
+    return FAIR_OK;
+}
+
+int sirt_weights_recip(const DevCSR &A, const DevCSR &AT, bool sart, double *d_Mi, double *d_Di,
+                       cudaStream_t s) {
+    FAIR_TRY(sirt_weights(A, AT, sart, d_Mi, d_Di, s));
+    FAIR_TRY(vec_reciprocal(d_Mi, A.m, s));
+    if (sart) FAIR_TRY(vec_reciprocal(d_Di, A.n, s));
+    return FAIR_OK;
+}
+
 int sirt_prepare_shadow(const SirtDev &S, cudaStream_t s) {
     if (S.prec != FAIR_PREC_F64 && S.n > 0) {
         k_to_f32v<<<elem_grid(S.n), 256, 0, s>>>(S.x, S.n, S.x32);

@@ -1,9 +1,9 @@
-"""Matrix-free parallel-beam projector / backprojector (include/fair_mf.h).
+"""Matrix-free projector / backprojector pairs (include/fair_mf.h).
 
 No counterpart in the reference, which stores the system matrix of
-``paralleltomo`` (system_generation.f90:309-492): the entries here are the
-same segment lengths computed on the fly, and the backprojector is the exact
-adjoint of the projector.
+``paralleltomo`` (system_generation.f90:309-492) and ``fanlineartomo``
+(:79-307): the entries here are the same segment lengths computed on the fly,
+and the backprojector is the exact adjoint of the projector.
 """
 from __future__ import annotations
 
@@ -16,10 +16,19 @@ from .airms import options
 
 
 class MatrixFree:
-    def __init__(self, dat, prec: str = "f32"):
+    """The operator of ``dat``'s geometry: ``beam="parallel"`` (paralleltomo)
+    or ``beam="fan"`` (fanlineartomo; ``geometry_fix`` as there)."""
+
+    def __init__(self, dat, prec: str = "f32", beam: str = "parallel", geometry_fix: int = 0):
         self._h = C.c_void_p()
         d = dat._c()
-        check(lib().fair_mf_create_parallel(C.byref(self._h), C.byref(d), PREC[prec]))
+        if beam == "parallel":
+            check(lib().fair_mf_create_parallel(C.byref(self._h), C.byref(d), PREC[prec]))
+        elif beam == "fan":
+            check(lib().fair_mf_create_fan(C.byref(self._h), C.byref(d), int(geometry_fix),
+                                           PREC[prec]))
+        else:
+            raise ValueError("beam must be 'parallel' or 'fan'")
         m, n = C.c_int32(), C.c_int32()
         check(lib().fair_mf_info(self._h, C.byref(m), C.byref(n)))
         self.m, self.n, self.prec = m.value, n.value, prec

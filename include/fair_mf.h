@@ -1,6 +1,7 @@
-/* fair_mf.h -- matrix-free projector / backprojector pair for the
- * parallel-beam geometry of paralleltomo (system_generation.f90:309-492), and
- * SIRT/SART on it (no counterpart in the reference, which always stores the
+/* fair_mf.h -- matrix-free projector / backprojector pairs for the
+ * parallel-beam geometry of paralleltomo (system_generation.f90:309-492) and
+ * the fan-beam geometry of fanlineartomo (system_generation.f90:79-307), and
+ * SIRT/SART on them (no counterpart in the reference, which always stores the
  * system matrix).
  *
  * Entry a_ij is the length of ray i inside pixel j, computed in closed form
@@ -31,6 +32,16 @@ typedef struct fair_mf_s *fair_mf;
  * prec FAIR_PREC_F64 (FP64 entries, vectors and sums) or FAIR_PREC_F32
  * (FP32 entries, vectors and sums; SIRT keeps FP64 weights and iterate). */
 int fair_mf_create_parallel(fair_mf *out, const fair_data *dat, int32_t prec);
+/* Operator of the fan-beam geometry in dat (n, p, nth, r, dw, sd, theta) as
+ * fanlineartomo builds it (system_generation.f90:79-307; geometry_fix as in
+ * fair_fanlineartomo: 0 keeps the reference's odd-p bin angles of :122):
+ * each ray's line from the same source position and direction values, one
+ * record per ray (about 112 bytes: 58 MB for 720 angles x 725 bins). The
+ * backprojector finds a pixel's rays per angle by the angle of the pixel
+ * seen from the source. A ray that the reference's rounding tilts across a
+ * grid line (odd p: the central ray at theta = pi/2, pi, 3pi/2, where the
+ * residue of cos or sin moves it by ~1e-16) lies on one side here. */
+int fair_mf_create_fan(fair_mf *out, const fair_data *dat, int32_t geometry_fix, int32_t prec);
 int fair_mf_destroy(fair_mf A);
 int fair_mf_set_stream(fair_mf A, void *cuda_stream);
 int fair_mf_info(fair_mf A, int32_t *m, int32_t *n);
