@@ -1302,11 +1302,15 @@ int lvl_sweep(const SweepDev &S, int dir, const RowStep *steps, const Box &box, 
     const int64_t *lptr = C.lptr.as<int64_t>();
     const int *nlev = C.dnlev.as<int>();
     const int *err = W.err.as<int>();
-    // warps per step: the average row in the registers of the group (4 chunks
-    // of 32 entries per warp); FAIR_SWEEP_GROUP overrides (1, 2, 4 or 8)
+    // warps per step: a long row (twice the mean, at most the longest) in 2
+    // chunks of 32 entries per warp, at most 8 warps: a warp's FP64
+    // instructions per step (64 cycles each) are on the level's critical path.
+    // Measured (GB300, 10 sweeps of fan N=128 / 20 of fan N=512 symmetric,
+    // s): G = 1 0.061 / 1.96, 2 0.041 / 1.16, 4 0.036 / 1.03, 8 0.038 / 1.00.
+    // FAIR_SWEEP_GROUP overrides (1, 2, 4 or 8).
     const double avg = S.nord > 0 ? (double)C.entries / S.nord : 0.0;
     int G = 1;
-    while (G < 8 && 128.0 * G < std::min(2.0 * avg, (double)A.max_row)) G *= 2;
+    while (G < 8 && 64.0 * G < std::min(2.0 * avg, (double)A.max_row)) G *= 2;
     const int Ge = env_int("FAIR_SWEEP_GROUP", 0);
     if (Ge == 1 || Ge == 2 || Ge == 4 || Ge == 8) G = Ge;
     FAIR_TRY((lvl_launch<4, 512>(S, sched, lptr, nlev, box, G, err, s)));
