@@ -41,6 +41,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "fair_internal.cuh"
 
@@ -1109,8 +1110,10 @@ int lvl_launch_cluster(int cs, size_t smem, const RowStep *sched, const int64_t 
 template <int CACHE, int NT>
 int lvl_launch(const SweepDev &S, const RowStep *sched, const int64_t *lptr, const int *nlev,
                const Box &box, int G, const int *err, cudaStream_t s) {
-    // cluster sizes found per device, x placement and image size
+    // cluster sizes found per device, x placement and image size (host
+    // threads may sweep on different handles at once)
     static struct { int32_t n = -1; int want = 0, cs = 0; } cache[128][2];
+    static std::mutex cache_mu;
     int dev = 0, optin = 0;
     FAIR_CUDA(cudaGetDevice(&dev));
     FAIR_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1121,6 +1124,7 @@ int lvl_launch(const SweepDev &S, const RowStep *sched, const int64_t *lptr, con
     const double *val = S.A->v64.as<double>();
     const size_t room = (size_t)optin - 8192;  // beside the static parts
     auto cluster = [&](int xd) {
+        std::lock_guard<std::mutex> lk(cache_mu);
         auto &c = cache[dev & 127][xd];
         if (c.n != n || c.want != want) {
             c.cs = xd ? lvl_cluster_size<XD, CACHE, NT>(want, n, room)
