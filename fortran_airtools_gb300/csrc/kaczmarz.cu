@@ -852,11 +852,32 @@ template <> struct XAcc<XD> {
 // in shared memory behind the group's named barrier, are added exactly and
 // rounded once; then the coefficient (b - a.x) * (omega / nrA) and the bounded
 // updates.
+// A warp's first CACHE chunks of a step (column and value of entry lane of
+// each chunk; column 0 and value 0 past the row's end).
+template <int CACHE> struct LvlChunks {
+    int32_t c[CACHE];
+    double v[CACHE];
+};
+template <int CACHE>
+__device__ __forceinline__ void lvl_load_chunks(const RowStep &st, const int32_t *__restrict__ col,
+                                                const double *__restrict__ val, int lane, int G,
+                                                int wg, LvlChunks<CACHE> &k) {
+    const int nq = (st.len + 31) >> 5;
+    const int nmine = nq > wg ? (nq - wg + G - 1) / G : 0;
+#pragma unroll
+    for (int i = 0; i < CACHE; ++i) {
+        const int e = (wg + G * i) * 32 + lane;
+        const bool h = i < nmine && e < st.len;
+        k.c[i] = h ? __ldg(col + st.s + e) : 0;
+        k.v[i] = h ? __ldg(val + st.s + e) : 0.0;
+    }
+}
+
 template <int XM, int CACHE>
 __device__ __forceinline__ void lvl_row(const RowStep &st, const int32_t *__restrict__ col,
                                         const double *__restrict__ val, const XAcc<XM> &X,
                                         const Box &box, int lane, int G, int wg, FxPart *parts,
-                                        int bar) {
+                                        int bar, const LvlChunks<CACHE> &pre) {
     using R = typename XAcc<XM>::R;
     constexpr int B = 4;  // chunks per batch beyond the cached ones
     R cr[CACHE];
@@ -866,11 +887,8 @@ __device__ __forceinline__ void lvl_row(const RowStep &st, const int32_t *__rest
     int32_t cj[CACHE];
 #pragma unroll
     for (int i = 0; i < CACHE; ++i) {
-        if (i >= nmine) break;
-        const int e = (wg + G * i) * 32 + lane;
-        const bool h = e < st.len;
-        cj[i] = h ? __ldg(col + st.s + e) : 0;
-        vv[i] = h ? __ldg(val + st.s + e) : 0.0;
+        cj[i] = pre.c[i];
+        vv[i] = pre.v[i];
     }
 #pragma unroll
     for (int i = 0; i < CACHE; ++i) {
@@ -963,9 +981,9 @@ __device__ __forceinline__ void lvl_row(const RowStep &st, const int32_t *__rest
 
 
 // The levels in order on one cluster of gridDim.x blocks (CLUSTER) or one
-// block. Groups of G consecutive warps take the steps of a level in turn; the
-// bounds of the next level and each group's first step in it are loaded one
-// level ahead, and that step's entries are prefetched into L2. With x in
+// block. Groups of G consecutive warps take the steps of a level in turn; each
+// group's first step of a level is known two levels ahead and its first
+// chunks are loaded one level ahead (in registers). With x in
 // (distributed) shared memory (XM = XS or XD, cb = log2 of a block's part), x
 // is loaded at the start and written back at the end.
 template <bool CLUSTER, int XM, int CACHE, int NT>
@@ -1003,17 +1021,35 @@ __global__ void __launch_bounds__(NT, 1) k_lvl_sweep(
     const int64_t NG = (int64_t)gridDim.x * (NW / G);
     const int bar = 1 + gl;
     const RowStep none{0, 0, 0, 0.0, 0.0};
-    int64_t a0 = 0, a1 = nlev > 0 ? lptr[1] : 0;
-    RowStep nxt = grp < a1 ? sched[grp] : none;
+    // State at the start of level l: the bounds of levels l, l+1, l+2
+    // ([a0, a1), [a1, a2), [a2, a3)); this group's first step of level l (cur,
+    // its first chunks in pc) and of level l+1 (nxt). During level l the group
+    // loads the bound after a3, its first step of level l+2 and the first
+    // chunks of nxt, so that no level waits for a load of its own bounds,
+    // steps or first entries; the rest of nxt's entries are prefetched into L2.
+    auto bound = [&](int q) -> int64_t { return q <= nlev ? lptr[q] : lptr[nlev]; };
+    int64_t a0 = 0, a1 = bound(1), a2 = bound(2), a3 = bound(3);
+    RowStep cur = grp < a1 ? sched[grp] : none;
+    RowStep nxt = a1 + grp < a2 ? sched[a1 + grp] : none;
+    LvlChunks<CACHE> pc;
+    lvl_load_chunks<CACHE>(cur, col, val, lane, G, wg, pc);
     for (int l = 0; l < nlev; ++l) {
-        const int64_t b1 = l + 1 < nlev ? lptr[l + 2] : a1;
-        const RowStep cur = nxt;
-        nxt = a1 + grp < b1 ? sched[a1 + grp] : none;
+        const int64_t a4 = bound(l + 4);
+        const RowStep nxt2 = a2 + grp < a3 ? sched[a2 + grp] : none;
+        LvlChunks<CACHE> pn;
+        lvl_load_chunks<CACHE>(nxt, col, val, lane, G, wg, pn);
         int par = 0;
-        for (int64_t k = a0 + grp; k < a1; k += NG, par ^= 1)
-            lvl_row<XM, CACHE>(k == a0 + grp ? cur : sched[k], col, val, X, box, lane, G, wg,
-                               parts[par] + gl * G, bar);
-        if (nxt.len > 0) {  // the next level's first step of this group: into L2
+        for (int64_t k = a0 + grp; k < a1; k += NG, par ^= 1) {
+            if (k == a0 + grp) {
+                lvl_row<XM, CACHE>(cur, col, val, X, box, lane, G, wg, parts[par] + gl * G, bar, pc);
+            } else {
+                const RowStep st = sched[k];
+                LvlChunks<CACHE> pk;
+                lvl_load_chunks<CACHE>(st, col, val, lane, G, wg, pk);
+                lvl_row<XM, CACHE>(st, col, val, X, box, lane, G, wg, parts[par] + gl * G, bar, pk);
+            }
+        }
+        if (nxt.len > 32 * G * CACHE) {  // the rest of the next level's first step: into L2
             const char *c0 = reinterpret_cast<const char *>(col + nxt.s);
             const char *v0 = reinterpret_cast<const char *>(val + nxt.s);
             const int nc = (nxt.len * 4 + 127) >> 7, nv = (nxt.len * 8 + 127) >> 7;
@@ -1025,7 +1061,12 @@ __global__ void __launch_bounds__(NT, 1) k_lvl_sweep(
         if (CLUSTER) cluster_barrier();
         else __syncthreads();
         a0 = a1;
-        a1 = b1;
+        a1 = a2;
+        a2 = a3;
+        a3 = a4;
+        cur = nxt;
+        nxt = nxt2;
+        pc = pn;
     }
     if constexpr (XM != XG) {
         for (int64_t i = threadIdx.x; i < plen; i += NT)
@@ -1317,7 +1358,7 @@ int lvl_sweep(const SweepDev &S, int dir, const RowStep *steps, const Box &box, 
     while (G < 8 && 64.0 * G < std::min(2.0 * avg, (double)A.max_row)) G *= 2;
     const int Ge = env_int("FAIR_SWEEP_GROUP", 0);
     if (Ge == 1 || Ge == 2 || Ge == 4 || Ge == 8) G = Ge;
-    FAIR_TRY((lvl_launch<4, 512>(S, sched, lptr, nlev, box, G, err, s)));
+    FAIR_TRY((lvl_launch<2, 512>(S, sched, lptr, nlev, box, G, err, s)));
     *done = true;
     return FAIR_OK;
 }
