@@ -346,6 +346,7 @@ struct SweepWork {
     // column level table (large images), the fallback flag, the blocks' stamp
     // tables
     DevBuf lens, eoff, idx, rec, dpath, lvl, cnt, lvtab, err, tabs;
+    DevBuf gsync;                      // grid barrier of the cooperative sweep {count, generation, error}
     int32_t tab_n = 0, tab_blocks = 0;
     uint64_t uid = 0;                  // next window stamp (the tables hold older ones)
     bool err_valid = false;            // err holds the set-up's repeated-column flag

@@ -986,13 +986,51 @@ __device__ __forceinline__ void lvl_row(const RowStep &st, const int32_t *__rest
 // chunks are loaded one level ahead (in registers). With x in
 // (distributed) shared memory (XM = XS or XD, cb = log2 of a block's part), x
 // is loaded at the start and written back at the end.
-template <bool CLUSTER, int XM, int CACHE, int NT>
+// A barrier of all blocks of a cooperative launch: gbar[0] counts the
+// arrivals, gbar[1] is the generation the last arrival advances (both zero at
+// the launch). A block that waits more than kGridSpinLimit polls sets *gerr
+// and returns false; the sweep then stops, and the host reports the error.
+constexpr unsigned long long kGridSpinLimit = 1ull << 26;
+enum { SYNC_BLOCK = 0, SYNC_CLUSTER = 1, SYNC_GRID = 2 };
+
+__device__ __forceinline__ bool grid_barrier(unsigned *gbar, int *gerr) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = gbar + 1;
+        const unsigned g = *gen;
+        int ok = 1;
+        __threadfence();
+        if (atomicAdd(gbar, 1u) == gridDim.x - 1) {
+            gbar[0] = 0u;  // nobody arrives again before the generation moves
+            __threadfence();
+            atomicAdd(gbar + 1, 1u);
+        } else {
+            unsigned long long it = 0;
+            while (*gen == g) {
+                if (++it > kGridSpinLimit || *(volatile int *)gerr) {
+                    atomicExch(gerr, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+template <int SYNC, int XM, int CACHE, int NT>
 __global__ void __launch_bounds__(NT, 1) k_lvl_sweep(
         const RowStep *__restrict__ sched, const int64_t *__restrict__ lptr,
         const int *__restrict__ nlevp, const int32_t *__restrict__ col,
         const double *__restrict__ val, double *x, int32_t n, int cb, Box box, int G,
-        const int *__restrict__ err) {
+        const int *__restrict__ err, unsigned *gbar, int *gerr) {
     constexpr int NW = NT / 32;
+    constexpr bool CLUSTER = SYNC == SYNC_CLUSTER;
     extern __shared__ __align__(16) double xsm[];
     __shared__ FxPart parts[2][NW];  // per group: two rows' parts (by parity), G each
     if (*err) return;
@@ -1058,8 +1096,12 @@ __global__ void __launch_bounds__(NT, 1) k_lvl_sweep(
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
             }
         }
-        if (CLUSTER) cluster_barrier();
-        else __syncthreads();
+        if (SYNC == SYNC_CLUSTER) cluster_barrier();
+        else if (SYNC == SYNC_GRID) {
+            if (!grid_barrier(gbar, gerr)) return;
+        } else {
+            __syncthreads();
+        }
         a0 = a1;
         a1 = a2;
         a2 = a3;
@@ -1092,7 +1134,7 @@ int part_log2(int cs, int32_t n) {
 // 1 if none can be had.
 template <int XM, int CACHE, int NT>
 int lvl_cluster_size(int want, int32_t n, size_t room) {
-    auto kern = k_lvl_sweep<true, XM, CACHE, NT>;
+    auto kern = k_lvl_sweep<SYNC_CLUSTER, XM, CACHE, NT>;
     for (int cs = 16; cs >= 2; cs >>= 1) {
         if (cs > want) continue;
         const size_t smem = XM == XD ? (size_t)8 << part_log2(cs, n) : 0;
@@ -1124,7 +1166,7 @@ template <int XM, int CACHE, int NT>
 int lvl_launch_cluster(int cs, size_t smem, const RowStep *sched, const int64_t *lptr,
                        const int *nlev, const int32_t *col, const double *val, double *x,
                        int32_t n, int cb, const Box &box, int G, const int *err, cudaStream_t s) {
-    auto kern = k_lvl_sweep<true, XM, CACHE, NT>;
+    auto kern = k_lvl_sweep<SYNC_CLUSTER, XM, CACHE, NT>;
     FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (cs > 8) FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg{};
@@ -1139,7 +1181,8 @@ int lvl_launch_cluster(int cs, size_t smem, const RowStep *sched, const int64_t 
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    FAIR_CUDA(cudaLaunchKernelEx(&cfg, kern, sched, lptr, nlev, col, val, x, n, cb, box, G, err));
+    FAIR_CUDA(cudaLaunchKernelEx(&cfg, kern, sched, lptr, nlev, col, val, x, n, cb, box, G, err,
+                                 (unsigned *)nullptr, (int *)nullptr));
     return FAIR_OK;
 }
 
@@ -1148,9 +1191,54 @@ int lvl_launch_cluster(int cs, size_t smem, const RowStep *sched, const int64_t 
 // block with x in its shared memory when no cluster can be had.
 // FAIR_SWEEP_CLUSTER caps the cluster size (1: one block), FAIR_SWEEP_XMEM
 // picks x's place (0: global, 1: shared/distributed).
+// The level sweep on a cooperative grid of nb blocks (x in global memory, the
+// software grid barrier between levels); gsync: {count, generation, error}.
+template <int CACHE, int NT>
+int lvl_launch_grid(int nb, const RowStep *sched, const int64_t *lptr, const int *nlev,
+                    const int32_t *col, const double *val, double *x, int32_t n, const Box &box,
+                    int G, const int *err, int *gsync, cudaStream_t s) {
+    auto kern = k_lvl_sweep<SYNC_GRID, XG, CACHE, NT>;
+    FAIR_CUDA(cudaMemsetAsync(gsync, 0, 4 * sizeof(int), s));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(nb);
+    cfg.blockDim = dim3(NT);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    FAIR_CUDA(cudaLaunchKernelEx(&cfg, kern, sched, lptr, nlev, col, val, x, n, 0, box, G, err,
+                                 (unsigned *)gsync, gsync + 2));
+    int gerr = 0;
+    FAIR_CUDA(cudaMemcpyAsync(&gerr, gsync + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FAIR_CUDA(cudaStreamSynchronize(s));
+    if (gerr) {
+        set_detail("Kaczmarz level sweep: a grid barrier timed out");
+        return FAIR_ERR_CUDA;
+    }
+    return FAIR_OK;
+}
+
+// Blocks of a cooperative grid for a level sweep whose levels hold `spl`
+// steps of G warps on average (about one round per level), at most the
+// co-resident blocks; 0 when the grid would not exceed the cluster (cs blocks).
+template <int CACHE, int NT>
+int lvl_grid_blocks(double spl, int G, int cs) {
+    const int want = (int)std::ceil(spl * 1.25 * G / (NT / 32));
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_lvl_sweep<SYNC_GRID, XG, CACHE, NT>, NT, 0) !=
+            cudaSuccess || occ < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    const int nb = std::min(want, occ * sm_count());
+    return nb > cs ? nb : 0;
+}
+
 template <int CACHE, int NT>
 int lvl_launch(const SweepDev &S, const RowStep *sched, const int64_t *lptr, const int *nlev,
-               const Box &box, int G, const int *err, cudaStream_t s) {
+               const Box &box, int G, const int *err, double spl, cudaStream_t s) {
     // cluster sizes found per device, x placement and image size (host
     // threads may sweep on different handles at once)
     static struct { int32_t n = -1; int want = 0, cs = 0; } cache[128][2];
@@ -1175,6 +1263,17 @@ int lvl_launch(const SweepDev &S, const RowStep *sched, const int64_t *lptr, con
         }
         return c.cs;
     };
+    // levels with more steps than one round of the cluster's groups: a
+    // cooperative grid (FAIR_SWEEP_GRID=0 keeps the cluster, 1 forces the grid)
+    {
+        const int gmode = env_int("FAIR_SWEEP_GRID", -1);
+        const int cs = cluster(xmem ? 1 : 0);
+        int nb = gmode == 0 ? 0 : lvl_grid_blocks<CACHE, NT>(spl, G, std::max(cs, 1));
+        if (gmode == 1 && nb == 0) nb = std::min(2 * std::max(cs, 1), sm_count());
+        if (nb > 0 && S.work)
+            return lvl_launch_grid<CACHE, NT>(nb, sched, lptr, nlev, col, val, S.x, n, box, G, err,
+                                              S.work->gsync.as<int>(), s);
+    }
     if (xmem) {
         const int cs = cluster(1);
         if (cs >= 2) {
@@ -1183,18 +1282,19 @@ int lvl_launch(const SweepDev &S, const RowStep *sched, const int64_t *lptr, con
                                                      S.x, n, cb, box, G, err, s);
         }
         if ((size_t)8 * n <= room) {
-            auto kern = k_lvl_sweep<false, XS, CACHE, NT>;
+            auto kern = k_lvl_sweep<SYNC_BLOCK, XS, CACHE, NT>;
             FAIR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(8 * (size_t)n)));
-            kern<<<1, NT, 8 * (size_t)n, s>>>(sched, lptr, nlev, col, val, S.x, n, 0, box, G, err);
+            kern<<<1, NT, 8 * (size_t)n, s>>>(sched, lptr, nlev, col, val, S.x, n, 0, box, G, err, nullptr,
+                                               nullptr);
             FAIR_CUDA(cudaGetLastError());
             return FAIR_OK;
         }
     }
     const int cs = cluster(0);
     if (cs <= 1) {
-        k_lvl_sweep<false, XG, CACHE, NT><<<1, NT, 0, s>>>(sched, lptr, nlev, col, val, S.x, n, 0,
-                                                          box, G, err);
+        k_lvl_sweep<SYNC_BLOCK, XG, CACHE, NT><<<1, NT, 0, s>>>(sched, lptr, nlev, col, val, S.x, n,
+                                                               0, box, G, err, nullptr, nullptr);
         FAIR_CUDA(cudaGetLastError());
         return FAIR_OK;
     }
@@ -1358,7 +1458,9 @@ int lvl_sweep(const SweepDev &S, int dir, const RowStep *steps, const Box &box, 
     while (G < 8 && 64.0 * G < std::min(2.0 * avg, (double)A.max_row)) G *= 2;
     const int Ge = env_int("FAIR_SWEEP_GROUP", 0);
     if (Ge == 1 || Ge == 2 || Ge == 4 || Ge == 8) G = Ge;
-    FAIR_TRY((lvl_launch<2, 512>(S, sched, lptr, nlev, box, G, err, s)));
+    if (W.gsync.grow(4 * sizeof(int))) return FAIR_OK;
+    const double spl = C.nlev > 0 ? (double)S.nord / C.nlev : 1.0;
+    FAIR_TRY((lvl_launch<2, 512>(S, sched, lptr, nlev, box, G, err, spl, s)));
     *done = true;
     return FAIR_OK;
 }
@@ -1377,6 +1479,7 @@ void SweepWork::release() {
     lvtab.release();
     err.release();
     tabs.release();
+    gsync.release();
     for (Levels &L : lev) {
         L.sched.release();
         L.lptr.release();

@@ -61,6 +61,21 @@ def test_level_sweep_orders(fan, fair, oracle, monkeypatch, cluster, xmem):
             assert rel_err(X[:, l], Xr[:, l]) < TOL64, (method, kw)
 
 
+@pytest.mark.parametrize("group", ["2", "8"])
+def test_level_sweep_cooperative_grid(fan, fair, oracle, monkeypatch, group):
+    """The level sweep on a cooperative grid of blocks (x in global memory, a
+    software grid barrier between levels), as taken when a level holds more
+    steps than one round of the cluster's warp groups."""
+    monkeypatch.setenv("FAIR_SWEEP_GRID", "1")
+    monkeypatch.setenv("FAIR_SWEEP_LEVELS_ALWAYS", "1")
+    monkeypatch.setenv("FAIR_SWEEP_GROUP", group)
+    A, R, b = fan
+    for method, K, kw in CASES:
+        X, Xr = run_both(fair, oracle, A, R, b, method, K, **kw)
+        for l in range(len(K)):
+            assert rel_err(X[:, l], Xr[:, l]) < TOL64, (method, kw)
+
+
 def test_level_sweep_equals_single_block_kernel(fan, fair, oracle, monkeypatch):
     """The level sweep (default) and the single-block sweep on one problem."""
     A, R, b = fan
