@@ -1221,11 +1221,14 @@ int lvl_launch_grid(int nb, const RowStep *sched, const int64_t *lptr, const int
 }
 
 // Blocks of a cooperative grid for a level sweep whose levels hold `spl`
-// steps of G warps on average (about one round per level), at most the
-// co-resident blocks; 0 when the grid would not exceed the cluster (cs blocks).
+// steps of G warps on average (room for twice that: the wavefront's levels
+// vary), at most the co-resident blocks; 0 when the grid would not exceed the
+// cluster (cs blocks).
 template <int CACHE, int NT>
 int lvl_grid_blocks(double spl, int G, int cs) {
-    const int want = (int)std::ceil(spl * 1.25 * G / (NT / 32));
+    int want = (int)std::ceil(spl * 2.0 * G / (NT / 32));
+    const int forced = env_int("FAIR_SWEEP_GRID_BLOCKS", 0);  // measurements
+    if (forced > 0) want = forced;
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_lvl_sweep<SYNC_GRID, XG, CACHE, NT>, NT, 0) !=
             cudaSuccess || occ < 1) {
@@ -1448,16 +1451,18 @@ int lvl_sweep(const SweepDev &S, int dir, const RowStep *steps, const Box &box, 
     const int *nlev = C.dnlev.as<int>();
     const int *err = W.err.as<int>();
     // warps per step: a long row (twice the mean, at most the longest) in 2
-    // chunks of 32 entries per warp, at most 8 warps: a warp's FP64
-    // instructions per step (64 cycles each) are on the level's critical path.
-    // Measured (GB300, 10 sweeps of fan N=128 / 20 of fan N=512 symmetric,
-    // s): G = 1 0.061 / 1.96, 2 0.041 / 1.16, 4 0.036 / 1.03, 8 0.038 / 1.00.
-    // FAIR_SWEEP_GROUP overrides (1, 2, 4 or 8).
+    // chunks of 32 entries per warp, at most 16 warps (a block): a warp's
+    // FP64 instructions per step (64 cycles each) are on the level's critical
+    // path. Measured (GB300, 10 sweeps of fan N=128 on the cluster, s): G = 1
+    // 0.061, 2 0.041, 4 0.036, 8 0.038; 20 sweeps of fan N=512 symmetric on
+    // the cooperative grid (s, blocks): G = 4 0.66 (102), 8 0.58 (51) / 0.52
+    // (152), 16 0.47 (101) / 0.42 (152). FAIR_SWEEP_GROUP overrides (1, 2, 4,
+    // 8 or 16).
     const double avg = S.nord > 0 ? (double)C.entries / S.nord : 0.0;
     int G = 1;
-    while (G < 8 && 64.0 * G < std::min(2.0 * avg, (double)A.max_row)) G *= 2;
+    while (G < 16 && 64.0 * G < std::min(2.0 * avg, (double)A.max_row)) G *= 2;
     const int Ge = env_int("FAIR_SWEEP_GROUP", 0);
-    if (Ge == 1 || Ge == 2 || Ge == 4 || Ge == 8) G = Ge;
+    if (Ge == 1 || Ge == 2 || Ge == 4 || Ge == 8 || Ge == 16) G = Ge;
     if (W.gsync.grow(4 * sizeof(int))) return FAIR_OK;
     const double spl = C.nlev > 0 ? (double)S.nord / C.nlev : 1.0;
     FAIR_TRY((lvl_launch<2, 512>(S, sched, lptr, nlev, box, G, err, spl, s)));

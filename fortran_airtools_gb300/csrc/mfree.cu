@@ -66,7 +66,6 @@ struct MfAngle {
     float Cf, Sf, Kf;    // float copies for the bracketing estimates
     float inv_fast;      // 1/sin (per-column walk) or 1/cos (per-row walk)
     float inv_c;         // 1/c
-    float scale_ramp;    // 2 * 2^-46 / (c s) (0 when s = 0; applied to the halved distance)
     int tie;             // s = 0: +1 / -1 = sign of d that keeps |d| = 1/2; 0 otherwise
     int by_column;       // 1: walk columns (|sin| >= |cos|)
     double inv_c64, scale_ramp64;
@@ -74,16 +73,6 @@ struct MfAngle {
     int H1s, H2s, Hcuts;
     float scale_ramp30;  // 2^-30 / (c s) (0 when s = 0)
 };
-
-// Conversion of 0 <= v < 2^47 to float / 2 (the last bit is below float
-// precision): two exact 23-bit halves through the 2^23 exponent trick.
-__device__ __forceinline__ float fix_to_float_half(long long v) {
-    const long long w = v >> 1;
-    const unsigned hi = (unsigned)(w >> 23), lo = (unsigned)(w & 0x7FFFFF);
-    const float fh = __int_as_float((int)(0x4B000000u | hi)) - 8388608.0f;
-    const float fl = __int_as_float((int)(0x4B000000u | lo)) - 8388608.0f;
-    return fmaf(fh, 8388608.0f, fl);
-}
 
 template <typename T> struct Chord;
 // FP32 entries: the exact distance is truncated to 30 fractional bits (far
@@ -415,7 +404,6 @@ void mf_line(double C, double S, double K, MfAngle &a) {
     a.inv_fast = (float)(1.0 / (a.by_column ? S : C));
     a.inv_c = (float)(1.0 / c);
     a.inv_c64 = 1.0 / c;
-    a.scale_ramp = s > 0 ? (float)(2.0 / (kOne * c * s)) : 0.f;
     a.scale_ramp64 = s > 0 ? 1.0 / (kOne * c * s) : 0.0;
     a.tie = 0;
     if (a.S == 0) a.tie = C > 0 ? 1 : -1;        // vertical ray, normal (+-1, 0)
