@@ -856,7 +856,7 @@ def run_mfree(args):
         M.close()
         if n == 2048 and not args.no_stored:
             res["stored_f32"] = stored_f32_arm(args, F, d, b, x_mf, K, stream, d_b, d_x)
-        if n == 1024:  # the stored form, packed FP32, autotuned
+        if n == 1024 and not args.no_stored:  # the stored form, packed FP32, autotuned
             A = F.paralleltomo(d)
             A.set_stream(stream.cuda_stream)
             A.set_precision("f32")
@@ -1055,7 +1055,7 @@ def main():
                     help="kaczmarz workload: cases to run (comma list of randkaczmarz, "
                          "symkaczmarz, kaczmarz; default all)")
     ap.add_argument("--no-stored", action="store_true",
-                    help="mfree workload: skip the stored FP32 arm at N=2048")
+                    help="mfree workload: skip the stored FP32 arms (N=2048 and N=1024)")
     ap.add_argument("--mf-sizes", default="",
                     help="matrix-free cases to run (comma list of 2048, 1024, fan; default all)")
     args = ap.parse_args()

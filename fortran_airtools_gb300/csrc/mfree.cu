@@ -24,11 +24,12 @@
 // arithmetic, so every kernel computes bit-identical entries whatever the
 // order it meets the (ray, pixel) pairs in. The projector runs one thread
 // per ray and walks the image along the ray's faster axis (per column when
-// |sin| >= |cos|, else per row), testing the 2-3 pixels of each column (row)
-// that a float estimate brackets, conservatively; the backprojector runs one
-// thread per pixel and, per angle, the 1-3 rays whose offsets bracket the
-// pixel's. Both keep only pairs with L > 0, so they sum the same entries: an
-// exact adjoint pair, deterministic, without atomics.
+// |sin| >= |cos|, else per row); at each step the only pixels within H2 of
+// the ray are the two that bracket its crossing, which the walk tracks
+// exactly with one 64-bit add per step. The backprojector runs one thread per
+// 4 pixels of an image column and, per angle, evaluates the two rays whose
+// offsets bracket each pixel's. Both keep only pairs with L > 0, so they sum
+// the same entries: an exact adjoint pair, deterministic, without atomics.
 //
 // Fan beam (fanlineartomo, system_generation.f90:79-307): ray (i, j) is the
 // line through the rotated source P_i with direction u_ij = R(omega_j) u0_i,
@@ -36,7 +37,9 @@
 // angles, the same products and sums). Its unit normal n = (b, -a)/|u| and
 // K_ij = n . ((1/2 - N/2, 1/2 - N/2) - P_i) give d = ix*n_x + iy*n_y + K_ij,
 // the same fixed-point form, one record per ray. The projector walks each ray
-// as above; the backprojector finds, per pixel and angle, the rays whose bin
+// as above (and the rays that walk image rows read a transposed copy of x, so
+// that a warp's rays gather adjacent addresses); the backprojector finds, per
+// pixel and angle, the rays whose bin
 // angle omega_j lies within asin(0.7072/|c - P_i|) (+ 2e-4) of the angle of
 // the pixel centre c seen from the source (a binary search over the bin
 // angles, sorted once: the reference's odd-p angles are not monotone in j),
@@ -59,49 +62,89 @@ namespace {
 constexpr int kFix = 46;
 constexpr double kOne = 70368744177664.0;  // 2^46
 
-struct MfAngle {
-    long long C, S, K;   // cos, sin, K_i in fixed point
-    long long H1, H2;    // (c - s)/2, (c + s)/2 in fixed point
-    long long Hcut;      // |d| >= Hcut leaves a segment of at most 1e-10: dropped
-    float Cf, Sf, Kf;    // float copies for the bracketing estimates
-    float inv_fast;      // 1/sin (per-column walk) or 1/cos (per-row walk)
+// The first 48 bytes hold what the FP32 backprojector reads per angle (three
+// 16-byte loads), the next 32 what FP64 adds.
+struct __align__(16) MfAngle {
+    long long C, S;      // cos, sin in fixed point
+    long long K, H2;     // K_i; (c + s)/2 in fixed point
+    int H2s;             // H2 truncated to 30 fractional bits (FP32 entries)
     float inv_c;         // 1/c
+    float ramp30;        // 2^-30 / s (0 when s = 0)
     int tie;             // s = 0: +1 / -1 = sign of d that keeps |d| = 1/2; 0 otherwise
-    int by_column;       // 1: walk columns (|sin| >= |cos|)
+    long long H1;        // (c - s)/2 in fixed point
+    long long Hcut;      // |d| >= Hcut leaves a segment of at most 1e-10: dropped
     double inv_c64, scale_ramp64;
-    // FP32 entries: |d| truncated to 30 fractional bits, thresholds likewise
-    int H1s, H2s, Hcuts;
-    float scale_ramp30;  // 2^-30 / (c s) (0 when s = 0)
+    float Cf, Sf, Kf;    // float copies for the walk's step range
+    int by_column;       // 1: walk columns (|sin| >= |cos|)
 };
+static_assert(sizeof(MfAngle) == 96, "MfAngle layout");
+
+// The fields of record p that a backprojector of entries T reads: the first
+// 48 bytes (FP32), or 80 (FP64), by 16-byte loads.
+template <typename T>
+__device__ __forceinline__ MfAngle mf_load(const MfAngle *p) {
+    const int4 *q = reinterpret_cast<const int4 *>(p);
+    auto ll = [](int lo, int hi) { return (long long)(((unsigned long long)(unsigned)hi << 32) | (unsigned)lo); };
+    MfAngle A;
+    const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    A.C = ll(a.x, a.y);
+    A.S = ll(a.z, a.w);
+    A.K = ll(b.x, b.y);
+    A.H2 = ll(b.z, b.w);
+    A.H2s = c.x;
+    A.inv_c = __int_as_float(c.y);
+    A.ramp30 = __int_as_float(c.z);
+    A.tie = c.w;
+    if constexpr (sizeof(T) == 8) {
+        const int4 d = __ldg(q + 3), e = __ldg(q + 4);
+        A.H1 = ll(d.x, d.y);
+        A.Hcut = ll(d.z, d.w);
+        A.inv_c64 = __hiloint2double(e.y, e.x);
+        A.scale_ramp64 = __hiloint2double(e.w, e.z);
+    }
+    return A;
+}
 
 template <typename T> struct Chord;
-// FP32 entries: the exact distance is truncated to 30 fractional bits (far
-// below FP32 precision) and the chord is evaluated in 32-bit integers; both
-// kernels truncate the same exact value, so they still agree bit for bit.
+// The chord of a unit pixel at |d| = ad < 2^47 from the line: ramp() for s > 0,
+// tied() for an axis-aligned line (s = 0), where tu = H2 when a ray on the
+// pixel's edge, on this side of it, keeps the pixel (else -1); at() picks one.
+// FP32 entries evaluate the ramp on the exact distance truncated to 30
+// fractional bits, as (1/c) sat((H2 - |d|) / s) with sat() the clamp to
+// [0, 1] (two multiplies on the FMA pipe; the cut of segments below 1e-10 is
+// left to the FP64 entries); every kernel evaluates the same expression on
+// the same exact value, so they agree bit for bit.
 template <> struct Chord<float> {
+    static __device__ __forceinline__ float ramp(const MfAngle &A, long long ad) {
+        const int u = (int)(ad >> 16);
+        return A.inv_c * __saturatef((float)(A.H2s - u) * A.ramp30);
+    }
+    static __device__ __forceinline__ float tied(const MfAngle &A, long long ad, long long tu) {
+        return ad < A.H2 || ad == tu ? A.inv_c : 0.f;
+    }
+    static __device__ __forceinline__ float at(const MfAngle &A, long long ad, long long tu) {
+        return A.tie != 0 ? tied(A, ad, tu) : ramp(A, ad);
+    }
     static __device__ __forceinline__ float of(const MfAngle &A, long long d) {
         const long long ad = d < 0 ? -d : d;
         if (ad >= (1LL << 47)) return 0.f;  // more than two pixels away
-        const int u = (int)(ad >> 16);
-        if (u >= A.Hcuts) {
-            // an axis-aligned ray on the pixel's edge belongs to the positive side
-            if (u == A.H2s && A.tie != 0 && (d > 0 ? 1 : -1) == A.tie) return A.inv_c;
-            return 0.f;
-        }
-        if (u <= A.H1s) return A.inv_c;
-        return (float)(A.H2s - u) * A.scale_ramp30;
+        return at(A, ad, A.tie == (d > 0 ? 1 : -1) ? A.H2 : -1);
     }
 };
 template <> struct Chord<double> {
+    static __device__ __forceinline__ double ramp(const MfAngle &A, long long ad) {
+        const double w = ad <= A.H1 ? A.inv_c64 : (double)(A.H2 - ad) * A.scale_ramp64;
+        return ad < A.Hcut ? w : 0.0;
+    }
+    static __device__ __forceinline__ double tied(const MfAngle &A, long long ad, long long tu) {
+        return ad < A.H2 || ad == tu ? A.inv_c64 : 0.0;
+    }
+    static __device__ __forceinline__ double at(const MfAngle &A, long long ad, long long tu) {
+        return A.tie != 0 ? tied(A, ad, tu) : ramp(A, ad);
+    }
     static __device__ __forceinline__ double of(const MfAngle &A, long long d) {
-        const long long u = d < 0 ? -d : d;
-        if (u >= A.Hcut) {
-            // an axis-aligned ray on the pixel's edge belongs to the positive side
-            if (u == A.H2 && A.tie != 0 && (d > 0 ? 1 : -1) == A.tie) return A.inv_c64;
-            return 0.0;
-        }
-        if (u <= A.H1) return A.inv_c64;
-        return (double)(A.H2 - u) * A.scale_ramp64;
+        const long long ad = d < 0 ? -d : d;
+        return at(A, ad, A.tie == (d > 0 ? 1 : -1) ? A.H2 : -1);
     }
 };
 
@@ -116,92 +159,217 @@ struct EpiCimminoW {  // M = m * sum_j a_ij^2 (the sum arrives in acc)
     __device__ void operator()(int64_t i, double acc) const { M[i] = m * acc; }
 };
 
+// One entry a_rq = w of a pass (valid: pixel q exists): MODE 0 adds w * v_q
+// (v read only for w > 0, as a stored matrix reads only its entries), MODE 1
+// adds w, MODE 2 w^2, MODE 3 counts w > 0.
+template <typename VT, typename ACC, int MODE>
+__device__ __forceinline__ void mf_add(ACC &acc, ACC w, bool valid, const VT *__restrict__ v,
+                                       int64_t q) {
+    if (MODE == 0) {
+        const ACC vq = valid && w > (ACC)0 ? (ACC)__ldg(v + q) : (ACC)0;
+        acc += w * vq;
+    } else if (MODE == 1) {
+        acc += valid ? w : (ACC)0;
+    } else if (MODE == 2) {
+        acc += valid ? w * w : (ACC)0;
+    } else {
+        acc += valid && w > (ACC)0 ? (ACC)1 : (ACC)0;
+    }
+}
+
+// The steps of one ray (see k_mf_project): E = |d| at pixel ua, Qa - E at
+// ua + 1; a step lowers E by Fw and moves ua down by one when E leaves
+// [0, Qa). TIE: an axis-aligned ray (tied chords). Two steps per iteration,
+// so that their gathers are in flight together.
+template <typename XT, typename ACC, int MODE, bool TIE>
+__device__ __forceinline__ ACC mf_walk(const MfAngle &A, long long E, int ua, long long Qa,
+                                       long long Fw, const XT *__restrict__ xv, int qt, int su,
+                                       int dqt, int N, int cnt, long long tua, long long tub) {
+    ACC acc = 0;
+    auto step = [&](ACC &wa, ACC &wb, int &qa, bool &va, bool &vb) {
+        if constexpr (TIE) {
+            wa = Chord<ACC>::tied(A, E, tua);
+            wb = Chord<ACC>::tied(A, Qa - E, tub);
+        } else {
+            wa = Chord<ACC>::ramp(A, E);
+            wb = Chord<ACC>::ramp(A, Qa - E);
+        }
+        qa = qt + ua * su;
+        va = (unsigned)ua < (unsigned)N;
+        vb = (unsigned)(ua + 1) < (unsigned)N;
+        E -= Fw;
+        if (E < 0) {
+            --ua;
+            E += Qa;
+        }
+        qt += dqt;
+    };
+    for (; cnt >= 2; cnt -= 2) {
+        ACC w0, w1, w2, w3;
+        int q0, q1;
+        bool v0, v1, v2, v3;
+        step(w0, w1, q0, v0, v1);
+        step(w2, w3, q1, v2, v3);
+        mf_add<XT, ACC, MODE>(acc, w0, v0, xv, q0);
+        mf_add<XT, ACC, MODE>(acc, w1, v1, xv, q0 + su);
+        mf_add<XT, ACC, MODE>(acc, w2, v2, xv, q1);
+        mf_add<XT, ACC, MODE>(acc, w3, v3, xv, q1 + su);
+    }
+    if (cnt > 0) {
+        ACC w0, w1;
+        int q0;
+        bool v0, v1;
+        step(w0, w1, q0, v0, v1);
+        mf_add<XT, ACC, MODE>(acc, w0, v0, xv, q0);
+        mf_add<XT, ACC, MODE>(acc, w1, v1, xv, q0 + su);
+    }
+    return acc;
+}
+
 // Per ray r: MODE 0 sums a_rj * x_j, MODE 1 sums a_rj, MODE 2 sums a_rj^2,
 // MODE 3 counts the pixels with a_rj > 0 (x unused for MODE 1-3).
 // FAN: ang holds one record per ray (K its own offset), else one per angle
 // (ray j of angle i at offset K - j).
+//
+// The ray walks its faster axis t (|F| <= |Q|): with g = sign(Q) d =
+// t Fp + u Qa + Gk, the pixels u of step t with |d| <= H2 (< Qa) lie within
+// one pixel of u* = -(t Fp + Gk)/Qa, so they are ua = floor(u*) and ua + 1,
+// at |d| = -g(t, ua) in [0, Qa) and Qa - that. The walk keeps ua and that
+// distance exactly: a step changes g by |Fp| (the walk runs in the direction
+// that makes the change non-negative). Only steps whose candidates can lie
+// in the image are walked (a float bound, widened).
+//
+// x is read as x[ix*N + N-1-iy] by the rays that walk columns (a warp's
+// adjacent rays then gather adjacent pixels of one column) and as its
+// transpose xt[(N-1-iy)*N + ix] by those that walk rows (adjacent pixels of
+// one row).
 template <typename XT, typename ACC, int MODE, bool FAN, class Epi>
 __global__ void __launch_bounds__(128) k_mf_project(const MfAngle *__restrict__ ang, int nth,
                                                     int p, int N, const XT *__restrict__ x,
-                                                    Epi epi) {
+                                                    const XT *__restrict__ xt, Epi epi) {
     const int64_t m = (int64_t)nth * p;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m;
          r += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(r / p), j = (int)(r - (int64_t)i * p);
-        const MfAngle A = ang[FAN ? r : i];
+        const MfAngle &A = ang[FAN ? r : i];
         const long long K = FAN ? A.K : A.K - ((long long)j << kFix);
         const float Kf = FAN ? A.Kf : A.Kf - (float)j;
+        const bool col = A.by_column != 0;
+        const long long F = col ? A.C : A.S, Q = col ? A.S : A.C;
+        const float Ff = col ? A.Cf : A.Sf, Qf = col ? A.Sf : A.Cf;
+        const int sq = Q > 0 ? 1 : -1;
+        const long long Qa = Q > 0 ? Q : -Q, Fp = sq * F, Gk = sq * K;
+        const float Qaf = fabsf(Qf), Fpf = sq * Ff, Gkf = sq * Kf;
+        // steps with u* in [-1, N): -N Qa < t Fp + Gk <= Qa (widened by 0.05)
+        const float lo = -(float)N * Qaf - 0.05f - Gkf, hi = Qaf + 0.05f - Gkf;
+        float ta = 0.f, tb = (float)(N - 1);
+        if (Fpf > 0.f) {
+            ta = fmaxf(ta, lo / Fpf);
+            tb = fminf(tb, hi / Fpf);
+        } else if (Fpf < 0.f) {
+            ta = fmaxf(ta, hi / Fpf);
+            tb = fminf(tb, lo / Fpf);
+        } else if (!(lo < 0.f && hi >= 0.f)) {
+            tb = -1.f;
+        }
+        const int t0 = max(0, (int)floorf(ta)), t1 = min(N - 1, (int)ceilf(tb));
         ACC acc = 0;
-        // walk the faster axis: d = t*F + u*Q + K with t the walked index
-        const long long F = A.by_column ? A.C : A.S, Q = A.by_column ? A.S : A.C;
-        const float Ff = A.by_column ? A.Cf : A.Sf;
-        // the pixels u of step t with |d| <= H2 lie in [(-h2 - fA)/Q, (h2 - fA)/Q];
-        // fA (float) is within 1e-3 of t*F + K here, so widening h2 by 2e-3
-        // brackets every one of them (|Q| >= 0.7); the exact test is Chord
-        const float h2 = (float)(A.H2 * (1.0 / kOne)) + 2e-3f;
-        long long base = K;  // t = 0
-        for (int t = 0; t < N; ++t, base += F) {
-            const float fA = fmaf((float)t, Ff, Kf);
-            const float t1 = (-h2 - fA) * A.inv_fast, t2 = (h2 - fA) * A.inv_fast;
-            int lo = (int)ceilf(fminf(t1, t2)), hi = (int)floorf(fmaxf(t1, t2));
-            lo = max(lo, 0);
-            hi = min(hi, N - 1);
-            long long d = base + (long long)lo * Q;
-            for (int u = lo; u <= hi; ++u, d += Q) {
-                const ACC w = Chord<ACC>::of(A, d);
-                if (w > (ACC)0) {
-                    const int ix = A.by_column ? t : u, iy = A.by_column ? u : t;
-                    if (MODE == 0) acc += w * (ACC)__ldg(x + (int64_t)ix * N + (N - 1 - iy));
-                    else if (MODE == 1) acc += w;
-                    else if (MODE == 2) acc += w * w;
-                    else acc += (ACC)1;
-                }
+        if (t0 <= t1) {
+            const int dir = Fp >= 0 ? 1 : -1;
+            const long long Fw = Fp >= 0 ? Fp : -Fp;
+            const int ts = dir > 0 ? t0 : t1;
+            const long long G = (long long)ts * Fp + Gk;
+            int ua = (int)floorf(-(float)G / (float)Qa);
+            long long e = G + (long long)ua * Qa;
+            while (e > 0) { --ua; e -= Qa; }
+            while (e <= -Qa) { ++ua; e += Qa; }
+            // pixel (t, u): element qt + u su of xv
+            const XT *__restrict__ xv = col ? x : xt;
+            const int su = col ? -1 : 1, dqt = col ? dir * N : -dir * N;
+            const int qt = col ? ts * N + N - 1 : (N - 1 - ts) * N;
+            if (A.tie != 0) {
+                // d at ua is sign(Q) e <= 0, at ua + 1 sign(Q) (e + Qa) > 0
+                const long long tua = A.tie == -sq ? A.H2 : -1, tub = A.tie == sq ? A.H2 : -1;
+                acc = mf_walk<XT, ACC, MODE, true>(A, -e, ua, Qa, Fw, xv, qt, su, dqt, N,
+                                                   t1 - t0 + 1, tua, tub);
+            } else {
+                acc = mf_walk<XT, ACC, MODE, false>(A, -e, ua, Qa, Fw, xv, qt, su, dqt, N,
+                                                    t1 - t0 + 1, -1, -1);
             }
         }
         epi(r, acc);
     }
 }
 
-// Sum over the rays through pixel q of a_rq * y_r, for every pixel; MODE 1
-// sums a_rq (y unused). A thread takes two vertically adjacent pixels of one
-// image column (iy and iy - 1), which share the per-angle set-up.
-template <typename YT, typename ACC, int MODE>
-__device__ __forceinline__ void bp_rays(const MfAngle &A, long long base, int i, int p,
-                                        const YT *__restrict__ y, ACC &acc) {
-    // rays j with |base - j 2^46| <= H2
-    const long long jlo = -((A.H2 - base) >> kFix), jhi = (base + A.H2) >> kFix;
-    const int j0 = (int)max(jlo, 0LL), j1 = (int)min(jhi, (long long)p - 1);
-    long long d = base - ((long long)j0 << kFix);
-    for (int j = j0; j <= j1; ++j, d -= (1LL << kFix)) {
-        const ACC w = Chord<ACC>::of(A, d);
-        if (w > (ACC)0) {
-            if (MODE == 0) acc += w * (ACC)__ldg(y + (int64_t)i * p + j);
-            else acc += w;
-        }
+// xt = the transpose of x viewed as an N x N array (32 x 32 tiles through
+// shared memory, both sides coalesced).
+template <typename T>
+__global__ void __launch_bounds__(256) k_mf_transpose(const T *__restrict__ x, T *__restrict__ xt,
+                                                      int N) {
+    __shared__ T tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int r = r0 + k, c = c0 + threadIdx.x;
+        if (r < N && c < N) tile[k][threadIdx.x] = x[(int64_t)r * N + c];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int r = c0 + k, c = r0 + threadIdx.x;
+        if (r < N && c < N) xt[(int64_t)r * N + c] = tile[threadIdx.x][k];
     }
 }
 
-template <typename YT, typename ACC, int MODE, class Epi>
+// Sum over the rays through pixel q of a_rq * y_r, for every pixel; MODE 1
+// sums a_rq (y unused). A thread takes PB vertically adjacent pixels of one
+// image column (iy0, iy0 - 1, ...), which share the per-angle set-up. With
+// D = ix C + iy S + K = jh 2^46 + dl (0 <= dl < 2^46), the rays j with
+// |D - j 2^46| <= H2 (< 2^46) are jh (d = dl) and jh + 1 (d = dl - 2^46).
+template <typename YT, typename ACC, int MODE, int PB, bool TIE>
+__device__ __forceinline__ void bp_angle(const MfAngle &A, long long D, int p,
+                                         const YT *__restrict__ yi, ACC (&acc)[PB]) {
+    constexpr long long kMask = (1LL << kFix) - 1;
+    const long long t0 = TIE && A.tie == 1 ? A.H2 : -1, t1 = TIE && A.tie == -1 ? A.H2 : -1;
+#pragma unroll
+    for (int b = 0; b < PB; ++b, D -= A.S) {
+        const int jh = (int)(D >> kFix);
+        const long long dl = D & kMask;
+        ACC w0, w1;
+        if constexpr (TIE) {
+            w0 = Chord<ACC>::tied(A, dl, t0);
+            w1 = Chord<ACC>::tied(A, (1LL << kFix) - dl, t1);
+        } else {
+            w0 = Chord<ACC>::ramp(A, dl);
+            w1 = Chord<ACC>::ramp(A, (1LL << kFix) - dl);
+        }
+        mf_add<YT, ACC, MODE>(acc[b], w0, (unsigned)jh < (unsigned)p, yi, jh);
+        mf_add<YT, ACC, MODE>(acc[b], w1, (unsigned)(jh + 1) < (unsigned)p, yi, jh + 1);
+    }
+}
+
+template <typename YT, typename ACC, int MODE, int PB, class Epi>
 __global__ void __launch_bounds__(128) k_mf_backproject(const MfAngle *__restrict__ ang,
                                                         int nth, int p, int N,
                                                         const YT *__restrict__ y, Epi epi) {
-    const int half = (N + 1) / 2;  // pixel pairs per image column
-    const int64_t npairs = (int64_t)N * half;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < npairs;
+    const int groups = (N + PB - 1) / PB;  // pixel groups per image column
+    const int64_t ngr = (int64_t)N * groups;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ngr;
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int ix = (int)(t / half), k = (int)(t - (int64_t)ix * half);
-        const int iy0 = N - 1 - 2 * k;     // pixel q0 = ix*N + 2k
-        const bool two = iy0 >= 1;         // and q0 + 1 (iy0 - 1) when it exists
-        ACC acc0 = 0, acc1 = 0;
+        const int ix = (int)(t / groups), k = (int)(t - (int64_t)ix * groups);
+        const int iy0 = N - 1 - PB * k;  // pixel q = ix*N + PB*k + b is iy0 - b
+        ACC acc[PB];
+#pragma unroll
+        for (int b = 0; b < PB; ++b) acc[b] = 0;
         for (int i = 0; i < nth; ++i) {
-            const MfAngle &A = ang[i];
-            const long long base0 = (long long)ix * A.C + (long long)iy0 * A.S + A.K;
-            bp_rays<YT, ACC, MODE>(A, base0, i, p, y, acc0);
-            if (two) bp_rays<YT, ACC, MODE>(A, base0 - A.S, i, p, y, acc1);
+            const MfAngle A = mf_load<ACC>(ang + i);
+            const YT *__restrict__ yi = y + (int64_t)i * p;
+            const long long D = (long long)ix * A.C + (long long)iy0 * A.S + A.K;
+            if (A.tie != 0) bp_angle<YT, ACC, MODE, PB, true>(A, D, p, yi, acc);
+            else bp_angle<YT, ACC, MODE, PB, false>(A, D, p, yi, acc);
         }
-        const int64_t q0 = (int64_t)ix * N + 2 * k;
-        epi(q0, acc0);
-        if (two) epi(q0 + 1, acc1);
+        const int64_t q0 = (int64_t)ix * N + PB * k;
+#pragma unroll
+        for (int b = 0; b < PB; ++b)
+            if (iy0 - b >= 0) epi(q0 + b, acc[b]);
     }
 }
 
@@ -269,6 +437,8 @@ __global__ void __launch_bounds__(128) k_mf_backproject_fan(
     }
 }
 
+constexpr int kMfPB = 4;  // pixels per backprojector thread (parallel beam)
+
 int grid_for(int64_t items, int threads) {
     int64_t b = (items + threads - 1) / threads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm_count() * 32));
@@ -287,6 +457,7 @@ struct fair_mf_s {
     fair::DevBuf ang;                  // MfAngle [nth] (parallel) or [nth*p] (fan: per ray)
     fair::DevBuf fang, oms, omj;       // fan: MfFanAngle [nth], sorted bin angles, their bins
     fair::DevBuf w_in, w_out;          // host-call staging (FP64)
+    fair::DevBuf xt;                   // the projector's transposed copy of x
     fair::DevBuf v_a, v_b;             // reduced-precision staging
     // SIRT state
     bool ready = false, sart = false;
@@ -302,14 +473,28 @@ namespace fair {
 namespace {
 
 // Projector / backprojector launches of either geometry.
+// The transposed copy of x that the projector reads (N^2 elements of the
+// operator's precision), grown before a pass that reads x.
+int mf_grow_xt(fair_mf A) {
+    const size_t es = A->prec == FAIR_PREC_F64 ? sizeof(double) : sizeof(float);
+    return A->xt.grow(es * (size_t)A->N * A->N);
+}
+
 template <typename XT, typename ACC, int MODE, class Epi>
 void mf_project(fair_mf A, const XT *x, Epi epi, cudaStream_t s) {
     const int64_t m = (int64_t)A->nth * A->p;
+    const int N = A->N;
     const MfAngle *ang = A->ang.as<MfAngle>();
+    const XT *xt = nullptr;
+    if (MODE == 0) {  // the rays that walk rows read the transpose (mf_grow_xt)
+        const int nb = (N + 31) / 32;
+        k_mf_transpose<XT><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(x, A->xt.as<XT>(), N);
+        xt = A->xt.as<XT>();
+    }
     if (A->kind == 1)
-        k_mf_project<XT, ACC, MODE, true><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N, x, epi);
+        k_mf_project<XT, ACC, MODE, true><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, N, x, xt, epi);
     else
-        k_mf_project<XT, ACC, MODE, false><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, A->N, x, epi);
+        k_mf_project<XT, ACC, MODE, false><<<grid_for(m, 128), 128, 0, s>>>(ang, A->nth, A->p, N, x, xt, epi);
 }
 template <typename YT, typename ACC, int MODE, class Epi>
 void mf_backproject(fair_mf A, const YT *y, Epi epi, cudaStream_t s) {
@@ -320,8 +505,8 @@ void mf_backproject(fair_mf A, const YT *y, Epi epi, cudaStream_t s) {
             ang, A->fang.as<MfFanAngle>(), A->oms.as<float>(), A->omj.as<int>(), A->nth, A->p,
             A->N, y, epi);
     else
-        k_mf_backproject<YT, ACC, MODE><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(ang, A->nth, A->p,
-                                                                               A->N, y, epi);
+        k_mf_backproject<YT, ACC, MODE, kMfPB><<<grid_for(n / kMfPB + A->N, 128), 128, 0, s>>>(
+            ang, A->nth, A->p, A->N, y, epi);
 }
 
 int mf_weights(fair_mf A, bool sart, cudaStream_t s) {
@@ -392,6 +577,7 @@ namespace {
 // for pixel (ix, iy): fixed-point terms, chord thresholds, walk axis, floats.
 void mf_line(double C, double S, double K, MfAngle &a) {
     const double c = std::max(fabs(C), fabs(S)), s = std::min(fabs(C), fabs(S));
+    a = MfAngle{};
     a.C = llround(C * kOne);
     a.S = llround(S * kOne);
     a.K = llround(K * kOne);
@@ -401,7 +587,6 @@ void mf_line(double C, double S, double K, MfAngle &a) {
     a.Sf = (float)S;
     a.Kf = (float)K;
     a.by_column = fabs(S) >= fabs(C) ? 1 : 0;
-    a.inv_fast = (float)(1.0 / (a.by_column ? S : C));
     a.inv_c = (float)(1.0 / c);
     a.inv_c64 = 1.0 / c;
     a.scale_ramp64 = s > 0 ? 1.0 / (kOne * c * s) : 0.0;
@@ -412,11 +597,8 @@ void mf_line(double C, double S, double K, MfAngle &a) {
     // segments of 1e-10 or less are dropped, as the ray tracer does
     // (system_generation.f90:393-394)
     a.Hcut = a.tie != 0 ? a.H2 : a.H2 - (long long)floor(1e-10 * c * s * kOne);
-    a.H1s = (int)(a.H1 >> 16);
     a.H2s = (int)(a.H2 >> 16);
-    a.Hcuts = (int)(a.Hcut >> 16);
-    if (a.tie == 0 && a.Hcuts >= a.H2s) a.Hcuts = a.H2s;  // s > 0: the ramp ends at H2s
-    a.scale_ramp30 = s > 0 ? (float)(1.0 / (1073741824.0 * c * s)) : 0.f;
+    a.ramp30 = s > 0 ? (float)(1.0 / (1073741824.0 * s)) : 0.f;
 }
 
 // A new operator handle with its own stream, or a status.
@@ -561,7 +743,7 @@ int fair_mf_destroy(fair_mf A) {
     cudaStreamSynchronize(A->stream);
     for (fair::DevBuf *d : {&A->ang, &A->fang, &A->oms, &A->omj, &A->w_in, &A->w_out, &A->v_a,
                             &A->v_b, &A->M_sart, &A->M_cim, &A->D, &A->x32, &A->r, &A->w_b,
-                            &A->w_x})
+                            &A->w_x, &A->xt})
         d->release();
     if (A->own_stream) cudaStreamDestroy(A->stream);
     delete A;
@@ -599,6 +781,7 @@ static int mf_apply(fair_mf A, bool back, const double *in, double *out) {
     cudaStream_t s = A->stream;
     FAIR_TRY(A->w_in.grow(sizeof(double) * (nin + 1)));
     FAIR_TRY(A->w_out.grow(sizeof(double) * (nout + 1)));
+    if (!back) FAIR_TRY(fair::mf_grow_xt(A));
     FAIR_CUDA(cudaMemcpyAsync(A->w_in.p, in, sizeof(double) * nin, cudaMemcpyHostToDevice, s));
     if (A->prec == FAIR_PREC_F64) {
         fair::EpiStore<double> e{A->w_out.as<double>()};
@@ -664,6 +847,7 @@ int fair_mf_sirt_prepare(fair_mf A, const char *sirt_method, const fair_opts *op
     const bool red = A->prec != FAIR_PREC_F64;
     FAIR_TRY(A->r.grow((red ? sizeof(float) : sizeof(double)) * (m + 1)));
     if (red) FAIR_TRY(A->x32.grow(sizeof(float) * (n + 1)));
+    FAIR_TRY(fair::mf_grow_xt(A));
     FAIR_TRY(fair::mf_weights(A, sart, A->stream));
     FAIR_CUDA(cudaStreamSynchronize(A->stream));
     A->ready = true;
