@@ -379,29 +379,42 @@ struct MfFanAngle {
     float px, py, ux, uy;
 };
 
+// The sorted bin angles oms and, for a uniform grid of L cells over
+// [oms[0], oms[p-1]], the first sorted index at or past each cell's start
+// (tab[L] = p): the search for an angle starts one cell before the cell it
+// falls in (the last cell past the grid), whose start lies below it, and
+// steps forward.
+struct MfBins {
+    const float *oms;
+    const int *omj;
+    const int *tab;
+    float om0, inv_cell;
+    int L;
+    // the first k with oms[k] >= lo
+    __device__ __forceinline__ int first(float lo, int p) const {
+        const float t = (lo - om0) * inv_cell;
+        const int k = t < 1.f ? 0 : (t >= (float)L ? L - 1 : (int)t - 1);
+        int a = __ldg(tab + k);
+        while (a < p && __ldg(oms + a) < lo) ++a;
+        return a;
+    }
+};
+
 // The rays of angle i through pixel (ix, iy): bin angles within the pixel's
 // angular half-width of its centre's angle from the source (oms sorted, omj
 // their bins), each tested with the exact fixed-point distance.
 template <typename YT, typename ACC, int MODE>
 __device__ __forceinline__ void bp_fan_rays(const MfAngle *__restrict__ rays, const MfFanAngle &F,
-                                            const float *__restrict__ oms,
-                                            const int *__restrict__ omj, int i, int p, int ix,
-                                            int iy, float cx, float cy, const YT *__restrict__ y,
-                                            ACC &acc) {
+                                            const MfBins &B, int i, int p, int ix, int iy, float cx,
+                                            float cy, const YT *__restrict__ y, ACC &acc) {
     const float vx = cx - F.px, vy = cy - F.py;
     const float al = atan2f(fmaf(F.ux, vy, -F.uy * vx), fmaf(F.ux, vx, F.uy * vy));
     const float de = asinf(fminf(1.f, 0.7072f * rsqrtf(fmaf(vx, vx, vy * vy)))) + 2e-4f;
     const float lo = al - de, hi = al + de;
-    int a = 0, b = p;  // first k with oms[k] >= lo
-    while (a < b) {
-        const int mid = (a + b) >> 1;
-        if (__ldg(oms + mid) < lo) a = mid + 1;
-        else b = mid;
-    }
-    for (int k = a; k < p && __ldg(oms + k) <= hi; ++k) {
-        const int j = __ldg(omj + k);
+    for (int k = B.first(lo, p); k < p && __ldg(B.oms + k) <= hi; ++k) {
+        const int j = __ldg(B.omj + k);
         const int64_t r = (int64_t)i * p + j;
-        const MfAngle &A = rays[r];
+        const MfAngle A = mf_load<ACC>(rays + r);
         const long long d = (long long)ix * A.C + (long long)iy * A.S + A.K;
         const ACC w = Chord<ACC>::of(A, d);
         if (w > (ACC)0) {
@@ -413,9 +426,8 @@ __device__ __forceinline__ void bp_fan_rays(const MfAngle *__restrict__ rays, co
 
 template <typename YT, typename ACC, int MODE, class Epi>
 __global__ void __launch_bounds__(128) k_mf_backproject_fan(
-        const MfAngle *__restrict__ rays, const MfFanAngle *__restrict__ fa,
-        const float *__restrict__ oms, const int *__restrict__ omj, int nth, int p, int N,
-        const YT *__restrict__ y, Epi epi) {
+        const MfAngle *__restrict__ rays, const MfFanAngle *__restrict__ fa, MfBins B, int nth,
+        int p, int N, const YT *__restrict__ y, Epi epi) {
     const int half = (N + 1) / 2;  // pixel pairs per image column
     const int64_t npairs = (int64_t)N * half;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < npairs;
@@ -428,8 +440,8 @@ __global__ void __launch_bounds__(128) k_mf_backproject_fan(
         ACC acc0 = 0, acc1 = 0;
         for (int i = 0; i < nth; ++i) {
             const MfFanAngle F = fa[i];
-            bp_fan_rays<YT, ACC, MODE>(rays, F, oms, omj, i, p, ix, iy0, cx, cy0, y, acc0);
-            if (two) bp_fan_rays<YT, ACC, MODE>(rays, F, oms, omj, i, p, ix, iy0 - 1, cx, cy0 - 1.f, y, acc1);
+            bp_fan_rays<YT, ACC, MODE>(rays, F, B, i, p, ix, iy0, cx, cy0, y, acc0);
+            if (two) bp_fan_rays<YT, ACC, MODE>(rays, F, B, i, p, ix, iy0 - 1, cx, cy0 - 1.f, y, acc1);
         }
         const int64_t q0 = (int64_t)ix * N + 2 * k;
         epi(q0, acc0);
@@ -455,7 +467,10 @@ struct fair_mf_s {
     int N = 0, p = 0, nth = 0;
     int kind = 0;                      // 0: parallel beam, 1: fan beam
     fair::DevBuf ang;                  // MfAngle [nth] (parallel) or [nth*p] (fan: per ray)
-    fair::DevBuf fang, oms, omj;       // fan: MfFanAngle [nth], sorted bin angles, their bins
+    fair::DevBuf fang, oms, omj, omt;  // fan: MfFanAngle [nth], sorted bin angles, their bins,
+                                       // first sorted index per cell of the angle grid
+    float om0 = 0.f, om_inv = 0.f;     // the grid: start, 1 / cell width, cells
+    int om_L = 1;
     fair::DevBuf w_in, w_out;          // host-call staging (FP64)
     fair::DevBuf xt;                   // the projector's transposed copy of x
     fair::DevBuf v_a, v_b;             // reduced-precision staging
@@ -502,8 +517,9 @@ void mf_backproject(fair_mf A, const YT *y, Epi epi, cudaStream_t s) {
     const MfAngle *ang = A->ang.as<MfAngle>();
     if (A->kind == 1)
         k_mf_backproject_fan<YT, ACC, MODE><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
-            ang, A->fang.as<MfFanAngle>(), A->oms.as<float>(), A->omj.as<int>(), A->nth, A->p,
-            A->N, y, epi);
+            ang, A->fang.as<MfFanAngle>(),
+            MfBins{A->oms.as<float>(), A->omj.as<int>(), A->omt.as<int>(), A->om0, A->om_inv, A->om_L},
+            A->nth, A->p, A->N, y, epi);
     else
         k_mf_backproject<YT, ACC, MODE, kMfPB><<<grid_for(n / kMfPB + A->N, 128), 128, 0, s>>>(
             ang, A->nth, A->p, A->N, y, epi);
@@ -728,8 +744,22 @@ int fair_mf_create_fan(fair_mf *out, const fair_data *dat, int32_t geometry_fix,
                      [&](int u, int v) { return (float)omega[u] < (float)omega[v]; });
     std::vector<float> oms(p);
     for (int k = 0; k < p; ++k) oms[k] = (float)omega[order[k]];
+    // a grid of 4p cells over the sorted angles; tab[c] = first k with oms[k] >=
+    // om0 + c / inv (the device starts one cell early and steps forward)
+    const int L = 4 * p;
+    const double span = (double)oms[p - 1] - (double)oms[0];
+    A->om0 = oms[0];
+    A->om_inv = span > 0 ? (float)(L / span) : 0.f;
+    A->om_L = L;
+    std::vector<int> tab(L + 1);
+    for (int c = 0, k = 0; c <= L; ++c) {
+        const double start = (double)oms[0] + (span > 0 ? c * span / L : 0.0);
+        while (k < p && (double)oms[k] < start) ++k;
+        tab[c] = c == L ? p : k;
+    }
     if (fair::mf_upload(A->ang, rays) != FAIR_OK || fair::mf_upload(A->fang, fa) != FAIR_OK ||
-        fair::mf_upload(A->oms, oms) != FAIR_OK || fair::mf_upload(A->omj, order) != FAIR_OK) {
+        fair::mf_upload(A->oms, oms) != FAIR_OK || fair::mf_upload(A->omj, order) != FAIR_OK ||
+        fair::mf_upload(A->omt, tab) != FAIR_OK) {
         fair_mf_destroy(A);
         *out = nullptr;
         return FAIR_ERR_ALLOC;
@@ -741,7 +771,7 @@ int fair_mf_destroy(fair_mf A) {
     if (!A) return FAIR_OK;
     cudaSetDevice(A->device);
     cudaStreamSynchronize(A->stream);
-    for (fair::DevBuf *d : {&A->ang, &A->fang, &A->oms, &A->omj, &A->w_in, &A->w_out, &A->v_a,
+    for (fair::DevBuf *d : {&A->ang, &A->fang, &A->oms, &A->omj, &A->omt, &A->w_in, &A->w_out, &A->v_a,
                             &A->v_b, &A->M_sart, &A->M_cim, &A->D, &A->x32, &A->r, &A->w_b,
                             &A->w_x, &A->xt})
         d->release();

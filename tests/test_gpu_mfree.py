@@ -110,3 +110,25 @@ def test_errors(fair):
     with pytest.raises(fair.FairError):
         M.prepare("landweber")
     M.close()
+
+
+@pytest.mark.parametrize("n,p", [(16, 23), (16, 24), (17, 25)])
+def test_axis_aligned_fp32_matches_fp64(fair, n, p):
+    """Rays at theta = 0, pi/2, pi, 3pi/2 are axis-aligned (their fixed-point
+    normal has a zero component): a ray on a grid line keeps the pixels on one
+    side, decided on the exact distance in both precisions, so the FP32
+    entries are the FP64 ones up to FP32 rounding (no pixel counted twice or
+    dropped) and the FP32 pair stays adjoint."""
+    th = np.array([0.0, np.pi / 2, np.pi, 1.5 * np.pi, np.pi / 4, 2.0])
+    d = fair.Data(n=n, p=p, nth=len(th), theta=th)
+    M64, M32 = fair.MatrixFree(d, "f64"), fair.MatrixFree(d, "f32")
+    rng = np.random.default_rng(n + p)
+    x, y = rng.random(n * n), rng.random(M64.m)
+    for v in (np.ones(n * n), x):
+        assert rel_err(M32.project(v), M64.project(v)) < 1e-6
+    for w in (np.ones(M64.m), y):
+        assert rel_err(M32.backproject(w), M64.backproject(w)) < 1e-6
+    lhs, rhs = M32.project(x) @ y, x @ M32.backproject(y)
+    assert abs(lhs - rhs) <= 2e-6 * abs(lhs)
+    M64.close()
+    M32.close()

@@ -102,3 +102,24 @@ def test_fan_sirt_matches_oracle(fair, oracle, method, prec, tol):
 def test_fan_beam_argument(fair):
     with pytest.raises(ValueError):
         fair.MatrixFree(fair.Data(n=8, p=10, nth=4, theta=np.zeros(4)), "f32", beam="cone")
+
+
+@pytest.mark.parametrize("n,p", [(24, 35), (26, 36)])
+def test_fan_fp32_matches_fp64(fair, n, p):
+    """Fan beam at theta = 2 pi k/8 (axis-aligned central rays included): the
+    FP32 entries are the FP64 ones up to FP32 rounding, and the FP32 pair is
+    adjoint."""
+    nth = 8
+    th = theta(nth, "plain")
+    d = fair.Data(n=n, p=p, nth=nth, r=2.0, dw=p / n, sd=2.0, theta=th)
+    M64, M32 = fair.MatrixFree(d, "f64", beam="fan"), fair.MatrixFree(d, "f32", beam="fan")
+    rng = np.random.default_rng(n)
+    x, y = rng.random(n * n), rng.random(M64.m)
+    for v in (np.ones(n * n), x):
+        assert rel_err(M32.project(v), M64.project(v)) < 1e-6
+    for w in (np.ones(M64.m), y):
+        assert rel_err(M32.backproject(w), M64.backproject(w)) < 1e-6
+    lhs, rhs = M32.project(x) @ y, x @ M32.backproject(y)
+    assert abs(lhs - rhs) <= 2e-6 * abs(lhs)
+    M64.close()
+    M32.close()
