@@ -1455,7 +1455,7 @@ int lvl_sweep(const SweepDev &S, int dir, const RowStep *steps, const Box &box, 
     // FP64 instructions per step (64 cycles each) are on the level's critical
     // path. Measured (GB300, 10 sweeps of fan N=128 on the cluster, s): G = 1
     // 0.061, 2 0.041, 4 0.036, 8 0.038; 20 sweeps of fan N=512 symmetric on
-    // the cooperative grid (s, blocks): G = 4 0.66 (102), 8 0.58 (51) / 0.52
+    // the cooperative grid (s, blocks): G = 4 0.66 (26), 8 0.58 (51) / 0.52
     // (152), 16 0.47 (101) / 0.42 (152). FAIR_SWEEP_GROUP overrides (1, 2, 4,
     // 8 or 16).
     const double avg = S.nord > 0 ? (double)C.entries / S.nord : 0.0;
