@@ -1227,7 +1227,9 @@ int lvl_launch_grid(int nb, const RowStep *sched, const int64_t *lptr, const int
 template <int CACHE, int NT>
 int lvl_grid_blocks(double spl, int G, int cs) {
     int want = (int)std::ceil(spl * 2.0 * G / (NT / 32));
-    const int forced = env_int("FAIR_SWEEP_GRID_BLOCKS", 0);  // measurements
+    // FAIR_SWEEP_GRID_BLOCKS sets the count instead (tuning measurements),
+    // still capped at the co-resident blocks
+    const int forced = env_int("FAIR_SWEEP_GRID_BLOCKS", 0);
     if (forced > 0) want = forced;
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_lvl_sweep<SYNC_GRID, XG, CACHE, NT>, NT, 0) !=
