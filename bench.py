@@ -521,6 +521,7 @@ def run_ours(args):
 
 
 SECONDARY = [  # (name, extra arguments, time limit in s): the other workloads of the path
+    ("c1_cimmino", ["--workload", "c1"], 300),
     ("kaczmarz", ["--workload", "kaczmarz", "--no-cpu"], 300),
     ("adjoint", ["--workload", "adjoint", "--no-cpu"], 300),
     ("batch", ["--workload", "batch", "--batch-layout", "auto", "--no-cpu"], 600),
@@ -529,11 +530,12 @@ SECONDARY = [  # (name, extra arguments, time limit in s): the other workloads o
 
 
 def run_secondary(args):
-    """The secondary workloads (Kaczmarz family, adjoint, batch, matrix-free and
-    stored FP32 at N=2048), each in a process of its own after the headline
-    run has freed its GPU memory; their JSON lines are collected here so that
-    one bench run records every workload. CPU baselines of these lines are
-    skipped (the headline line carries the CPU comparison)."""
+    """The secondary workloads (the fan N=128 Cimmino run, Kaczmarz family,
+    adjoint, batch, matrix-free and stored FP32 at N=2048), each in a process
+    of its own after the headline run has freed its GPU memory; their JSON
+    lines are collected here so that one bench run records every workload.
+    CPU baselines are skipped but for the Cimmino run (a few seconds; the
+    headline line carries the main CPU comparison)."""
     out = {}
     for name, extra, limit in SECONDARY:
         t0 = time.perf_counter()
@@ -547,6 +549,54 @@ def run_secondary(args):
         except subprocess.TimeoutExpired:
             out[name] = {"rc": None, "error": f"timed out after {limit} s"}
     return out
+
+
+def run_c1(args):
+    """The Cimmino run of the plain FP64 configuration (a secondary line): fan
+    beam N=128, 360 angles over [0, 2pi), 181 unit bins, source radius 2N,
+    Shepp-Logan phantom, 1% noise (seed 0), Cimmino SIRT for 100 iterations
+    with relaxation 1.9 and lower bound 0, FP64. Iterations/s through the host
+    call (b uploaded, x downloaded, the weights computed inside the call as the
+    reference does per call), beside the oracle's Cimmino on one core and on
+    all host threads (CPU time of the same 100 iterations), and the GPU
+    iterate's error against the oracle's."""
+    import fortran_airtools_gb300 as F
+    from oracle import oracle as O
+    n, nth, p, K = 128, 360, 181, 100
+    th = 2 * np.pi * np.arange(nth) / nth
+    d = F.Data(n=n, p=p, nth=nth, r=2.0, dw=p / n, sd=2.0, theta=th)
+    A = F.fanlineartomo(d)
+    m, ncol, nnz = A.info()
+    b = noisy(A.matvecmul(F.phantomgallery.shepplogan(n)), seed=0)
+    opts = F.airms.options(relaxpar=1.9, lbound=0.0)
+    F.airms.sirt("cimmino", A, b, [K], opts=opts)  # warm-up
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        x = F.airms.sirt("cimmino", A, b, [K], opts=opts)
+    gpu_s = (time.perf_counter() - t0) / reps
+    vA, IA, JA = A.arrays()
+    R = O.OracleCSR(m, ncol, IA, JA, vA)
+    ro = O.options(relaxpar=1.9, lbound=0.0)
+    nthreads = os.cpu_count() or 1
+    cpu = {}
+    xo = None
+    for label, nt in (("one_thread", 1), ("all_threads", nthreads)):
+        if args.no_cpu and label == "one_thread":
+            continue
+        t0 = time.perf_counter()
+        xo = O.sirt("cimmino", R, b, K, opts=ro, nthreads=nt)
+        cpu[label] = {"value": K / (time.perf_counter() - t0), "unit": "iter/s", "cores": nt}
+    head = cpu.get("one_thread", cpu["all_threads"])
+    line = {"metric": "cimmino iter/s (100 iterations)", "workload": f"fan N={n}, {nth} angles, {p} bins",
+            "value": K / gpu_s, "unit": "iter/s", "ms_per_call": gpu_s * 1e3, "iterations": K,
+            "nnz": nnz, "dtype": "f64", "rel_err_vs_oracle": float(np.linalg.norm(x - xo) / np.linalg.norm(xo)),
+            "note": "fair_sirt host call: b uploaded, x downloaded, weights computed in the call",
+            "cpu_baseline": {"value": head["value"], "unit": "iter/s", "cores": head["cores"], "kind": "port",
+                             "sample": f"{K} iterations of the same problem", "variants": cpu}}
+    print(json.dumps(line), flush=True)
+    A.close()
+    return 0
 
 
 def run_kaczmarz(args):
@@ -1042,9 +1092,9 @@ def main():
     ap.add_argument("--n", type=int, default=1024, help="image size N (profiling cases)")
     ap.add_argument("--angles", type=int, default=720)
     ap.add_argument("--bins", type=int, default=1448)
-    ap.add_argument("--workload", choices=["sirt", "kaczmarz", "adjoint", "batch", "mfree"],
+    ap.add_argument("--workload", choices=["sirt", "c1", "kaczmarz", "adjoint", "batch", "mfree"],
                     default="sirt",
-                    help="sirt: the headline line; kaczmarz, adjoint, batch, mfree: secondary lines")
+                    help="sirt: the headline line; c1, kaczmarz, adjoint, batch, mfree: secondary lines")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--batch-prec", choices=["f64", "f32", "f16", "q16"], default="f32")
     ap.add_argument("--batch-layout", default="auto,tiled,packed",
@@ -1066,6 +1116,8 @@ def main():
     WORKLOAD = (f"parallel-beam N={N}, {NTH} angles over [0,pi), {P} bins; SIRT (Cimmino)")
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "c1":
+        return run_c1(args)
     if args.workload == "kaczmarz":
         return run_kaczmarz(args)
     if args.workload == "batch":

@@ -172,6 +172,59 @@ template <> struct VLoad<int16_t, float> {
 // Row sums of one chunk (rows base..base+31): returns, in lane l, the sum of
 // row base+l. All lanes of the warp call it together.
 // VT: stored value type; XT: gathered vector type; ACC: accumulator type.
+// The sum of row `row` (0 past m) by the G lanes of its group, gl the lane's
+// place in the group: each lane takes the 4-entry groups at (s & ~3) + 4 gl,
+// then every 4 G entries, adding each group's products in order; the group's
+// butterfly leaves the sum in every lane of the group.
+template <typename VT, typename XT, typename ACC, int G>
+__device__ __forceinline__ ACC csr_row_sum(const int64_t *__restrict__ rowptr, int32_t m,
+                                           const int32_t *__restrict__ col,
+                                           const VT *__restrict__ val,
+                                           const XT *__restrict__ x, int64_t row, int gl) {
+    int64_t s = 0, e = 0;
+    if (row < m) {
+        s = __ldg(rowptr + row);
+        e = __ldg(rowptr + row + 1);
+    }
+    ACC acc = 0;
+    int64_t k = (s & ~(int64_t)3) + 4 * gl;
+    int4 cc = make_int4(0, 0, 0, 0);
+    ACC vv[4] = {0, 0, 0, 0};
+    if (k < e) {
+        cc = ld_stream(reinterpret_cast<const int4 *>(col + k));
+        VLoad<VT, ACC>::ld(val + k, vv);
+    }
+    while (k < e) {
+        const int64_t kn = k + 4 * G;
+        int4 cn = make_int4(0, 0, 0, 0);
+        ACC vn[4] = {0, 0, 0, 0};
+        if (kn < e) {
+            cn = ld_stream(reinterpret_cast<const int4 *>(col + kn));
+            VLoad<VT, ACC>::ld(val + kn, vn);
+        }
+        if (k >= s && k + 3 < e) {
+            acc += (ACC)__ldg(x + cc.x) * vv[0];
+            acc += (ACC)__ldg(x + cc.y) * vv[1];
+            acc += (ACC)__ldg(x + cc.z) * vv[2];
+            acc += (ACC)__ldg(x + cc.w) * vv[3];
+        } else {
+            if (k >= s && k < e) acc += (ACC)__ldg(x + cc.x) * vv[0];
+            if (k + 1 >= s && k + 1 < e) acc += (ACC)__ldg(x + cc.y) * vv[1];
+            if (k + 2 >= s && k + 2 < e) acc += (ACC)__ldg(x + cc.z) * vv[2];
+            if (k + 3 >= s && k + 3 < e) acc += (ACC)__ldg(x + cc.w) * vv[3];
+        }
+        cc = cn;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) vv[t] = vn[t];
+        k = kn;
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
+}
+
+// The sums of the 32 rows of a chunk, row base + lane in lane `lane`: 32/G
+// rows at a time, one per group of G lanes.
 template <typename VT, typename XT, typename ACC, int G>
 __device__ __forceinline__ ACC csr_chunk_sums(const int64_t *__restrict__ rowptr, int32_t m,
                                               const int32_t *__restrict__ col,
@@ -182,46 +235,7 @@ __device__ __forceinline__ ACC csr_chunk_sums(const int64_t *__restrict__ rowptr
     ACC mine = 0;
 #pragma unroll 1
     for (int sub = 0; sub < 32; sub += R) {
-        const int64_t row = base + sub + g;
-        int64_t s = 0, e = 0;
-        if (row < m) {
-            s = __ldg(rowptr + row);
-            e = __ldg(rowptr + row + 1);
-        }
-        ACC acc = 0;
-        int64_t k = (s & ~(int64_t)3) + 4 * gl;
-        int4 cc = make_int4(0, 0, 0, 0);
-        ACC vv[4] = {0, 0, 0, 0};
-        if (k < e) {
-            cc = ld_stream(reinterpret_cast<const int4 *>(col + k));
-            VLoad<VT, ACC>::ld(val + k, vv);
-        }
-        while (k < e) {
-            const int64_t kn = k + 4 * G;
-            int4 cn = make_int4(0, 0, 0, 0);
-            ACC vn[4] = {0, 0, 0, 0};
-            if (kn < e) {
-                cn = ld_stream(reinterpret_cast<const int4 *>(col + kn));
-                VLoad<VT, ACC>::ld(val + kn, vn);
-            }
-            if (k >= s && k + 3 < e) {
-                acc += (ACC)__ldg(x + cc.x) * vv[0];
-                acc += (ACC)__ldg(x + cc.y) * vv[1];
-                acc += (ACC)__ldg(x + cc.z) * vv[2];
-                acc += (ACC)__ldg(x + cc.w) * vv[3];
-            } else {
-                if (k >= s && k < e) acc += (ACC)__ldg(x + cc.x) * vv[0];
-                if (k + 1 >= s && k + 1 < e) acc += (ACC)__ldg(x + cc.y) * vv[1];
-                if (k + 2 >= s && k + 2 < e) acc += (ACC)__ldg(x + cc.z) * vv[2];
-                if (k + 3 >= s && k + 3 < e) acc += (ACC)__ldg(x + cc.w) * vv[3];
-            }
-            cc = cn;
-#pragma unroll
-            for (int t = 0; t < 4; ++t) vv[t] = vn[t];
-            k = kn;
-        }
-#pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        const ACC acc = csr_row_sum<VT, XT, ACC, G>(rowptr, m, col, val, x, base + sub + g, gl);
         ACC r = __shfl_sync(0xffffffffu, acc, ((lane - sub) & (R - 1)) * G);
         if (lane >= sub && lane < sub + R) mine = r;
     }
@@ -248,6 +262,27 @@ __device__ __forceinline__ void chunk_rows(const int64_t *__restrict__ rowptr, i
         if (row < m) epi(row, mine);
     }
     finish_chunks(sched, nwarps, lane);
+}
+
+// The same row sums with each warp taking one group of 32/G consecutive rows
+// at a time instead of a chunk of 32: G times the warps for the same rows, the
+// same arithmetic per row (csr_row_sum), so the same results bit for bit.
+// For matrices with too few 32-row chunks to fill the GPU.
+template <typename VT, typename XT, typename ACC, int G, class Epi>
+__device__ __forceinline__ void rows_by_group(const int64_t *__restrict__ rowptr, int32_t m,
+                                              const int32_t *__restrict__ col,
+                                              const VT *__restrict__ val,
+                                              const XT *__restrict__ x, Epi &epi) {
+    constexpr int R = 32 / G;
+    const int lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nunits = ((int64_t)m + R - 1) / R;
+    for (int64_t u = warp; u < nunits; u += nwarps) {
+        const int64_t row = u * R + g;
+        const ACC acc = csr_row_sum<VT, XT, ACC, G>(rowptr, m, col, val, x, row, gl);
+        if (gl == 0 && row < m) epi(row, acc);
+    }
 }
 
 // ---- packed index stream ------------------------------------------------------

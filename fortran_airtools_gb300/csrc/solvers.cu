@@ -80,6 +80,14 @@ __global__ void __launch_bounds__(256) k_sirt_resid_f64(const int64_t *rowptr, i
                                                         unsigned *sched) {
     chunk_rows<double, double, double, G>(rowptr, m, col, v, x, epi, sched);
 }
+// Matrices with few rows: a group of 32/G rows per warp (rows_by_group, the
+// same per-row arithmetic as the chunked kernels above).
+template <int G, class Epi>
+__global__ void __launch_bounds__(256) k_sirt_rows_f64(const int64_t *rowptr, int32_t m,
+                                                       const int32_t *col, const double *v,
+                                                       const double *x, Epi epi) {
+    rows_by_group<double, double, double, G>(rowptr, m, col, v, x, epi);
+}
 template <typename VT, int G>
 __global__ void __launch_bounds__(256) k_sirt_resid_lp(const int64_t *rowptr, int32_t m,
                                                        const int32_t *col, const VT *v,
@@ -457,6 +465,24 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
         }
         const int64_t *rp = M.rowptr.as<int64_t>();
         const int32_t *cl = M.col.as<int32_t>();
+        // fewer 32-row chunks than 16 warps per SM: a group of rows per warp
+        if (((int64_t)M.m + 31) / 32 < (int64_t)sm_count() * 16) {
+            auto go = [&](auto kern, const double *xv, const auto &e) {
+                int occ = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, 0);
+                const int64_t units = ((int64_t)M.m * G + 31) / 32;  // groups of 32/G rows
+                const int64_t blocks = std::min<int64_t>((units + 7) / 8, (int64_t)sm_count() * std::max(occ, 1));
+                kern<<<(int)std::max<int64_t>(blocks, 1), 256, 0, s>>>(rp, M.m, cl, M.v64.as<double>(), xv, e);
+            };
+            if (pass == 1) {
+                const EpiResidF64 e{S.b, S.Minv, (double *)S.r};
+                FAIR_G_DISPATCH(G, go(k_sirt_rows_f64<g_, EpiResidF64>, S.x, e));
+            } else {
+                const EpiUpdateF64 e{S.D, S.x, S.omg, S.lb, S.ub, S.bmode};
+                FAIR_G_DISPATCH(G, go(k_sirt_rows_f64<g_, EpiUpdateF64>, (const double *)S.r, e));
+            }
+            return;
+        }
         if (pass == 1) {
             EpiResidF64 e{S.b, S.Minv, (double *)S.r};
             FAIR_G_DISPATCH(G, (k_sirt_resid_f64<g_><<<chunk_grid(k_sirt_resid_f64<g_>, M.m), 256, 0, s>>>(
