@@ -986,10 +986,15 @@ __device__ __forceinline__ void lvl_row(const RowStep &st, const int32_t *__rest
 // chunks are loaded one level ahead (in registers). With x in
 // (distributed) shared memory (XM = XS or XD, cb = log2 of a block's part), x
 // is loaded at the start and written back at the end.
-// A barrier of all blocks of a cooperative launch: gbar[0] counts the
-// arrivals, gbar[1] is the generation the last arrival advances (both zero at
-// the launch). A block that waits more than kGridSpinLimit polls sets *gerr
-// and returns false; the sweep then stops, and the host reports the error.
+// A barrier of all blocks of a cooperative launch on one counter, gbar[0]
+// (zero at the launch): block 0 adds 2^31 - (blocks - 1), every other block
+// 1, so the counter's top bit flips exactly when the last block arrives -- one
+// atomic per block and nothing to reset (the counter wraps). The arrival
+// follows a fence (the block's writes of the level are visible first); the
+// waiting thread reads the counter with acquire semantics. A block that waits
+// more than kGridSpinLimit polls, or sees *gerr set (checked every 1024
+// polls), sets *gerr and returns false; the sweep then stops, and the host
+// reports the error.
 constexpr unsigned long long kGridSpinLimit = 1ull << 26;
 enum { SYNC_BLOCK = 0, SYNC_CLUSTER = 1, SYNC_GRID = 2 };
 
@@ -997,26 +1002,21 @@ __device__ __forceinline__ bool grid_barrier(unsigned *gbar, int *gerr) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *gen = gbar + 1;
-        const unsigned g = *gen;
+        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
         int ok = 1;
         __threadfence();
-        if (atomicAdd(gbar, 1u) == gridDim.x - 1) {
-            gbar[0] = 0u;  // nobody arrives again before the generation moves
-            __threadfence();
-            atomicAdd(gbar + 1, 1u);
-        } else {
-            unsigned long long it = 0;
-            while (*gen == g) {
-                if (++it > kGridSpinLimit || *(volatile int *)gerr) {
-                    atomicExch(gerr, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
+        const unsigned old = atomicAdd(gbar, add);
+        for (unsigned long long it = 1;; ++it) {
+            unsigned cur;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(gbar) : "memory");
+            if ((cur ^ old) & 0x80000000u) break;
+            if ((it & 1023u) == 0 && (it > kGridSpinLimit || *(volatile int *)gerr)) {
+                atomicExch(gerr, 1);
+                ok = 0;
+                break;
             }
+            __nanosleep(32);
         }
-        __threadfence();
         ok_s = ok;
     }
     __syncthreads();
@@ -1192,7 +1192,7 @@ int lvl_launch_cluster(int cs, size_t smem, const RowStep *sched, const int64_t 
 // FAIR_SWEEP_CLUSTER caps the cluster size (1: one block), FAIR_SWEEP_XMEM
 // picks x's place (0: global, 1: shared/distributed).
 // The level sweep on a cooperative grid of nb blocks (x in global memory, the
-// software grid barrier between levels); gsync: {count, generation, error}.
+// software grid barrier between levels); gsync: {barrier counter, unused, error}.
 template <int CACHE, int NT>
 int lvl_launch_grid(int nb, const RowStep *sched, const int64_t *lptr, const int *nlev,
                     const int32_t *col, const double *val, double *x, int32_t n, const Box &box,
