@@ -402,15 +402,30 @@ struct MfBins {
 
 // The rays of angle i through pixel (ix, iy): bin angles within the pixel's
 // angular half-width of its centre's angle from the source (oms sorted, omj
-// their bins), each tested with the exact fixed-point distance.
-template <typename YT, typename ACC, int MODE>
+// their bins), each tested with the exact fixed-point distance. TANK: the
+// keys are tan(bin angle) (a source at least 1.42 N from the centre: every
+// pixel lies within 30 degrees of the central ray, where tan is monotone), and
+// the window is the tangent of the angle window, t = tan(alpha) = cross/dot
+// and tan(de) = 0.7072/sqrt(|v|^2 - 0.7072^2) + 2.5e-4 combined by the
+// tangent addition formula -- no arctangent or arcsine.
+template <typename YT, typename ACC, int MODE, bool TANK>
 __device__ __forceinline__ void bp_fan_rays(const MfAngle *__restrict__ rays, const MfFanAngle &F,
                                             const MfBins &B, int i, int p, int ix, int iy, float cx,
                                             float cy, const YT *__restrict__ y, ACC &acc) {
     const float vx = cx - F.px, vy = cy - F.py;
-    const float al = atan2f(fmaf(F.ux, vy, -F.uy * vx), fmaf(F.ux, vx, F.uy * vy));
-    const float de = asinf(fminf(1.f, 0.7072f * rsqrtf(fmaf(vx, vx, vy * vy)))) + 2e-4f;
-    const float lo = al - de, hi = al + de;
+    const float cr = fmaf(F.ux, vy, -F.uy * vx), dt = fmaf(F.ux, vx, F.uy * vy);
+    float lo, hi;
+    if constexpr (TANK) {
+        const float t = __fdividef(cr, dt);
+        const float tau = 0.7072f * rsqrtf(fmaf(vx, vx, fmaf(vy, vy, -0.50014f))) + 2.5e-4f;
+        lo = __fdividef(t - tau, fmaf(t, tau, 1.f));
+        hi = __fdividef(t + tau, fmaf(-t, tau, 1.f));
+    } else {
+        const float al = atan2f(cr, dt);
+        const float de = asinf(fminf(1.f, 0.7072f * rsqrtf(fmaf(vx, vx, vy * vy)))) + 2e-4f;
+        lo = al - de;
+        hi = al + de;
+    }
     for (int k = B.first(lo, p); k < p && __ldg(B.oms + k) <= hi; ++k) {
         const int j = __ldg(B.omj + k);
         const int64_t r = (int64_t)i * p + j;
@@ -424,7 +439,7 @@ __device__ __forceinline__ void bp_fan_rays(const MfAngle *__restrict__ rays, co
     }
 }
 
-template <typename YT, typename ACC, int MODE, class Epi>
+template <typename YT, typename ACC, int MODE, bool TANK, class Epi>
 __global__ void __launch_bounds__(128) k_mf_backproject_fan(
         const MfAngle *__restrict__ rays, const MfFanAngle *__restrict__ fa, MfBins B, int nth,
         int p, int N, const YT *__restrict__ y, Epi epi) {
@@ -440,8 +455,8 @@ __global__ void __launch_bounds__(128) k_mf_backproject_fan(
         ACC acc0 = 0, acc1 = 0;
         for (int i = 0; i < nth; ++i) {
             const MfFanAngle F = fa[i];
-            bp_fan_rays<YT, ACC, MODE>(rays, F, B, i, p, ix, iy0, cx, cy0, y, acc0);
-            if (two) bp_fan_rays<YT, ACC, MODE>(rays, F, B, i, p, ix, iy0 - 1, cx, cy0 - 1.f, y, acc1);
+            bp_fan_rays<YT, ACC, MODE, TANK>(rays, F, B, i, p, ix, iy0, cx, cy0, y, acc0);
+            if (two) bp_fan_rays<YT, ACC, MODE, TANK>(rays, F, B, i, p, ix, iy0 - 1, cx, cy0 - 1.f, y, acc1);
         }
         const int64_t q0 = (int64_t)ix * N + 2 * k;
         epi(q0, acc0);
@@ -471,6 +486,7 @@ struct fair_mf_s {
                                        // first sorted index per cell of the angle grid
     float om0 = 0.f, om_inv = 0.f;     // the grid: start, 1 / cell width, cells
     int om_L = 1;
+    bool tan_keys = false;             // oms holds tan(bin angle) (the backprojector's TANK)
     fair::DevBuf w_in, w_out;          // host-call staging (FP64)
     fair::DevBuf xt;                   // the projector's transposed copy of x
     fair::DevBuf v_a, v_b;             // reduced-precision staging
@@ -515,11 +531,15 @@ template <typename YT, typename ACC, int MODE, class Epi>
 void mf_backproject(fair_mf A, const YT *y, Epi epi, cudaStream_t s) {
     const int64_t n = (int64_t)A->N * A->N;
     const MfAngle *ang = A->ang.as<MfAngle>();
-    if (A->kind == 1)
-        k_mf_backproject_fan<YT, ACC, MODE><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
-            ang, A->fang.as<MfFanAngle>(),
-            MfBins{A->oms.as<float>(), A->omj.as<int>(), A->omt.as<int>(), A->om0, A->om_inv, A->om_L},
-            A->nth, A->p, A->N, y, epi);
+    if (A->kind == 1) {
+        const MfBins B{A->oms.as<float>(), A->omj.as<int>(), A->omt.as<int>(), A->om0, A->om_inv, A->om_L};
+        if (A->tan_keys)
+            k_mf_backproject_fan<YT, ACC, MODE, true><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
+                ang, A->fang.as<MfFanAngle>(), B, A->nth, A->p, A->N, y, epi);
+        else
+            k_mf_backproject_fan<YT, ACC, MODE, false><<<grid_for(n / 2 + 1, 128), 128, 0, s>>>(
+                ang, A->fang.as<MfFanAngle>(), B, A->nth, A->p, A->N, y, epi);
+    }
     else
         k_mf_backproject<YT, ACC, MODE, kMfPB><<<grid_for(n / kMfPB + A->N, 128), 128, 0, s>>>(
             ang, A->nth, A->p, A->N, y, epi);
@@ -742,8 +762,14 @@ int fair_mf_create_fan(fair_mf *out, const fair_data *dat, int32_t geometry_fix,
     for (int j = 0; j < p; ++j) order[j] = j;
     std::stable_sort(order.begin(), order.end(),
                      [&](int u, int v) { return (float)omega[u] < (float)omega[v]; });
+    // keys: tan of the bin angles when the source is at least 1.42 N from the
+    // centre (every pixel within 30 degrees of the central ray) and every bin
+    // angle below 1.5 rad, else the angles
+    bool tk = R >= 1.42 * N;
+    for (int j = 0; j < p; ++j) tk = tk && std::fabs(omega[j]) < 1.5;
+    A->tan_keys = tk;
     std::vector<float> oms(p);
-    for (int k = 0; k < p; ++k) oms[k] = (float)omega[order[k]];
+    for (int k = 0; k < p; ++k) oms[k] = (float)(tk ? std::tan(omega[order[k]]) : omega[order[k]]);
     // a grid of 4p cells over the sorted angles; tab[c] = first k with oms[k] >=
     // om0 + c / inv (the device starts one cell early and steps forward)
     const int L = 4 * p;
