@@ -14,6 +14,7 @@
 // are evaluated on the GPU: a flag set by a one-block kernel gates the later
 // kernels, so the host enqueues all iterations without synchronising.
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 #include "fair_internal.cuh"
@@ -466,7 +467,9 @@ void sirt_pass(const SirtDev &S, int pass, cudaStream_t s) {
         const int64_t *rp = M.rowptr.as<int64_t>();
         const int32_t *cl = M.col.as<int32_t>();
         // fewer 32-row chunks than 16 warps per SM: a group of rows per warp
-        if (((int64_t)M.m + 31) / 32 < (int64_t)sm_count() * 16) {
+        // (FAIR_ROWS_BY_GROUP=0: the chunked engine for every matrix)
+        const char *bg = getenv("FAIR_ROWS_BY_GROUP");
+        if (!(bg && bg[0] == '0') && ((int64_t)M.m + 31) / 32 < (int64_t)sm_count() * 16) {
             auto go = [&](auto kern, const double *xv, const auto &e) {
                 int occ = 0;
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, 0);

@@ -55,6 +55,33 @@ def test_sirt(par, fair, oracle, method, bounds):
     assert rel_err(x, xr) < TOL64
 
 
+def test_rows_by_group_equals_chunked(par, fair, monkeypatch):
+    """A matrix with few 32-row chunks (8,640 rays, 4,096 pixels) runs its FP64
+    CSR passes a group of rows per warp; the chunked engine
+    (FAIR_ROWS_BY_GROUP=0) has the same arithmetic per row: the same bits."""
+    A, R, _, b = par
+    o = fair.airms.options(relaxpar=1.5, lbound=0.0)
+    x1 = fair.airms.sirt("cimmino", A, b, 10, opts=o)
+    monkeypatch.setenv("FAIR_ROWS_BY_GROUP", "0")
+    x2 = fair.airms.sirt("cimmino", A, b, 10, opts=o)
+    assert np.array_equal(x1, x2)
+
+
+def test_fp64_csr_many_rows(fair, oracle):
+    """Parallel N=96, 720 angles, 136 bins: 97,920 rays, enough 32-row chunks
+    for the chunked engine on A (A' still a group of rows per warp)."""
+    n, nth, p = 96, 720, 136
+    th = np.pi * np.arange(nth) / nth
+    A = fair.paralleltomo(fair.Data(n=n, p=p, nth=nth, theta=th))
+    R = oracle.paralleltomo(n, nth, p, th)
+    b = oracle.matvecmul(R, oracle.shepplogan(n))
+    for method in ("cimmino", "sart"):
+        x = fair.airms.sirt(method, A, b, 5, opts=fair.airms.options(lbound=0.0))
+        xr = oracle.sirt(method, R, b, 5, opts=oracle.options(lbound=0.0))
+        assert rel_err(x, xr) < TOL64
+    A.close()
+
+
 def test_sirt_x0_and_defaults(par, fair, oracle):
     A, R, _, b = par
     x0 = np.full(R.n, 0.1)
