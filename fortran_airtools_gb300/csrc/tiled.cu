@@ -559,18 +559,27 @@ __device__ __forceinline__ void tl_fill_tile(const TlGeo &G, int4 U, const XT *_
             }
         }
     } else {  // W bins per angle of the tile's angle block, one cell per thread in
-              // turn (W is about 1.5 warps wide: a warp per angle would idle lanes)
+              // turn (W is about 1.5 warps wide: a warp per angle would idle lanes);
+              // the cell's angle and bin carried from step to step (no division)
         const int pt = U.x / G.nab, a0 = (U.x - pt * G.nab) * G.NA;
-        for (int e = threadIdx.x; e < G.NA * G.W; e += blockDim.x) {
-            const int ai = e / G.W, a = a0 + ai;
+        const int W = G.W, dai = (int)blockDim.x / W, dr = (int)blockDim.x - dai * W;
+        int ai = (int)threadIdx.x / W, r = (int)threadIdx.x - ai * W;
+        for (int e = threadIdx.x; e < G.NA * W; e += blockDim.x) {
+            const int a = a0 + ai;
             bool in = false;
             int b = 0;
             if (a < G.nth) {
-                b = __ldg(G.bmin + (int64_t)pt * G.nth + a) + (e - ai * G.W);
+                b = __ldg(G.bmin + (int64_t)pt * G.nth + a) + r;
                 in = b < G.p;
             }
             if (in) cp_async_elem(xs + e, x + (int64_t)a * G.p + b);
             else xs[e] = (XT)0;
+            ai += dai;
+            r += dr;
+            if (r >= W) {
+                r -= W;
+                ++ai;
+            }
         }
     }
     if (threadIdx.x == 0) xs[G.cells()] = (XT)0;  // the zero cell of padding entries
