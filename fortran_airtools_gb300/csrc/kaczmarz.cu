@@ -379,18 +379,23 @@ int sweep_warps() {
 // The levels are exact, computed per sweep order in windows of 32 steps:
 //   k_lvl_setup (every SM, windows in parallel): each entry swaps a stamp
 //     into its column's cell of the block's table; a stamp of an earlier step
-//     of the window makes the entry "shared" and sets that step's bit in this
-//     step's predecessor mask; the step's entries are written in groups
-//     [first touch in the window and last | first, not last | shared, not
-//     last | shared and last];
-//   k_lvl_levels (one block, windows in order): a step's level is the larger
-//     of 1 + the table's level over its first-touch columns and 1 + the level
-//     of each predecessor in its mask (a 32-lane recurrence); the last touches
-//     write the step's level into the table;
+//     of the window makes the entry "shared" and that step a predecessor; the
+//     step's entries are written in groups [first touch in the window and
+//     last | first, not last | shared, not last | shared and last], and the
+//     longest paths between the window's steps (predecessor chains) as one
+//     byte per pair;
+//   k_lvl_levels (one block; k_lvl_levels_cluster for tables that do not fit
+//     shared memory, on a 16-block cluster), windows in order: a step's level
+//     is the largest, over the steps a of its window with a path to it, of
+//     base(a) + the path's length, base(a) = 1 + the table's level over a's
+//     first-touch columns; the last touches write the levels into the table;
 //   counting sort of the steps by level (level pointers, steps in level order).
-// The sweep (k_lvl_sweep) runs on one thread-block cluster: a warp per step,
-// the steps of a level spread over the cluster's warps, a cluster barrier
-// between levels; x stays in global memory (L2), read past L1.
+// The sweep (k_lvl_sweep) runs a group of G warps per step, the steps of a
+// level spread over the groups, on one thread-block cluster (a cluster barrier
+// between levels; x in the cluster's distributed shared memory when its parts
+// fit, else in global memory read past L1) or, when a level outgrows the
+// cluster, on a cooperative grid of up to one block per SM (a software grid
+// barrier between levels; x in global memory).
 
 struct WinRow {
     int64_t off;              // first entry of the step in the grouped column array
